@@ -1,0 +1,171 @@
+/*
+ * lss.h -- C ABI of the GB300-native locally-stiff linear solver.
+ *
+ * One solver object = one polysolve `GPUHybrid` linear solver
+ * (src/polysolve/linear/GPUHybrid.hpp:27-192 in the reference), re-built for
+ * a single GB300: l1 row-norm scoring and 1D-GMM stiff-DOF selection, a
+ * multilevel additive Schwarz (MAS) preconditioner composed with a dense FP64
+ * factor of the stiff block, and FP64 PCG.  Hand-written sm_103a kernels.
+ *
+ * Conventions
+ *  - Matrices are Eigen-style compressed storage (`StiffnessMatrix`,
+ *    src/polysolve/Types.hpp:11-15): int32 outer[n+1], int32 inner[nnz],
+ *    double values[nnz].  As in the reference (GPUHybrid.cu:203-209, the CSC
+ *    arrays are handed to hypre as CSR) the outer index is the row; the matrix
+ *    must be symmetric positive definite, so CSC and CSR coincide.
+ *  - Host pointers in, host pointers out, unless a name ends in `_device`.
+ *  - Every entry point returns an lss_status and never exits the process
+ *    (the reference calls exit() on CUDA errors, GPUHybrid.cu:34-63).
+ *  - A solver is not thread-safe (the reference's objects are not copyable or
+ *    movable, Solver.hpp:8-12); use one solver per host thread.
+ *  - The device is selected by the "device" key of the "gb300" parameter
+ *    object (the reference hard-codes device 0, GPUHybrid.cu:96).
+ */
+#ifndef LSS_H
+#define LSS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lss_status {
+    LSS_OK = 0,
+    LSS_ERR_INVALID_ARGUMENT = 1,
+    LSS_ERR_CUDA = 2,
+    LSS_ERR_OOM = 3,
+    LSS_ERR_NOT_FACTORIZED = 4,
+    LSS_ERR_NOT_SPD = 5,          /* a MAS or stiff block has a zero / non-finite pivot */
+    LSS_ERR_NONFINITE = 6,        /* NaN or Inf in the matrix or right-hand side */
+    LSS_ERR_INTERNAL = 7,
+    LSS_ERR_BUFFER_TOO_SMALL = 8,
+    LSS_ERR_NO_DEVICE = 9,
+    LSS_ERR_UNSUPPORTED = 10
+} lss_status;
+
+typedef struct lss_solver lss_solver;
+
+/* Human-readable name of a status code. */
+const char *lss_status_string(lss_status s);
+
+/* Last error message of `s`; with s == NULL, of the last failed lss_create on
+ * this thread.  Valid until the next call on the same solver / thread. */
+const char *lss_last_error(const lss_solver *s);
+
+/* Solver::create(json) + GPUHybrid::GPUHybrid + set_parameters
+ * (Solver.cpp:143-173, GPUHybrid.cu:79-179).  params_json: the polysolve
+ * parameter object, e.g. {"solver": "GPUHybrid", "GPUHybrid": {...}} (the
+ * alias "GPUHybridSolver" is accepted; keys of linear-solver-spec.json:646-747,
+ * with that file's defaults), plus an optional "gb300" object for the
+ * extensions (precision, composition, ...).  NULL or "" = all defaults. */
+lss_status lss_create(const char *params_json, lss_solver **out);
+
+/* GPUHybrid::~GPUHybrid (GPUHybrid.cu:1514-1533). */
+lss_status lss_destroy(lss_solver *s);
+
+/* GPUHybrid::set_parameters (GPUHybrid.cu:106-179). */
+lss_status lss_set_parameters(lss_solver *s, const char *params_json);
+
+/* GPUHybrid::get_info (GPUHybrid.cu:181-185): writes a JSON object with
+ * "num_iterations" and "final_res_norm" (absolute ||b - A x||) plus extras.
+ * *len receives the full length (excluding the NUL); returns
+ * LSS_ERR_BUFFER_TOO_SMALL when cap <= *len. */
+lss_status lss_get_info(const lss_solver *s, char *buf, size_t cap, size_t *len);
+
+/* GPUHybrid::name (GPUHybrid.hpp:57-67): "GPUHybrid" / "GPUAMGF" / "GPUAMG". */
+lss_status lss_name(const lss_solver *s, char *buf, size_t cap);
+
+/* Solver::analyze_pattern (Solver.hpp:97; a no-op in GPUHybrid).  Here it
+ * partitions the block graph, builds the permuted BSR layout and the MAS
+ * coarse space once; factorize() with the same pattern reuses them. */
+lss_status lss_analyze_pattern(lss_solver *s, int32_t n, int64_t nnz, const int32_t *outer,
+                               const int32_t *inner);
+
+/* GPUHybrid::factorize (GPUHybrid.cu:195-282): stiff-DOF selection,
+ * subdomain post-processing, stiff-block factor, MAS setup.  Calls
+ * analyze_pattern itself when the pattern is new. */
+lss_status lss_factorize(lss_solver *s, int32_t n, int64_t nnz, const int32_t *outer,
+                         const int32_t *inner, const double *values);
+
+/* GPUHybrid::set_problematic_dofs (GPUHybrid.hpp:69): the DOF set used
+ * when select_bad_dofs_from_l1_norm is false.  idx need not be sorted. */
+lss_status lss_set_problematic_dofs(lss_solver *s, const int32_t *idx, int32_t count);
+
+/* GPUHybrid::solve (GPUHybrid.cu:342-399): x is the initial guess on entry
+ * (GPUHybrid.cu:347) and the solution on exit.  nrhs right-hand sides are
+ * stored column by column with leading dimension ld (>= n); they are solved
+ * one after the other.  Returns LSS_OK whether or not the tolerance was met
+ * (as the reference); lss_get_info reports the stop reason. */
+lss_status lss_solve(lss_solver *s, const double *b, double *x, int32_t nrhs, int64_t ld);
+
+/* Same as lss_solve with device pointers (one right-hand side), ordered on
+ * `stream` (a cudaStream_t, NULL = the legacy default stream).  Used by the
+ * PyTorch extension. */
+lss_status lss_solve_device(lss_solver *s, const double *d_b, double *d_x, void *stream);
+
+/* Backward of x = A^-1 b (no counterpart in the reference): solves
+ * A^T lambda = g with the same factorized hybrid preconditioner and PCG
+ * (A is SPD so A^T = A), writing lambda; lambda is the initial guess. */
+lss_status lss_solve_transpose(lss_solver *s, const double *g, double *lambda);
+
+/* dL/dA on A's pattern (no counterpart in the reference):
+ * dA_values[k] = -lambda[row(k)] * x[col(k)] for every stored entry k, with
+ * row = outer index and col = inner index, in the input's storage order. */
+lss_status lss_grad_A_pattern(lss_solver *s, const double *lambda, const double *x,
+                              double *dA_values);
+lss_status lss_grad_A_pattern_device(lss_solver *s, const double *d_lambda, const double *d_x,
+                                     double *d_dA_values, void *stream);
+
+/* The selected stiff DOF set after post-processing (the union of the stiff
+ * subdomains, ascending; GPUHybrid.cu:240-262 d_all_bad_dofs).  With
+ * out == NULL only *count is written. */
+lss_status lss_selected_dofs(const lss_solver *s, int32_t *out, int32_t cap, int32_t *count);
+
+/* The GMM stage's raw selection {i : gamma0_i < gamma1_i} before filter /
+ * expand / decompose (GPUHybrid.cu:859-879). */
+lss_status lss_gmm_selection(const lss_solver *s, int32_t *out, int32_t cap, int32_t *count);
+
+/* Stiff subdomains (GPUHybrid.cu:691-735 bad_indices_arrays): offsets[nsub+1]
+ * into dofs[]; each subdomain ascending, subdomains ordered by first DOF. */
+lss_status lss_subdomains(const lss_solver *s, int32_t *offsets, int32_t cap_offsets,
+                          int32_t *dofs, int32_t cap_dofs, int32_t *nsub, int32_t *ndofs);
+
+/* The partition behind the MAS preconditioner (MASSolver.cu:292-311):
+ * perm[old block row] = new block row (size n / block_size) and
+ * part_offsets[nparts+1] in the new numbering. */
+lss_status lss_partition(const lss_solver *s, int32_t *perm, int32_t cap_perm,
+                         int32_t *part_offsets, int32_t cap_offsets, int32_t *nparts);
+
+/* ---- operator-level entry points (parity tests and benchmarks) ---------- */
+
+/* rn[i] = sum |values| of outer slice i, on the GPU (GPUHybrid.cu:753-765). */
+lss_status lss_op_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer,
+                               const double *values, double *rn);
+
+/* y = A x with the factorized FP64 operator (original ordering). */
+lss_status lss_op_spmv(lss_solver *s, const double *x, double *y);
+
+/* z = MAS^-1 r alone (MASPreconditioner::apply, MASPreconditioner.cu:1099). */
+lss_status lss_op_mas_apply(lss_solver *s, const double *r, double *z);
+
+/* z = M^-1 r, the full hybrid preconditioner (GPUHybrid.cu:521-542 with
+ * MAS in place of BoomerAMG). */
+lss_status lss_op_precond(lss_solver *s, const double *r, double *z);
+
+/* Time `reps` launches of one kernel family on device-resident operands:
+ * kind 0 = FP64 SpMV, 1 = MAS apply, 2 = full preconditioner, 3 = one PCG
+ * iteration.  Writes the mean milliseconds per launch (CUDA events on the
+ * solver's stream) and the algorithmic bytes of one launch. */
+lss_status lss_op_time(lss_solver *s, int32_t kind, int32_t reps, double *ms_per_launch,
+                       double *bytes_per_launch);
+
+/* Cap device allocations of solvers created afterwards (bytes, 0 = none):
+ * exercises the out-of-memory path without exhausting the GPU. */
+lss_status lss_set_memory_cap(size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,298 @@
+// extern "C" entry points (include/lss.h).  Every call converts exceptions
+// into status codes and records the message; nothing here exits the process.
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "solver.hpp"
+
+namespace lss {
+size_t &alloc_cap_bytes()
+{
+    static size_t cap = 0;
+    return cap;
+}
+size_t &alloc_live_bytes()
+{
+    static size_t live = 0;
+    return live;
+}
+}  // namespace lss
+
+struct lss_solver {
+    lss::HybridSolver *impl = nullptr;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+template <typename F>
+lss_status guarded(lss_solver *s, F f)
+{
+    try {
+        f();
+        if (s) s->impl->last_error.clear();
+        return LSS_OK;
+    } catch (const lss::Error &e) {
+        if (s) s->impl->last_error = e.what();
+        else g_create_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        if (s) s->impl->last_error = "host allocation failed";
+        else g_create_error = "host allocation failed";
+        return LSS_ERR_OOM;
+    } catch (const std::exception &e) {
+        if (s) s->impl->last_error = e.what();
+        else g_create_error = e.what();
+        return LSS_ERR_INTERNAL;
+    }
+}
+
+bool valid(const lss_solver *s) { return s && s->impl; }
+
+lss_status copy_out(const std::string &src, char *buf, size_t cap, size_t *len)
+{
+    if (len) *len = src.size();
+    if (!buf || cap <= src.size()) {
+        if (buf && cap) buf[0] = '\0';
+        return LSS_ERR_BUFFER_TOO_SMALL;
+    }
+    std::memcpy(buf, src.c_str(), src.size() + 1);
+    return LSS_OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char *lss_status_string(lss_status s)
+{
+    switch (s) {
+    case LSS_OK: return "ok";
+    case LSS_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case LSS_ERR_CUDA: return "CUDA error";
+    case LSS_ERR_OOM: return "out of memory";
+    case LSS_ERR_NOT_FACTORIZED: return "not factorized";
+    case LSS_ERR_NOT_SPD: return "matrix block not positive definite";
+    case LSS_ERR_NONFINITE: return "non-finite input";
+    case LSS_ERR_INTERNAL: return "internal error";
+    case LSS_ERR_BUFFER_TOO_SMALL: return "buffer too small";
+    case LSS_ERR_NO_DEVICE: return "no CUDA device";
+    case LSS_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}
+
+const char *lss_last_error(const lss_solver *s)
+{
+    if (!s) return g_create_error.c_str();
+    if (!s->impl) return "invalid solver";
+    return s->impl->last_error.c_str();
+}
+
+lss_status lss_create(const char *params_json, lss_solver **out)
+{
+    if (!out) return LSS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    lss::HybridSolver *impl = nullptr;
+    lss_status st = guarded(nullptr, [&]() {
+        lss::Params p = lss::parse_params(params_json, lss::Params());
+        if (p.memory_cap_bytes) lss::alloc_cap_bytes() = p.memory_cap_bytes;
+        impl = new lss::HybridSolver(p);
+    });
+    if (st != LSS_OK) return st;
+    *out = new lss_solver{impl};
+    return LSS_OK;
+}
+
+lss_status lss_destroy(lss_solver *s)
+{
+    if (!s) return LSS_OK;
+    delete s->impl;
+    delete s;
+    return LSS_OK;
+}
+
+lss_status lss_set_parameters(lss_solver *s, const char *params_json)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->set_parameters(params_json); });
+}
+
+lss_status lss_get_info(const lss_solver *s, char *buf, size_t cap, size_t *len)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return copy_out(s->impl->info_json(), buf, cap, len);
+}
+
+lss_status lss_name(const lss_solver *s, char *buf, size_t cap)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return copy_out(s->impl->name(), buf, cap, nullptr);
+}
+
+lss_status lss_analyze_pattern(lss_solver *s, int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->analyze(n, nnz, outer, inner); });
+}
+
+lss_status lss_factorize(lss_solver *s, int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                         const double *values)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->factorize(n, nnz, outer, inner, values); });
+}
+
+lss_status lss_set_problematic_dofs(lss_solver *s, const int32_t *idx, int32_t count)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->set_problematic_dofs(idx, count); });
+}
+
+lss_status lss_solve(lss_solver *s, const double *b, double *x, int32_t nrhs, int64_t ld)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() {
+        if (nrhs < 0 || (nrhs > 1 && ld < s->impl->n())) lss::fail(LSS_ERR_INVALID_ARGUMENT, "invalid nrhs / ld");
+        for (int32_t k = 0; k < nrhs; ++k) s->impl->solve_host(b + (int64_t)k * ld, x + (int64_t)k * ld);
+    });
+}
+
+lss_status lss_solve_device(lss_solver *s, const double *d_b, double *d_x, void *stream)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->solve_device(d_b, d_x, (cudaStream_t)stream); });
+}
+
+lss_status lss_solve_transpose(lss_solver *s, const double *g, double *lambda)
+{
+    // A is symmetric positive definite: A^T lambda = g is the same system
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->solve_host(g, lambda); });
+}
+
+lss_status lss_grad_A_pattern(lss_solver *s, const double *lambda, const double *x, double *dA_values)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->grad_pattern_host(lambda, x, dA_values); });
+}
+
+lss_status lss_grad_A_pattern_device(lss_solver *s, const double *d_lambda, const double *d_x, double *d_dA_values,
+                                     void *stream)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->grad_pattern_device(d_lambda, d_x, d_dA_values, (cudaStream_t)stream); });
+}
+
+lss_status lss_selected_dofs(const lss_solver *s, int32_t *out, int32_t cap, int32_t *count)
+{
+    if (!valid(s) || !count) return LSS_ERR_INVALID_ARGUMENT;
+    const std::vector<int32_t> sel = s->impl->selected();
+    *count = (int32_t)sel.size();
+    if (!out) return LSS_OK;
+    if (cap < (int32_t)sel.size()) return LSS_ERR_BUFFER_TOO_SMALL;
+    std::memcpy(out, sel.data(), sel.size() * sizeof(int32_t));
+    return LSS_OK;
+}
+
+lss_status lss_gmm_selection(const lss_solver *s, int32_t *out, int32_t cap, int32_t *count)
+{
+    if (!valid(s) || !count) return LSS_ERR_INVALID_ARGUMENT;
+    const std::vector<int32_t> &sel = s->impl->gmm_selection();
+    *count = (int32_t)sel.size();
+    if (!out) return LSS_OK;
+    if (cap < (int32_t)sel.size()) return LSS_ERR_BUFFER_TOO_SMALL;
+    std::memcpy(out, sel.data(), sel.size() * sizeof(int32_t));
+    return LSS_OK;
+}
+
+lss_status lss_subdomains(const lss_solver *s, int32_t *offsets, int32_t cap_offsets, int32_t *dofs, int32_t cap_dofs,
+                          int32_t *nsub, int32_t *ndofs)
+{
+    if (!valid(s) || !nsub || !ndofs) return LSS_ERR_INVALID_ARGUMENT;
+    const auto &subs = s->impl->subdomains();
+    int64_t total = 0;
+    for (const auto &v : subs) total += (int64_t)v.size();
+    *nsub = (int32_t)subs.size();
+    *ndofs = (int32_t)total;
+    if (!offsets || !dofs) return LSS_OK;
+    if (cap_offsets < (int32_t)subs.size() + 1 || cap_dofs < total) return LSS_ERR_BUFFER_TOO_SMALL;
+    int32_t pos = 0;
+    offsets[0] = 0;
+    for (size_t k = 0; k < subs.size(); ++k) {
+        std::memcpy(dofs + pos, subs[k].data(), subs[k].size() * sizeof(int32_t));
+        pos += (int32_t)subs[k].size();
+        offsets[k + 1] = pos;
+    }
+    return LSS_OK;
+}
+
+lss_status lss_partition(const lss_solver *s, int32_t *perm, int32_t cap_perm, int32_t *part_offsets,
+                         int32_t cap_offsets, int32_t *nparts)
+{
+    if (!valid(s) || !nparts) return LSS_ERR_INVALID_ARGUMENT;
+    const auto &P = s->impl->pattern();
+    *nparts = P.part.part_offsets.empty() ? 0 : (int32_t)P.part.part_offsets.size() - 1;
+    if (!perm || !part_offsets) return LSS_OK;
+    if (cap_perm < (int32_t)P.part.perm.size() || cap_offsets < (int32_t)P.part.part_offsets.size())
+        return LSS_ERR_BUFFER_TOO_SMALL;
+    std::memcpy(perm, P.part.perm.data(), P.part.perm.size() * sizeof(int32_t));
+    std::memcpy(part_offsets, P.part.part_offsets.data(), P.part.part_offsets.size() * sizeof(int32_t));
+    return LSS_OK;
+}
+
+lss_status lss_op_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer, const double *values, double *rn)
+{
+    if (n <= 0 || nnz < 0 || !outer || !values || !rn) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(nullptr, [&]() {
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            lss::fail(LSS_ERR_NO_DEVICE, "no CUDA device available");
+        }
+        cudaStream_t st;
+        LSS_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        {
+            lss::DBuf<int32_t> d_outer;
+            lss::DBuf<double> d_vals, d_rn(n);
+            d_outer.upload(outer, (size_t)n + 1, st);
+            d_vals.upload(values, (size_t)nnz, st);
+            lss::launch_row_l1_norms(n, nnz, d_outer.data(), d_vals.data(), d_rn.data(), st);
+            LSS_CUDA(cudaMemcpyAsync(rn, d_rn.data(), (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
+            LSS_CUDA(cudaStreamSynchronize(st));
+        }
+        cudaStreamDestroy(st);
+    });
+}
+
+lss_status lss_op_spmv(lss_solver *s, const double *x, double *y)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->op_spmv(x, y); });
+}
+
+lss_status lss_op_mas_apply(lss_solver *s, const double *r, double *z)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->op_mas(r, z); });
+}
+
+lss_status lss_op_precond(lss_solver *s, const double *r, double *z)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->op_precond(r, z); });
+}
+
+lss_status lss_op_time(lss_solver *s, int32_t kind, int32_t reps, double *ms_per_launch, double *bytes_per_launch)
+{
+    if (!valid(s) || !ms_per_launch || !bytes_per_launch) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->op_time(kind, reps, ms_per_launch, bytes_per_launch); });
+}
+
+lss_status lss_set_memory_cap(size_t bytes)
+{
+    lss::alloc_cap_bytes() = bytes;
+    return LSS_OK;
+}
+
+}  // extern "C"

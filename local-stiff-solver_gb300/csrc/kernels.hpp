@@ -1,0 +1,158 @@
+// Device data views and kernel launchers of the GB300 hybrid solver.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "lss_common.hpp"
+
+namespace lss {
+
+constexpr int RED_MAX_VALUES = 8;   // values per grid reduction
+constexpr int GRID_MAX = 152 * 16;  // upper bound of CTAs of any reducing kernel (16 per SM)
+
+// Scratch of the deterministic grid reductions (device memory, counter zeroed once).
+struct GridReduce {
+    double *partials = nullptr;  // GRID_MAX * RED_MAX_VALUES
+    unsigned *counter = nullptr; // one arrival counter
+};
+
+inline int grid_for(long long work_items, int items_per_cta, int max_ctas = GRID_MAX)
+{
+    long long g = (work_items + items_per_cta - 1) / items_per_cta;
+    if (g < 1) g = 1;
+    if (g > max_ctas) g = max_ctas;
+    return (int)g;
+}
+
+// ---------------------------------------------------------------- selection
+struct GmmState {
+    double sum, mean, var, mn, mx;
+    double m0, m1, v0, v1, w0, w1;        // current parameters
+    double em0, em1, ev0, ev1, ew0, ew1;  // parameters of the last E-step
+    double s0, s1;                        // responsibilities' sums of the last E-step
+    int esteps, converged, pad0, pad1;
+};
+
+void launch_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer, const double *vals, double *rn,
+                         cudaStream_t s);
+void launch_gmm(int32_t n, const double *rn, GmmState *st, int max_iterations, double tol, GridReduce gr,
+                cudaStream_t s);
+void launch_gmm_mark(int32_t n, const double *rn, const GmmState *st, double threshold, int32_t *block_count,
+                     double *block_margin, cudaStream_t s);
+void launch_gmm_scatter(int32_t n, const double *rn, const GmmState *st, double threshold,
+                        const int32_t *block_offset, int32_t *out, cudaStream_t s);
+
+// ---------------------------------------------------------------- operator
+struct BsrDev {
+    int32_t nb = 0, bd = 1;
+    int lanes = 8;                 // threads per block row in SpMV
+    const int32_t *rows = nullptr;
+    const int32_t *cols = nullptr;
+    const double *vals = nullptr;  // row-sliced layout (spmv.cuh)
+    const float *vals32 = nullptr; // FP32 copy (mixed precision preconditioner)
+};
+
+// vals[j] = src >= 0 ? csc[src] : 0  (BSR slot gather)
+void launch_gather_values(int64_t count, const int64_t *src, const double *csc, double *vals, float *vals32,
+                          cudaStream_t s);
+// y = A x  (FP64)
+void launch_spmv(const BsrDev &A, const double *x, double *y, const int *done, cudaStream_t s);
+// y = r - A x, FP64 (fp32 == false) or with the FP32 operator copy (fp32 == true)
+void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, double *y, bool fp32,
+                          const int *done, cudaStream_t s);
+
+// ---------------------------------------------------------------- PCG
+enum StopReason : int {
+    STOP_RUNNING = 0,
+    STOP_CONVERGED_REL = 1,
+    STOP_CONVERGED_ABS = 2,
+    STOP_ZERO_PAP = 3,
+    STOP_NEGATIVE_ALPHA = 4,
+    STOP_SUBNORMAL_ALPHA = 5,
+    STOP_MAX_ITER = 6,
+    STOP_NONFINITE = 7,
+};
+
+struct PcgState {
+    double bb, gamma, alpha, beta, pAp, rr, rel_eps, abs_eps;
+    int iter, done, max_iter, pad;
+};
+
+void launch_dot(int64_t n, const double *a, const double *b, double *out, GridReduce gr, cudaStream_t s);
+// Ap = A p; pAp = p.Ap; alpha = gamma / pAp with the reference's breakdown tests
+void launch_pcg_spmv_alpha(const BsrDev &A, const double *p, double *Ap, PcgState *st, GridReduce gr,
+                           cudaStream_t s);
+// x += alpha p; r -= alpha Ap; rr = r.r; convergence tests
+void launch_pcg_update_xr(int64_t n, double *x, double *r, const double *p, const double *Ap, PcgState *st,
+                          GridReduce gr, cudaStream_t s);
+// p = z + beta p
+void launch_pcg_update_p(int64_t n, double *p, const double *z, const PcgState *st, cudaStream_t s);
+void launch_copy(int64_t n, const double *src, double *dst, const int *done, cudaStream_t s);
+void launch_permute(int64_t nb, int bd, const int32_t *perm, const double *src, double *dst, bool to_new,
+                    cudaStream_t s);
+void launch_grad_pattern(int32_t n, const int32_t *outer, const int32_t *inner, const double *lambda,
+                         const double *x, double *dA, cudaStream_t s);
+
+// ---------------------------------------------------------------- MAS
+constexpr int MAS_MAXL = 7;
+
+struct MasDev {
+    int L = 1, bd = 1;
+    int32_t nb = 0, nparts = 0;
+    const int32_t *part_off = nullptr;  // nparts+1
+    const uint8_t *key0 = nullptr;      // per node: local level-1 aggregate id inside its part
+    const int32_t *cbase0 = nullptr;    // per part: first level-1 item
+    const uint8_t *ccnt0 = nullptr;     // per part: number of level-1 items
+    int32_t nitems[MAS_MAXL] = {};      // level l >= 1 items
+    int32_t nbanks[MAS_MAXL] = {};      // level l banks (level 0: nparts)
+    int64_t voff[MAS_MAXL] = {};        // l >= 1: element offset of level-l vectors
+    int32_t boff[MAS_MAXL] = {};        // l >= 1: first coarse bank of level l
+    const uint8_t *key[MAS_MAXL] = {};  // l >= 1: per item local aggregate id at level l+1
+    const int32_t *cbase[MAS_MAXL] = {};
+    const uint8_t *ccnt[MAS_MAXL] = {};
+    int32_t ncoarse = 0;                // total coarse banks
+    int64_t tile_elems = 0;             // inverse elements per bank
+    int64_t level_elems = 0;            // elements of the level-vector buffers
+};
+
+int64_t mas_tile_elems(int bd);
+
+// Galerkin assembly into per-bank dense N x N FP64 staging (N = 32 bd)
+void launch_mas_assemble0(const BsrDev &A, const int32_t *part_of, const int32_t *part_off, double *stage,
+                          cudaStream_t s);
+void launch_mas_assemble_coarse(const BsrDev &A, const MasDev &m, const int32_t *cmap /* nb*(L-1) */,
+                                double *stage, cudaStream_t s);
+// pad zero diagonals, invert (symmetric sweep), write bank tiles (FP32 or FP64)
+void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, bool fp32, int *bad,
+                       cudaStream_t s);
+// z = MAS^-1 xin (acc: z += MAS^-1 xin).  dot_mode 1: st->gamma = rdot.z;
+// dot_mode 2: st->beta = rdot.z / st->gamma, st->gamma = rdot.z.
+void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
+                      const double *xin, double *z, bool acc, const double *rdot, PcgState *st, int dot_mode,
+                      GridReduce gr, const int *done, cudaStream_t s);
+
+// ---------------------------------------------------------------- stiff blocks
+struct StiffDev {
+    int32_t nsub = 0, ndof = 0;
+    const int32_t *dofs = nullptr;     // ndof permuted scalar ids, grouped by subdomain
+    const int32_t *sub_of = nullptr;   // ndof
+    const int32_t *off = nullptr;      // nsub+1 (into dofs)
+    const int64_t *inv_off = nullptr;  // nsub (into inverse storage)
+    const double *inv = nullptr;       // row-major m x m per subdomain
+    const float *inv32 = nullptr;
+    double *t = nullptr;               // ndof scratch
+};
+
+void launch_stiff_extract(const BsrDev &A, const StiffDev &S, double *stage, cudaStream_t s);
+void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, const int64_t *h_inv_off,
+                         double *inv, int *bad, cudaStream_t s);
+void launch_stiff_to_fp32(int64_t count, const double *src, float *dst, cudaStream_t s);
+// t = r_S - (A z)_S   (residual = true) or t = r_S
+void launch_stiff_gather(const BsrDev &A, const StiffDev &S, const double *r, const double *z, bool residual,
+                         const int *done, cudaStream_t s);
+// z_S += Inv t
+void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done, cudaStream_t s);
+
+}  // namespace lss

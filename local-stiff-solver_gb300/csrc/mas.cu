@@ -1,0 +1,449 @@
+// Multilevel additive Schwarz (MAS) preconditioner kernels (sm_103a).
+//
+// Semantics follow MASPreconditioner (MASPreconditioner.cu:376-1164 in the
+// reference): level 0 = one 32*bd x 32*bd block per partition ("bank"), coarse
+// level l = banks of 32 consecutive components of level l-1; each bank's
+// Galerkin block is inverted exactly; apply = restrict (sum) -> per-bank
+// symmetric matrix-vector product -> prolong (inject and add).
+//
+// GB300 layout of the inverses ("circulant tiles").  Inside a bank the scalar
+// index is component-major (comp * 32 + lane).  The N x N inverse is cut into
+// 32 x 32 tiles (c, c2), c <= c2; tile element [d][r] holds
+// Inv[c*32 + r][c2*32 + (r+d) % 32], d = 0..16 for diagonal tiles (d = 16 kept
+// twice, so 17*32 entries = the packed-triangle size plus 16) and d = 0..31 for
+// off-diagonal tiles.  A warp owns a bank, lane r owns row r of every tile:
+// every tile load is one 128-byte (FP32) / 256-byte (FP64) coalesced line,
+// and the symmetric partner term travels by warp shuffle instead of being
+// stored twice.  The inverse streams from HBM once per apply with evict-first
+// loads; residual and coarse vectors stay in L2.
+#include "device_common.cuh"
+#include "kernels.hpp"
+
+namespace lss {
+
+int64_t mas_tile_elems(int bd) { return (int64_t)bd * 17 * 32 + (int64_t)bd * (bd - 1) / 2 * 1024; }
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <int BD>
+__host__ __device__ constexpr int64_t tile_elems() { return (int64_t)BD * 17 * 32 + (int64_t)BD * (BD - 1) / 2 * 1024; }
+
+template <typename T>
+__device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
+
+// y = Inv x for one bank; lane r holds x[c] = x_{c*32+r}.
+template <int BD, typename T>
+__device__ __forceinline__ void tile_symv(const T *__restrict__ tile, const T (&x)[BD], T (&y)[BD], int lane)
+{
+#pragma unroll
+    for (int c = 0; c < BD; ++c) y[c] = T(0);
+    const T *__restrict__ t = tile;
+#pragma unroll
+    for (int c = 0; c < BD; ++c) {
+        {
+            T a = ld_stream(t + lane);
+            y[c] += a * x[c];
+#pragma unroll
+            for (int d = 1; d < 16; ++d) {
+                a = ld_stream(t + d * 32 + lane);
+                const T xs = __shfl_sync(FULL, x[c], (lane + d) & 31);
+                y[c] += a * xs;
+                const T tr = a * x[c];
+                y[c] += __shfl_sync(FULL, tr, (lane - d) & 31);
+            }
+            a = ld_stream(t + 16 * 32 + lane);
+            y[c] += a * __shfl_xor_sync(FULL, x[c], 16);
+            t += 17 * 32;
+        }
+#pragma unroll
+        for (int c2 = c + 1; c2 < BD; ++c2) {
+#pragma unroll 8
+            for (int d = 0; d < 32; ++d) {
+                const T a = ld_stream(t + d * 32 + lane);
+                const T xs = __shfl_sync(FULL, x[c2], (lane + d) & 31);
+                y[c] += a * xs;
+                const T tr = a * x[c];
+                y[c2] += __shfl_sync(FULL, tr, (lane - d) & 31);
+            }
+            t += 32 * 32;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ setup
+
+template <int BD>
+__global__ void __launch_bounds__(256) assemble0_kernel(BsrDev A, const int32_t *__restrict__ part_of,
+                                                        const int32_t *__restrict__ part_off,
+                                                        double *__restrict__ stage)
+{
+    constexpr int N = 32 * BD;
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.nb) return;
+    const int32_t p = part_of[i], lo = part_off[p], hi = part_off[p + 1], li = i - lo;
+    double *base = stage + (int64_t)p * N * N;
+    const int32_t b = A.rows[i], len = A.rows[i + 1] - b;
+    const double *v = A.vals + (int64_t)b * BD * BD;
+    for (int32_t l = 0; l < len; ++l) {
+        const int32_t j = A.cols[b + l];
+        if (j < lo || j >= hi) continue;
+        const int32_t lj = j - lo;
+#pragma unroll
+        for (int bi = 0; bi < BD; ++bi)
+#pragma unroll
+            for (int bj = 0; bj < BD; ++bj)
+                base[(int64_t)(bi * 32 + li) * N + bj * 32 + lj] = v[(int64_t)(bi * BD + bj) * len + l];
+    }
+}
+
+template <int BD>
+__global__ void __launch_bounds__(256) assemble_coarse_kernel(BsrDev A, MasDev m, const int32_t *__restrict__ cmap,
+                                                              double *__restrict__ stage)
+{
+    constexpr int N = 32 * BD;
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.nb) return;
+    const int32_t b = A.rows[i], len = A.rows[i + 1] - b;
+    const double *v = A.vals + (int64_t)b * BD * BD;
+    for (int l = 1; l < m.L; ++l) {
+        const int32_t *map = cmap + (int64_t)(l - 1) * A.nb;
+        const int32_t ci = map[i];
+        const int32_t g = m.boff[l] + (ci >> 5);
+        double *base = stage + (int64_t)g * N * N;
+        for (int32_t q = 0; q < len; ++q) {
+            const int32_t cj = map[A.cols[b + q]];
+            if ((cj >> 5) != (ci >> 5)) continue;
+#pragma unroll
+            for (int bi = 0; bi < BD; ++bi)
+#pragma unroll
+                for (int bj = 0; bj < BD; ++bj) {
+                    const int row = bi * 32 + (ci & 31), col = bj * 32 + (cj & 31);
+                    if (row > col) continue;  // upper triangle only
+                    atomicAdd(base + (int64_t)row * N + col, v[(int64_t)(bi * BD + bj) * len + q]);
+                }
+        }
+    }
+}
+
+// Symmetric sweep inversion of S (N x N, leading dimension ld, in shared
+// memory): the Gauss-Jordan variant of MASPreconditioner.cu:799-900, which
+// leaves -A^-1 in S.  Flags zero / non-finite pivots.
+__device__ void sweep_invert(double *S, int ld, int N, double *col, double *scol, int *bad)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+    for (int p = 0; p < N; ++p) {
+        const double piv = S[p * ld + p];
+        for (int t = tid; t < N; t += nt) {
+            const double cv = (t == p) ? 0.0 : S[t * ld + p];
+            col[t] = cv;
+            scol[t] = cv / piv;
+        }
+        if (tid == 0 && (!isfinite(piv) || piv == 0.0)) atomicOr(bad, 1);
+        __syncthreads();
+        for (int t = wid; t < N; t += nw) {
+            if (t == p) continue;
+            const double st = scol[t];
+            for (int c = lane; c < N; c += 32)
+                if (c != p) S[t * ld + c] -= st * col[c];
+        }
+        __syncthreads();
+        for (int t = tid; t < N; t += nt) {
+            if (t == p) S[p * ld + p] = -1.0 / piv;
+            else {
+                S[t * ld + p] = scol[t];
+                S[p * ld + t] = scol[t];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int BD, typename T>
+__global__ void __launch_bounds__(256) mas_invert_kernel(const double *__restrict__ stage, T *__restrict__ out,
+                                                         int *bad)
+{
+    constexpr int N = 32 * BD, LD = N + 1;
+    extern __shared__ double sm[];
+    double *S = sm, *col = sm + N * LD, *scol = col + N;
+    const int64_t bank = blockIdx.x;
+    const double *src = stage + bank * N * N;
+    for (int idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
+        const int r = idx / N, c = idx % N;
+        S[r * LD + c] = (r <= c) ? src[(int64_t)r * N + c] : src[(int64_t)c * N + r];
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < N; d += blockDim.x)
+        if (S[d * LD + d] == 0.0) S[d * LD + d] = 1.0;  // padding (MASPreconditioner.cu:779-796)
+    __syncthreads();
+    sweep_invert(S, LD, N, col, scol, bad);
+    // tiles
+    T *dst = out + bank * tile_elems<BD>();
+    int64_t off = 0;
+    for (int c = 0; c < BD; ++c)
+        for (int c2 = c; c2 < BD; ++c2) {
+            const int nd = (c == c2) ? 17 : 32;
+            for (int e = threadIdx.x; e < nd * 32; e += blockDim.x) {
+                const int d = e >> 5, r = e & 31;
+                const double val = -S[(c * 32 + r) * LD + c2 * 32 + ((r + d) & 31)];
+                if (!isfinite(val)) atomicOr(bad, 2);
+                dst[off + e] = (T)val;
+            }
+            off += nd * 32;
+        }
+}
+
+// ------------------------------------------------------------------ apply
+
+// level 0 -> level 1: per-part component sums of r
+template <int BD, typename T>
+__global__ void __launch_bounds__(256) restrict0_kernel(MasDev m, const double *__restrict__ r, T *__restrict__ v,
+                                                        const int *done)
+{
+    if (done && *done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    T *v1 = v + m.voff[1];
+    for (int64_t p = w0; p < m.nparts; p += nw) {
+        const int32_t lo = m.part_off[p], node = lo + lane;
+        const bool valid = node < m.part_off[p + 1];
+        double x[BD];
+        int key = 255;
+        if (valid) {
+            key = m.key0[node];
+#pragma unroll
+            for (int c = 0; c < BD; ++c) x[c] = r[(int64_t)node * BD + c];
+        } else {
+#pragma unroll
+            for (int c = 0; c < BD; ++c) x[c] = 0.0;
+        }
+        const int ncc = m.ccnt0[p];
+        const int32_t base = m.cbase0[p];
+        for (int k = 0; k < ncc; ++k) {
+#pragma unroll
+            for (int c = 0; c < BD; ++c) {
+                const double s = warp_sum(key == k ? x[c] : 0.0);
+                if (lane == c) v1[(int64_t)(base + k) * BD + c] = (T)s;
+            }
+        }
+    }
+}
+
+// level l -> level l+1 (l >= 1)
+template <int BD, typename T>
+__global__ void __launch_bounds__(256) restrict_kernel(MasDev m, int l, T *__restrict__ v, const int *done)
+{
+    if (done && *done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const T *vl = v + m.voff[l];
+    T *vn = v + m.voff[l + 1];
+    const uint8_t *key_l = m.key[l];
+    for (int64_t b = w0; b < m.nbanks[l]; b += nw) {
+        const int64_t item = b * 32 + lane;
+        const bool valid = item < m.nitems[l];
+        double x[BD];
+#pragma unroll
+        for (int c = 0; c < BD; ++c) x[c] = valid ? (double)vl[item * BD + c] : 0.0;
+        const int key = valid ? key_l[item] : 255;
+        const int ncc = m.ccnt[l][b];
+        const int32_t base = m.cbase[l][b];
+        for (int k = 0; k < ncc; ++k) {
+#pragma unroll
+            for (int c = 0; c < BD; ++c) {
+                const double s = warp_sum(key == k ? x[c] : 0.0);
+                if (lane == c) vn[(int64_t)(base + k) * BD + c] = (T)s;
+            }
+        }
+    }
+}
+
+// all coarse banks: u_l = Inv_l v_l
+template <int BD, typename T>
+__global__ void __launch_bounds__(256) symv_coarse_kernel(MasDev m, const T *__restrict__ invc,
+                                                          const T *__restrict__ v, T *__restrict__ u,
+                                                          const int *done)
+{
+    if (done && *done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t g = w0; g < m.ncoarse; g += nw) {
+        int l = 1;
+        while (l + 1 < m.L && g >= m.boff[l + 1]) ++l;
+        const int64_t b = g - m.boff[l];
+        const int64_t e0 = m.voff[l] + (b * 32 + lane) * BD;
+        T x[BD], y[BD];
+#pragma unroll
+        for (int c = 0; c < BD; ++c) x[c] = v[e0 + c];
+        tile_symv<BD, T>(invc + g * m.tile_elems, x, y, lane);
+#pragma unroll
+        for (int c = 0; c < BD; ++c) u[e0 + c] = y[c];
+    }
+}
+
+// u_l += P u_{l+1} (top-down, one level per launch)
+template <int BD, typename T>
+__global__ void __launch_bounds__(256) prolong_kernel(MasDev m, int l, T *__restrict__ u, const int *done)
+{
+    if (done && *done) return;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.nitems[l]) return;
+    const int64_t parent = m.cbase[l][k >> 5] + m.key[l][k];
+#pragma unroll
+    for (int c = 0; c < BD; ++c) u[m.voff[l] + k * BD + c] += u[m.voff[l + 1] + parent * BD + c];
+}
+
+// level 0: z = Inv_0 x (+ coarse correction u_1), optional accumulate and r.z
+template <int BD, typename T, bool ACC, int DOT>
+__global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restrict__ inv0, const T *__restrict__ u,
+                                                    const double *__restrict__ xin, double *__restrict__ z,
+                                                    const double *__restrict__ rdot, PcgState *st, GridReduce gr,
+                                                    const int *done)
+{
+    if (done && *done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double dot[1] = {0.0};
+    const T *u1 = u + m.voff[1];
+    for (int64_t p = w0; p < m.nparts; p += nw) {
+        const int32_t lo = m.part_off[p], node = lo + lane;
+        const bool valid = node < m.part_off[p + 1];
+        T x[BD], y[BD];
+#pragma unroll
+        for (int c = 0; c < BD; ++c) x[c] = valid ? (T)xin[(int64_t)node * BD + c] : T(0);
+        tile_symv<BD, T>(inv0 + p * m.tile_elems, x, y, lane);
+        if (valid) {
+            int64_t cidx = -1;
+            if (m.L > 1) cidx = (int64_t)(m.cbase0[p] + m.key0[node]) * BD;
+#pragma unroll
+            for (int c = 0; c < BD; ++c) {
+                double val = (double)y[c];
+                if (cidx >= 0) val += (double)u1[cidx + c];
+                const int64_t e = (int64_t)node * BD + c;
+                if (ACC) val += z[e];
+                z[e] = val;
+                if (DOT) dot[0] += rdot[e] * val;
+            }
+        }
+    }
+    if (DOT) {
+        double tot[1];
+        if (grid_sum<1>(dot, gr, tot)) {
+            // DOT == 1: initial gamma (GPUHybrid.cu:1450-1451); DOT == 2: new gamma and
+            // beta = gamma_new / gamma_old (GPUHybrid.cu:1501-1504)
+            if (DOT == 2) st->beta = tot[0] / st->gamma;
+            st->gamma = tot[0];
+        }
+    }
+}
+
+template <int BD, typename T>
+void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, const double *xin, double *z,
+                     bool acc, const double *rdot, PcgState *st, int dot_mode, GridReduce gr, const int *done,
+                     cudaStream_t s)
+{
+    if (m.L > 1) {
+        restrict0_kernel<BD, T><<<grid_for((int64_t)m.nparts * 32, 256, 152 * 16), 256, 0, s>>>(m, xin, v, done);
+        for (int l = 1; l + 1 < m.L; ++l)
+            restrict_kernel<BD, T><<<grid_for((int64_t)m.nbanks[l] * 32, 256, 152 * 16), 256, 0, s>>>(m, l, v, done);
+        symv_coarse_kernel<BD, T><<<grid_for((int64_t)m.ncoarse * 32, 256, 152 * 16), 256, 0, s>>>(m, invc, v, u,
+                                                                                                   done);
+        for (int l = m.L - 2; l >= 1; --l)
+            prolong_kernel<BD, T><<<grid_for(m.nitems[l], 256, 1 << 30), 256, 0, s>>>(m, l, u, done);
+    }
+    const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
+    if (dot_mode == 0) {
+        if (acc) symv0_kernel<BD, T, true, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
+        else symv0_kernel<BD, T, false, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
+    } else if (dot_mode == 1) {
+        if (acc) symv0_kernel<BD, T, true, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
+        else symv0_kernel<BD, T, false, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
+    } else {
+        if (acc) symv0_kernel<BD, T, true, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
+        else symv0_kernel<BD, T, false, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
+    }
+    LSS_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+void launch_mas_assemble0(const BsrDev &A, const int32_t *part_of, const int32_t *part_off, double *stage,
+                          cudaStream_t s)
+{
+    const int grid = (int)((A.nb + 255) / 256);
+    if (grid == 0) return;
+    switch (A.bd) {
+    case 1: assemble0_kernel<1><<<grid, 256, 0, s>>>(A, part_of, part_off, stage); break;
+    case 2: assemble0_kernel<2><<<grid, 256, 0, s>>>(A, part_of, part_off, stage); break;
+    default: assemble0_kernel<3><<<grid, 256, 0, s>>>(A, part_of, part_off, stage); break;
+    }
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_mas_assemble_coarse(const BsrDev &A, const MasDev &m, const int32_t *cmap, double *stage,
+                                cudaStream_t s)
+{
+    const int grid = (int)((A.nb + 255) / 256);
+    if (grid == 0 || m.L < 2) return;
+    switch (A.bd) {
+    case 1: assemble_coarse_kernel<1><<<grid, 256, 0, s>>>(A, m, cmap, stage); break;
+    case 2: assemble_coarse_kernel<2><<<grid, 256, 0, s>>>(A, m, cmap, stage); break;
+    default: assemble_coarse_kernel<3><<<grid, 256, 0, s>>>(A, m, cmap, stage); break;
+    }
+    LSS_LAUNCH_CHECK();
+}
+
+template <int BD, typename T>
+static void invert_t(int64_t nbanks, const double *stage, T *out, int *bad, cudaStream_t s)
+{
+    constexpr int N = 32 * BD;
+    const size_t smem = (size_t)(N * (N + 1) + 2 * N) * sizeof(double);
+    LSS_CUDA(cudaFuncSetAttribute(mas_invert_kernel<BD, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    for (int64_t b0 = 0; b0 < nbanks; b0 += 1 << 30) {
+        const int64_t cnt = std::min<int64_t>(nbanks - b0, 1 << 30);
+        mas_invert_kernel<BD, T><<<(unsigned)cnt, 256, smem, s>>>(stage + b0 * N * N, out + b0 * mas_tile_elems(BD),
+                                                                  bad);
+    }
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, bool fp32, int *bad, cudaStream_t s)
+{
+    if (nbanks == 0) return;
+    if (fp32) {
+        if (bd == 1) invert_t<1, float>(nbanks, stage, (float *)out, bad, s);
+        else if (bd == 2) invert_t<2, float>(nbanks, stage, (float *)out, bad, s);
+        else invert_t<3, float>(nbanks, stage, (float *)out, bad, s);
+    } else {
+        if (bd == 1) invert_t<1, double>(nbanks, stage, (double *)out, bad, s);
+        else if (bd == 2) invert_t<2, double>(nbanks, stage, (double *)out, bad, s);
+        else invert_t<3, double>(nbanks, stage, (double *)out, bad, s);
+    }
+}
+
+void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
+                      const double *xin, double *z, bool acc, const double *rdot, PcgState *st, int dot_mode,
+                      GridReduce gr, const int *done, cudaStream_t s)
+{
+#define LSS_MAS(BD_, T_)                                                                                          \
+    mas_apply_dot_t<BD_, T_>(m, (const T_ *)inv0, (const T_ *)invc, (T_ *)v, (T_ *)u, xin, z, acc, rdot, st,     \
+                             dot_mode, gr, done, s)
+    if (fp32) {
+        if (m.bd == 1) LSS_MAS(1, float);
+        else if (m.bd == 2) LSS_MAS(2, float);
+        else LSS_MAS(3, float);
+    } else {
+        if (m.bd == 1) LSS_MAS(1, double);
+        else if (m.bd == 2) LSS_MAS(2, double);
+        else LSS_MAS(3, double);
+    }
+#undef LSS_MAS
+}
+
+}  // namespace lss

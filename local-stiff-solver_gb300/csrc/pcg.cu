@@ -1,0 +1,360 @@
+// Operator and PCG kernels (sm_103a): FP64 BSR/CSR SpMV with fused epilogues,
+// PCG vector updates with deterministic fused reductions, permutation and
+// the pattern-restricted gradient of the adjoint.
+//
+// PCG follows GPUHybrid::pcg_solve (GPUHybrid.cu:1413-1512): recurrence
+// residual, relative test rr / bb < rel_tol^2 and absolute test rr < abs_tol^2
+// every iteration, breakdown stops on p.Ap == 0, alpha <= 0 and subnormal
+// alpha.  The scalars live on the device; every kernel of an iteration
+// returns immediately once st->done is set, so the host only polls the flag
+// every few iterations (the reference synchronises on every dot product).
+#include <cfloat>
+
+#include "device_common.cuh"
+#include "kernels.hpp"
+#include "spmv.cuh"
+
+namespace lss {
+namespace {
+
+__global__ void gather_values_kernel(int64_t count, const int64_t *__restrict__ src, const double *__restrict__ csc,
+                                     double *__restrict__ vals, float *__restrict__ vals32)
+{
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = src[j];
+        const double v = k >= 0 ? csc[k] : 0.0;
+        vals[j] = v;
+        if (vals32) vals32[j] = (float)v;
+    }
+}
+
+// y = A x
+template <int BD, int LANES>
+__global__ void __launch_bounds__(256) spmv_kernel(BsrDev A, const double *__restrict__ x, double *__restrict__ y,
+                                                   const int *done)
+{
+    if (done && *done) return;
+    const int lane = threadIdx.x % LANES;
+    constexpr int RPW = 32 / LANES;  // block rows per warp and sweep
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    // warp-uniform trip count: every lane reaches the group shuffles together
+    for (int64_t wr = w0 * RPW; wr < A.nb; wr += nw * RPW) {
+        const int64_t i = wr + (threadIdx.x & 31) / LANES;
+        const bool valid = i < A.nb;
+        double acc[BD];
+        bsr_block_row<BD, LANES, double, double, double>(A.rows, A.cols, A.vals, (int32_t)i, valid, x, lane, acc);
+        if (valid && lane < BD) {
+            double o = acc[0];
+#pragma unroll
+            for (int k = 1; k < BD; ++k)
+                if (lane == k) o = acc[k];
+            y[i * BD + lane] = o;
+        }
+    }
+}
+
+// y = r - A x, operator in VT precision, accumulation in ACC
+template <int BD, int LANES, typename VT, typename ACC>
+__global__ void __launch_bounds__(256) residual_kernel(BsrDev A, const VT *__restrict__ vals,
+                                                       const double *__restrict__ r, const double *__restrict__ x,
+                                                       double *__restrict__ y, const int *done)
+{
+    if (done && *done) return;
+    const int lane = threadIdx.x % LANES;
+    constexpr int RPW = 32 / LANES;  // block rows per warp and sweep
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    // warp-uniform trip count: every lane reaches the group shuffles together
+    for (int64_t wr = w0 * RPW; wr < A.nb; wr += nw * RPW) {
+        const int64_t i = wr + (threadIdx.x & 31) / LANES;
+        const bool valid = i < A.nb;
+        ACC acc[BD];
+        bsr_block_row<BD, LANES, VT, double, ACC>(A.rows, A.cols, vals, (int32_t)i, valid, x, lane, acc);
+        if (valid && lane < BD) {
+            ACC o = acc[0];
+#pragma unroll
+            for (int k = 1; k < BD; ++k)
+                if (lane == k) o = acc[k];
+            y[i * BD + lane] = r[i * BD + lane] - (double)o;
+        }
+    }
+}
+
+// Ap = A p, p.Ap, then alpha with the breakdown tests (GPUHybrid.cu:1458-1480)
+template <int BD, int LANES>
+__global__ void __launch_bounds__(256) spmv_alpha_kernel(BsrDev A, const double *__restrict__ p,
+                                                         double *__restrict__ Ap, PcgState *st, GridReduce gr)
+{
+    if (st->done) return;
+    const int lane = threadIdx.x % LANES;
+    constexpr int RPW = 32 / LANES;  // block rows per warp and sweep
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double dot[1] = {0.0};
+    // warp-uniform trip count: every lane reaches the group shuffles together
+    for (int64_t wr = w0 * RPW; wr < A.nb; wr += nw * RPW) {
+        const int64_t i = wr + (threadIdx.x & 31) / LANES;
+        const bool valid = i < A.nb;
+        double acc[BD];
+        bsr_block_row<BD, LANES, double, double, double>(A.rows, A.cols, A.vals, (int32_t)i, valid, p, lane, acc);
+        if (valid && lane < BD) {
+            double o = acc[0];
+#pragma unroll
+            for (int k = 1; k < BD; ++k)
+                if (lane == k) o = acc[k];
+            Ap[i * BD + lane] = o;
+            dot[0] += p[i * BD + lane] * o;
+        }
+    }
+    double tot[1];
+    if (grid_sum<1>(dot, gr, tot)) {
+        st->iter += 1;
+        const double pAp = tot[0];
+        st->pAp = pAp;
+        if (pAp == 0.0) { st->done = STOP_ZERO_PAP; return; }
+        const double alpha = st->gamma / pAp;
+        if (!(alpha == alpha) || isinf(alpha)) { st->done = STOP_NONFINITE; return; }
+        if (alpha <= 0.0) { st->done = STOP_NEGATIVE_ALPHA; return; }
+        if (alpha < DBL_MIN) { st->done = STOP_SUBNORMAL_ALPHA; return; }
+        st->alpha = alpha;
+    }
+}
+
+// x += alpha p; r -= alpha Ap; rr; convergence (GPUHybrid.cu:1482-1496)
+__global__ void __launch_bounds__(256) update_xr_kernel(int64_t n, double *__restrict__ x, double *__restrict__ r,
+                                                        const double *__restrict__ p, const double *__restrict__ Ap,
+                                                        PcgState *st, GridReduce gr)
+{
+    if (st->done) return;
+    const double alpha = st->alpha;
+    double s[1] = {0.0};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] += alpha * p[i];
+        const double ri = r[i] - alpha * Ap[i];
+        r[i] = ri;
+        s[0] += ri * ri;
+    }
+    double tot[1];
+    if (grid_sum<1>(s, gr, tot)) {
+        const double rr = tot[0];
+        st->rr = rr;
+        if (!(rr == rr) || isinf(rr)) { st->done = STOP_NONFINITE; return; }
+        if (st->rel_eps > 0 && rr / st->bb < st->rel_eps) { st->done = STOP_CONVERGED_REL; return; }
+        if (st->abs_eps > 0 && rr < st->abs_eps) { st->done = STOP_CONVERGED_ABS; return; }
+        if (st->iter >= st->max_iter) { st->done = STOP_MAX_ITER; return; }
+    }
+}
+
+// p = z + beta p (GPUHybrid.cu:1506-1507)
+__global__ void __launch_bounds__(256) update_p_kernel(int64_t n, double *__restrict__ p, const double *__restrict__ z,
+                                                       const PcgState *st)
+{
+    if (st->done) return;
+    const double beta = st->beta;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = z[i] + beta * p[i];
+}
+
+__global__ void __launch_bounds__(256) dot_kernel(int64_t n, const double *__restrict__ a, const double *__restrict__ b,
+                                                  double *out, GridReduce gr)
+{
+    double s[1] = {0.0};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s[0] += a[i] * b[i];
+    double tot[1];
+    if (grid_sum<1>(s, gr, tot)) *out = tot[0];
+}
+
+__global__ void copy_kernel(int64_t n, const double *__restrict__ src, double *__restrict__ dst, const int *done)
+{
+    if (done && *done) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+__global__ void permute_kernel(int64_t nb, int bd, const int32_t *__restrict__ perm, const double *__restrict__ src,
+                               double *__restrict__ dst, bool to_new)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb * bd;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t blk = i / bd, c = i % bd;
+        const int64_t q = (int64_t)perm[blk] * bd + c;
+        if (to_new) dst[q] = src[i];
+        else dst[i] = src[q];
+    }
+}
+
+// dA[k] = -lambda[row] * x[col] over the stored pattern (outer = row)
+__global__ void grad_pattern_kernel(int32_t n, const int32_t *__restrict__ outer, const int32_t *__restrict__ inner,
+                                    const double *__restrict__ lambda, const double *__restrict__ x,
+                                    double *__restrict__ dA)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = w0; i < n; i += nw) {
+        const double li = lambda[i];
+        for (int32_t k = outer[i] + lane; k < outer[i + 1]; k += 32) dA[k] = -li * x[inner[k]];
+    }
+}
+
+// gamma bookkeeping from r.z: mode 1 initial gamma, mode 2 beta and new gamma
+__global__ void __launch_bounds__(256) rz_kernel(int64_t n, const double *__restrict__ r, const double *__restrict__ z,
+                                                 PcgState *st, int mode, GridReduce gr)
+{
+    if (st->done) return;
+    double s[1] = {0.0};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s[0] += r[i] * z[i];
+    double tot[1];
+    if (grid_sum<1>(s, gr, tot)) {
+        if (mode == 2) st->beta = tot[0] / st->gamma;
+        st->gamma = tot[0];
+    }
+}
+
+__global__ void check_finite_kernel(int64_t n, const double *__restrict__ v, int *flag)
+{
+    bool bad = false;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        bad |= !isfinite(v[i]);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+template <int BD>
+void spmv_dispatch(const BsrDev &A, const double *x, double *y, const int *done, cudaStream_t s)
+{
+    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, 152 * 16);
+    switch (A.lanes) {
+    case 2: spmv_kernel<BD, 2><<<grid, 256, 0, s>>>(A, x, y, done); break;
+    case 4: spmv_kernel<BD, 4><<<grid, 256, 0, s>>>(A, x, y, done); break;
+    case 8: spmv_kernel<BD, 8><<<grid, 256, 0, s>>>(A, x, y, done); break;
+    case 16: spmv_kernel<BD, 16><<<grid, 256, 0, s>>>(A, x, y, done); break;
+    default: spmv_kernel<BD, 32><<<grid, 256, 0, s>>>(A, x, y, done); break;
+    }
+}
+
+template <int BD, typename VT, typename ACC>
+void residual_dispatch(const BsrDev &A, const VT *vals, const double *r, const double *x, double *y,
+                       const int *done, cudaStream_t s)
+{
+    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, 152 * 16);
+    switch (A.lanes) {
+    case 2: residual_kernel<BD, 2, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    case 4: residual_kernel<BD, 4, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    case 8: residual_kernel<BD, 8, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    case 16: residual_kernel<BD, 16, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    default: residual_kernel<BD, 32, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    }
+}
+
+template <int BD>
+void spmv_alpha_dispatch(const BsrDev &A, const double *p, double *Ap, PcgState *st, GridReduce gr, cudaStream_t s)
+{
+    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, GRID_MAX);
+    switch (A.lanes) {
+    case 2: spmv_alpha_kernel<BD, 2><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
+    case 4: spmv_alpha_kernel<BD, 4><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
+    case 8: spmv_alpha_kernel<BD, 8><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
+    case 16: spmv_alpha_kernel<BD, 16><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
+    default: spmv_alpha_kernel<BD, 32><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
+    }
+}
+
+}  // namespace
+
+void launch_gather_values(int64_t count, const int64_t *src, const double *csc, double *vals, float *vals32,
+                          cudaStream_t s)
+{
+    if (count == 0) return;
+    gather_values_kernel<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(count, src, csc, vals, vals32);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_spmv(const BsrDev &A, const double *x, double *y, const int *done, cudaStream_t s)
+{
+    if (A.bd == 1) spmv_dispatch<1>(A, x, y, done, s);
+    else if (A.bd == 2) spmv_dispatch<2>(A, x, y, done, s);
+    else spmv_dispatch<3>(A, x, y, done, s);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, double *y, bool fp32, const int *done,
+                          cudaStream_t s)
+{
+    if (fp32) {
+        if (A.bd == 1) residual_dispatch<1, float, float>(A, A.vals32, r, x, y, done, s);
+        else if (A.bd == 2) residual_dispatch<2, float, float>(A, A.vals32, r, x, y, done, s);
+        else residual_dispatch<3, float, float>(A, A.vals32, r, x, y, done, s);
+    } else {
+        if (A.bd == 1) residual_dispatch<1, double, double>(A, A.vals, r, x, y, done, s);
+        else if (A.bd == 2) residual_dispatch<2, double, double>(A, A.vals, r, x, y, done, s);
+        else residual_dispatch<3, double, double>(A, A.vals, r, x, y, done, s);
+    }
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_dot(int64_t n, const double *a, const double *b, double *out, GridReduce gr, cudaStream_t s)
+{
+    dot_kernel<<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, a, b, out, gr);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_pcg_spmv_alpha(const BsrDev &A, const double *p, double *Ap, PcgState *st, GridReduce gr, cudaStream_t s)
+{
+    if (A.bd == 1) spmv_alpha_dispatch<1>(A, p, Ap, st, gr, s);
+    else if (A.bd == 2) spmv_alpha_dispatch<2>(A, p, Ap, st, gr, s);
+    else spmv_alpha_dispatch<3>(A, p, Ap, st, gr, s);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_pcg_update_xr(int64_t n, double *x, double *r, const double *p, const double *Ap, PcgState *st,
+                          GridReduce gr, cudaStream_t s)
+{
+    update_xr_kernel<<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, x, r, p, Ap, st, gr);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_pcg_update_p(int64_t n, double *p, const double *z, const PcgState *st, cudaStream_t s)
+{
+    update_p_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, p, z, st);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_copy(int64_t n, const double *src, double *dst, const int *done, cudaStream_t s)
+{
+    copy_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, src, dst, done);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_permute(int64_t nb, int bd, const int32_t *perm, const double *src, double *dst, bool to_new,
+                    cudaStream_t s)
+{
+    permute_kernel<<<grid_for(nb * bd, 1024, 152 * 16), 256, 0, s>>>(nb, bd, perm, src, dst, to_new);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_pcg_rz(int64_t n, const double *r, const double *z, PcgState *st, int dot_mode, GridReduce gr,
+                   cudaStream_t s)
+{
+    rz_kernel<<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, r, z, st, dot_mode, gr);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_check_finite(int64_t n, const double *v, int *flag, cudaStream_t s)
+{
+    if (n == 0) return;
+    check_finite_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, v, flag);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_grad_pattern(int32_t n, const int32_t *outer, const int32_t *inner, const double *lambda,
+                         const double *x, double *dA, cudaStream_t s)
+{
+    grad_pattern_kernel<<<grid_for((int64_t)n * 32, 256, 152 * 16), 256, 0, s>>>(n, outer, inner, lambda, x, dA);
+    LSS_LAUNCH_CHECK();
+}
+
+}  // namespace lss

@@ -1,0 +1,750 @@
+// GPUHybrid-compatible orchestration on one GB300.
+//
+// factorize (GPUHybrid::factorize, GPUHybrid.cu:195-282):
+//   values -> device, gathered into the permuted row-sliced BSR operator;
+//   stiff-DOF selection on the GPU (select.cu) and host post-processing
+//   (postproc.cpp); dense FP64 inverses of the stiff subdomains (stiff.cu);
+//   MAS setup (mas.cu) -- in place of BoomerAMG setup (GPUHybrid.cu:357-376).
+// solve (GPUHybrid::solve + pcg_solve, GPUHybrid.cu:342-399, 1413-1512):
+//   device-resident FP64 PCG with the multiplicative MAS - direct - MAS
+//   preconditioner (custom_mixed_precond_iter, GPUHybrid.cu:521-542);
+//   iterations are captured as a CUDA graph in chunks and the host polls the
+//   device stop flag once per chunk.
+#include "solver.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <sstream>
+
+namespace lss {
+
+void launch_pcg_rz(int64_t n, const double *r, const double *z, PcgState *st, int dot_mode, GridReduce gr,
+                   cudaStream_t s);
+void launch_check_finite(int64_t n, const double *v, int *flag, cudaStream_t s);
+
+namespace {
+using clk = std::chrono::steady_clock;
+double secs(clk::time_point t0) { return std::chrono::duration<double>(clk::now() - t0).count(); }
+
+const char *stop_name(int s)
+{
+    switch (s) {
+    case STOP_RUNNING: return "running";
+    case STOP_CONVERGED_REL: return "converged_rel";
+    case STOP_CONVERGED_ABS: return "converged_abs";
+    case STOP_ZERO_PAP: return "err_zero_sdotp";
+    case STOP_NEGATIVE_ALPHA: return "err_negative_alpha";
+    case STOP_SUBNORMAL_ALPHA: return "err_subnormal_alpha";
+    case STOP_MAX_ITER: return "max_iterations";
+    case STOP_NONFINITE: return "err_nonfinite";
+    default: return "unknown";
+    }
+}
+}  // namespace
+
+HybridSolver::HybridSolver(const Params &p) : p_(p)
+{
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        fail(LSS_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (p_.device < 0 || p_.device >= ndev) fail(LSS_ERR_INVALID_ARGUMENT, "gb300.device out of range");
+    LSS_CUDA(cudaSetDevice(p_.device));
+    LSS_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    LSS_CUDA(cudaMallocHost((void **)&h_state_, sizeof(PcgState)));
+    d_state_.resize(1);
+    d_partials_.resize((size_t)GRID_MAX * RED_MAX_VALUES);
+    d_counter_.resize(1);
+    d_counter_.zero(stream_);
+    d_scalar_.resize(8);
+    d_bad_.resize(1);
+    gr_.partials = d_partials_.data();
+    gr_.counter = d_counter_.data();
+}
+
+HybridSolver::~HybridSolver()
+{
+    invalidate_graph();
+    if (h_state_) cudaFreeHost(h_state_);
+    if (stream_) {
+        cudaStreamSynchronize(stream_);
+        cudaStreamDestroy(stream_);
+    }
+}
+
+void HybridSolver::set_parameters(const char *json)
+{
+    Params np = parse_params(json, p_);
+    if (np.device != p_.device) fail(LSS_ERR_INVALID_ARGUMENT, "the device of an existing solver cannot change");
+    const bool pattern_affecting = np.block_size != p_.block_size || np.max_coarse_levels != p_.max_coarse_levels;
+    const bool value_affecting = pattern_affecting || np.mixed != p_.mixed || np.do_hybrid != p_.do_hybrid ||
+                                 np.select_l1 != p_.select_l1 || np.jump_threshold != p_.jump_threshold ||
+                                 np.gmm_tol != p_.gmm_tol || np.max_gmm_iterations != p_.max_gmm_iterations ||
+                                 np.cond_threshold != p_.cond_threshold || np.decompose != p_.decompose ||
+                                 np.min_sub != p_.min_sub || np.max_sub != p_.max_sub || np.expand != p_.expand ||
+                                 np.float_subdomains != p_.float_subdomains ||
+                                 np.multiplicative != p_.multiplicative;
+    p_ = np;
+    if (pattern_affecting) have_pattern_ = false;
+    if (value_affecting) factorized_ = false;
+    invalidate_graph();
+}
+
+std::string HybridSolver::name() const
+{
+    // GPUHybrid.hpp:57-67
+    if (p_.do_hybrid) return p_.select_l1 ? "GPUHybrid" : "GPUAMGF";
+    return "GPUAMG";
+}
+
+std::vector<int32_t> HybridSolver::selected() const
+{
+    std::vector<int32_t> all;
+    for (const auto &s : subs_) all.insert(all.end(), s.begin(), s.end());
+    std::sort(all.begin(), all.end());
+    return all;
+}
+
+std::string HybridSolver::info_json() const
+{
+    std::ostringstream o;
+    o.precision(17);
+    o << "{\"num_iterations\": " << num_iterations_ << ", \"final_res_norm\": " << final_res_norm_;
+    o << ", \"relative_residual\": " << (rhs_norm_ > 0 ? final_res_norm_ / rhs_norm_ : 0.0);
+    o << ", \"status\": \"" << stop_name(stop_reason_) << "\"";
+    o << ", \"refinements\": " << refinements_;
+    o << ", \"precision\": \"" << (p_.mixed ? "mixed" : "fp64") << "\"";
+    o << ", \"composition\": \"" << (p_.multiplicative ? "multiplicative" : "additive") << "\"";
+    int64_t nstiff = 0;
+    for (const auto &s : subs_) nstiff += (int64_t)s.size();
+    o << ", \"num_stiff_dofs\": " << nstiff << ", \"num_subdomains\": " << subs_.size();
+    o << ", \"num_gmm_selected\": " << gmm_sel_.size();
+    if (have_pattern_) {
+        o << ", \"num_parts\": " << (pat_.part.part_offsets.size() - 1) << ", \"mas_levels\": " << cs_.L;
+        o << ", \"block_size\": " << pat_.bd << ", \"nnz_blocks\": " << pat_.rows.back();
+        o << ", \"spmv_lanes\": " << A_.lanes;
+    }
+    for (const auto &kv : stats_) o << ", \"" << kv.first << "\": " << kv.second;
+    for (const auto &kv : sstats_) o << ", \"" << kv.first << "\": \"" << kv.second << "\"";
+    o << "}";
+    return o.str();
+}
+
+void HybridSolver::invalidate_graph()
+{
+    if (graph_exec_) {
+        cudaGraphExecDestroy(graph_exec_);
+        graph_exec_ = nullptr;
+    }
+    graph_iters_ = 0;
+}
+
+// ------------------------------------------------------------------ pattern
+
+void HybridSolver::analyze(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner)
+{
+    if (!outer || !inner || n <= 0 || nnz < 0) fail(LSS_ERR_INVALID_ARGUMENT, "invalid matrix arguments");
+    auto t0 = clk::now();
+    invalidate_graph();
+    factorized_ = false;
+    have_pattern_ = false;
+    pat_ = analyze_pattern(n, nnz, outer, inner, p_.block_size, p_.partition_threads);
+    h_outer_.assign(outer, outer + n + 1);
+    h_inner_.assign(inner, inner + nnz);
+    d_outer_.release();
+    d_inner_.release();
+    stats_["time_partition_and_layout"] = secs(t0);
+    auto t1 = clk::now();
+    cs_ = build_coarse_space(pat_, p_.max_coarse_levels);
+    stats_["time_coarse_space"] = secs(t1);
+
+    // device pattern
+    d_rows_.upload(pat_.rows, stream_);
+    d_cols_.upload(pat_.cols, stream_);
+    d_src_.upload(pat_.src, stream_);
+    d_perm_.upload(pat_.part.perm, stream_);
+    d_vals_.resize(pat_.src.size());
+    A_ = BsrDev();
+    A_.nb = pat_.nb;
+    A_.bd = pat_.bd;
+    A_.rows = d_rows_.data();
+    A_.cols = d_cols_.data();
+    A_.vals = d_vals_.data();
+    if (p_.spmv_lanes > 0) A_.lanes = p_.spmv_lanes;
+    else {
+        // lanes per block row: smallest power of two >= mean blocks per row, in [2, 32]
+        const double m = pat_.mean_blocks_per_row;
+        int l = 2;
+        while (l < 32 && l < m) l <<= 1;
+        A_.lanes = l;
+    }
+    // MAS device maps
+    const int32_t nparts = (int32_t)pat_.part.part_offsets.size() - 1;
+    d_part_off_.upload(pat_.part.part_offsets, stream_);
+    d_part_of_.upload(cs_.part_of, stream_);
+    d_key0_.upload(cs_.key0, stream_);
+    d_ccnt0_.upload(cs_.ccnt0, stream_);
+    d_cbase0_.upload(cs_.cbase0, stream_);
+    d_cmap_.upload(cs_.cmap, stream_);
+    d_key_.clear();
+    d_ccnt_.clear();
+    d_cbase_.clear();
+    d_key_.resize(cs_.L);
+    d_ccnt_.resize(cs_.L);
+    d_cbase_.resize(cs_.L);
+    mas_ = MasDev();
+    mas_.L = cs_.L;
+    mas_.bd = pat_.bd;
+    mas_.nb = pat_.nb;
+    mas_.nparts = nparts;
+    mas_.part_off = d_part_off_.data();
+    mas_.key0 = d_key0_.data();
+    mas_.cbase0 = d_cbase0_.data();
+    mas_.ccnt0 = d_ccnt0_.data();
+    mas_.nbanks[0] = nparts;
+    mas_.tile_elems = mas_tile_elems(pat_.bd);
+    int64_t voff = 0;
+    int32_t boff = 0;
+    for (int l = 1; l < cs_.L; ++l) {
+        mas_.nitems[l] = cs_.nitems[l];
+        mas_.nbanks[l] = cs_.nbanks[l];
+        mas_.voff[l] = voff;
+        voff += (int64_t)cs_.nbanks[l] * 32 * pat_.bd;
+        mas_.boff[l] = boff;
+        boff += cs_.nbanks[l];
+        if (l + 1 < cs_.L) {
+            d_key_[l].upload(cs_.key[l], stream_);
+            d_ccnt_[l].upload(cs_.ccnt[l], stream_);
+            d_cbase_[l].upload(cs_.cbase[l], stream_);
+            mas_.key[l] = d_key_[l].data();
+            mas_.ccnt[l] = d_ccnt_[l].data();
+            mas_.cbase[l] = d_cbase_[l].data();
+        }
+    }
+    mas_.ncoarse = boff;
+    mas_.level_elems = voff;
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    have_pattern_ = true;
+    stats_["time_analyze"] = secs(t0);
+    stats_["num_parts_filled_fraction"] = nparts ? (double)pat_.nb / (32.0 * nparts) : 0.0;
+}
+
+// ------------------------------------------------------------------ factorize
+
+void HybridSolver::factorize(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                             const double *values)
+{
+    if (!outer || !inner || !values || n <= 0 || nnz < 0) fail(LSS_ERR_INVALID_ARGUMENT, "invalid matrix arguments");
+    auto t0 = clk::now();
+    factorized_ = false;
+    invalidate_graph();
+    if (!have_pattern_ || pat_.n != n || pat_.nnz != nnz || pat_.hash != pattern_hash(n, nnz, outer, inner))
+        analyze(n, nnz, outer, inner);
+    auto t1 = clk::now();
+    // values -> device (pinned staging), gather into the BSR layout
+    double *pin = (double *)pin_.get((size_t)nnz * sizeof(double));
+    std::memcpy(pin, values, (size_t)nnz * sizeof(double));
+    d_csc_.resize(nnz);
+    LSS_CUDA(cudaMemcpyAsync(d_csc_.data(), pin, (size_t)nnz * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    d_bad_.zero(stream_);
+    launch_check_finite(nnz, d_csc_.data(), d_bad_.data(), stream_);
+    mas_fp32_ = p_.mixed;
+    if (p_.mixed) d_vals32_.resize(pat_.src.size());
+    else d_vals32_.release();
+    launch_gather_values((int64_t)pat_.src.size(), d_src_.data(), d_csc_.data(), d_vals_.data(),
+                         p_.mixed ? d_vals32_.data() : nullptr, stream_);
+    A_.vals = d_vals_.data();
+    A_.vals32 = p_.mixed ? d_vals32_.data() : nullptr;
+    int bad = 0;
+    LSS_CUDA(cudaMemcpyAsync(&bad, d_bad_.data(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    if (bad) fail(LSS_ERR_NONFINITE, "the matrix holds NaN or Inf values");
+    stats_["time_copy_matrix_to_gpu"] = secs(t1);
+
+    // stiff DOFs
+    auto t2 = clk::now();
+    CscView A{n, nnz, outer, inner, values};
+    select_stiff(A);
+    stats_["time_bad_dof_selection"] = secs(t2);
+    auto t3 = clk::now();
+    setup_stiff();
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    stats_["time_factorize_submatrix"] = secs(t3);
+    auto t4 = clk::now();
+    setup_mas();
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    stats_["time_mas_setup"] = secs(t4);
+    ensure_vectors();
+    d_csc_.release();
+    factorized_ = true;
+    stats_["time_factorize"] = secs(t0);
+}
+
+void HybridSolver::set_problematic_dofs(const int32_t *idx, int32_t count)
+{
+    if (count < 0 || (count > 0 && !idx)) fail(LSS_ERR_INVALID_ARGUMENT, "invalid problematic DOF list");
+    user_dofs_.assign(idx, idx + count);
+    std::sort(user_dofs_.begin(), user_dofs_.end());
+    user_dofs_.erase(std::unique(user_dofs_.begin(), user_dofs_.end()), user_dofs_.end());
+}
+
+void HybridSolver::select_stiff(const CscView &A)
+{
+    gmm_sel_.clear();
+    subs_.clear();
+    if (!p_.do_hybrid) return;
+    std::vector<int32_t> sel;
+    if (p_.select_l1) {
+        const int32_t n = A.n;
+        DBuf<double> rn(n);
+        DBuf<GmmState> st(1);
+        st.zero(stream_);
+        if (d_outer_.size() != (size_t)n + 1) d_outer_.upload(A.outer, (size_t)n + 1, stream_);
+        launch_row_l1_norms(n, A.nnz, d_outer_.data(), d_csc_.data(), rn.data(), stream_);
+        launch_gmm(n, rn.data(), st.data(), p_.max_gmm_iterations, p_.gmm_tol, gr_, stream_);
+        const int nblk = (n + 255) / 256;
+        DBuf<int32_t> bcount(nblk), boffs(nblk);
+        DBuf<double> bmargin(nblk);
+        launch_gmm_mark(n, rn.data(), st.data(), p_.jump_threshold, bcount.data(), bmargin.data(), stream_);
+        std::vector<int32_t> hc = bcount.download(stream_);
+        std::vector<double> hm = bmargin.download(stream_);
+        std::vector<GmmState> hs = st.download(stream_);
+        std::vector<int32_t> ho(nblk);
+        int64_t total = 0;
+        for (int b = 0; b < nblk; ++b) {
+            ho[b] = (int32_t)total;
+            total += hc[b];
+        }
+        double margin = INFINITY;
+        for (double m : hm) margin = std::min(margin, m);
+        sel.resize(total);
+        if (total > 0) {
+            boffs.upload(ho, stream_);
+            DBuf<int32_t> out(total);
+            launch_gmm_scatter(n, rn.data(), st.data(), p_.jump_threshold, boffs.data(), out.data(), stream_);
+            sel = out.download(stream_);
+        }
+        const GmmState &g = hs[0];
+        stats_["gmm_global_mean"] = g.mean;
+        stats_["gmm_global_var"] = g.var;
+        stats_["gmm_mean_0"] = g.m0;
+        stats_["gmm_mean_1"] = g.m1;
+        stats_["gmm_var_0"] = g.v0;
+        stats_["gmm_var_1"] = g.v1;
+        stats_["gmm_iters"] = g.converged ? g.esteps - 1 : g.esteps;
+        stats_["gmm_min_log_margin"] = std::isfinite(margin) ? margin : -1.0;
+    } else {
+        for (int32_t v : user_dofs_)
+            if (v >= 0 && v < A.n) sel.push_back(v);
+    }
+    gmm_sel_ = sel;
+    // GPUHybrid.cu:221-238
+    if (p_.decompose) {
+        FilterCounters fc;
+        sel = filter_subdomains(A, sel, p_.min_sub, p_.max_sub, p_.cond_threshold, &fc);
+        stats_["filter_too_small"] = fc.too_small;
+        stats_["filter_too_large"] = fc.too_large;
+        stats_["filter_not_poorly_conditioned"] = fc.not_poorly_conditioned;
+    }
+    if (p_.expand && !sel.empty()) sel = expand_subdomains(A, sel);
+    if (sel.empty()) return;
+    // Without decompose_subdomains the reference factors one block with every
+    // selected DOF; its inverse is block diagonal over the connected components,
+    // so factoring the components separately applies the same operator.
+    subs_ = decompose_subdomains(A, sel, p_.decompose ? (int64_t)p_.max_sub : INT64_MAX);
+}
+
+void HybridSolver::setup_stiff()
+{
+    stiff_ = StiffDev();
+    d_sdofs_.release();
+    d_ssub_.release();
+    d_soff_.release();
+    d_sinvoff_.release();
+    d_sinv_.release();
+    d_sinv32_.release();
+    d_st_.release();
+    if (subs_.empty()) return;
+    const int bd = pat_.bd;
+    std::vector<int32_t> dofs, sub_of, off{0};
+    std::vector<int64_t> inv_off;
+    int64_t inv_total = 0;
+    for (size_t s = 0; s < subs_.size(); ++s) {
+        std::vector<int32_t> d(subs_[s].size());
+        for (size_t k = 0; k < d.size(); ++k) {
+            const int32_t g = subs_[s][k];
+            d[k] = pat_.part.perm[g / bd] * bd + g % bd;
+        }
+        std::sort(d.begin(), d.end());
+        dofs.insert(dofs.end(), d.begin(), d.end());
+        sub_of.insert(sub_of.end(), d.size(), (int32_t)s);
+        off.push_back((int32_t)dofs.size());
+        inv_off.push_back(inv_total);
+        inv_total += (int64_t)d.size() * (int64_t)d.size();
+    }
+    d_sdofs_.upload(dofs, stream_);
+    d_ssub_.upload(sub_of, stream_);
+    d_soff_.upload(off, stream_);
+    d_sinvoff_.upload(inv_off, stream_);
+    d_sinv_.resize(inv_total);
+    d_sinv_.zero(stream_);
+    d_st_.resize(dofs.size());
+    stiff_.nsub = (int32_t)subs_.size();
+    stiff_.ndof = (int32_t)dofs.size();
+    stiff_.dofs = d_sdofs_.data();
+    stiff_.sub_of = d_ssub_.data();
+    stiff_.off = d_soff_.data();
+    stiff_.inv_off = d_sinvoff_.data();
+    stiff_.inv = d_sinv_.data();
+    stiff_.t = d_st_.data();
+    launch_stiff_extract(A_, stiff_, d_sinv_.data(), stream_);
+    d_bad_.zero(stream_);
+    launch_stiff_invert(stiff_, off.data(), stiff_.nsub, inv_off.data(), d_sinv_.data(), d_bad_.data(), stream_);
+    int bad = 0;
+    LSS_CUDA(cudaMemcpyAsync(&bad, d_bad_.data(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    if (bad) fail(LSS_ERR_NOT_SPD, "a stiff subdomain block has a zero or non-finite pivot");
+    if (p_.float_subdomains) {
+        d_sinv32_.resize(inv_total);
+        launch_stiff_to_fp32(inv_total, d_sinv_.data(), d_sinv32_.data(), stream_);
+        stiff_.inv32 = d_sinv32_.data();
+    }
+    int64_t maxm = 0;
+    for (const auto &s : subs_) maxm = std::max<int64_t>(maxm, (int64_t)s.size());
+    stats_["max_subdomain_dofs"] = (double)maxm;
+}
+
+void HybridSolver::setup_mas()
+{
+    const int bd = pat_.bd, N = 32 * bd;
+    const int64_t nparts = mas_.nparts, ncoarse = mas_.ncoarse;
+    const int64_t te = mas_.tile_elems;
+    const size_t esz = mas_fp32_ ? sizeof(float) : sizeof(double);
+    d_inv0_.resize(nparts * te * esz);
+    d_invc_.resize(std::max<int64_t>(ncoarse, 1) * te * esz);
+    d_bad_.zero(stream_);
+    {
+        // level 0 (no atomics: every entry comes from its own row)
+        DBuf<double> stage((size_t)nparts * N * N);
+        stage.zero(stream_);
+        launch_mas_assemble0(A_, d_part_of_.data(), d_part_off_.data(), stage.data(), stream_);
+        launch_mas_invert(bd, nparts, stage.data(), d_inv0_.data(), mas_fp32_, d_bad_.data(), stream_);
+        LSS_CUDA(cudaStreamSynchronize(stream_));
+    }
+    if (ncoarse > 0) {
+        DBuf<double> stage((size_t)ncoarse * N * N);
+        stage.zero(stream_);
+        launch_mas_assemble_coarse(A_, mas_, d_cmap_.data(), stage.data(), stream_);
+        launch_mas_invert(bd, ncoarse, stage.data(), d_invc_.data(), mas_fp32_, d_bad_.data(), stream_);
+        LSS_CUDA(cudaStreamSynchronize(stream_));
+    }
+    int bad = 0;
+    LSS_CUDA(cudaMemcpyAsync(&bad, d_bad_.data(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    if (bad) fail(LSS_ERR_NOT_SPD, "[MAS] packed inverse failed (zero or non-finite pivot)");
+    d_v_.resize(std::max<int64_t>(mas_.level_elems, 1) * esz);
+    d_u_.resize(std::max<int64_t>(mas_.level_elems, 1) * esz);
+    d_v_.zero(stream_);
+    d_u_.zero(stream_);
+    stats_["mas_inverse_bytes"] = (double)(nparts + ncoarse) * te * esz;
+}
+
+void HybridSolver::ensure_vectors()
+{
+    const int64_t n = n_vec();
+    for (DBuf<double> *b : {&d_x_, &d_b_, &d_r_, &d_p_, &d_z_, &d_ap_, &d_w_, &d_tmp_}) b->resize(n);
+}
+
+// ------------------------------------------------------------------ preconditioner
+
+void HybridSolver::mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode)
+{
+    launch_mas_apply(mas_, d_inv0_.data(), d_invc_.data(), d_v_.data(), d_u_.data(), mas_fp32_, xin, z, acc, rdot,
+                     d_state_.data(), dot_mode, gr_, &d_state_.data()->done, stream_);
+}
+
+void HybridSolver::rz_dot(const double *r, const double *z, int dot_mode)
+{
+    launch_pcg_rz(n_vec(), r, z, d_state_.data(), dot_mode, gr_, stream_);
+}
+
+// z = M^-1 r.  dot_mode 0: nothing; 1: gamma = r.z; 2: beta, gamma update.
+void HybridSolver::precond(const double *r, double *z, int dot_mode)
+{
+    const int *done = &d_state_.data()->done;
+    const bool stiff = p_.do_hybrid && stiff_.ndof > 0;
+    if (!stiff) {  // GPUHybrid.cu:523-527
+        mas_apply(r, z, false, r, dot_mode);
+        return;
+    }
+    if (!p_.multiplicative) {  // MASSolver.cu:583-615: z = M r + S^T A_SS^-1 S r
+        mas_apply(r, z, false, nullptr, 0);
+        launch_stiff_gather(A_, stiff_, r, nullptr, false, done, stream_);
+        launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_);
+        if (dot_mode) rz_dot(r, z, dot_mode);
+        return;
+    }
+    // GPUHybrid.cu:528-540: z1 = M r; z2 = z1 + S^T A_SS^-1 S (r - A z1); z = z2 + M (r - A z2)
+    mas_apply(r, z, false, nullptr, 0);
+    launch_stiff_gather(A_, stiff_, r, z, true, done, stream_);
+    launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_);
+    launch_residual_spmv(A_, r, z, d_w_.data(), p_.mixed, done, stream_);
+    mas_apply(d_w_.data(), z, true, r, dot_mode);
+}
+
+// ------------------------------------------------------------------ PCG
+
+void HybridSolver::iteration()
+{
+    launch_pcg_spmv_alpha(A_, d_p_.data(), d_ap_.data(), d_state_.data(), gr_, stream_);
+    launch_pcg_update_xr(n_vec(), d_x_.data(), d_r_.data(), d_p_.data(), d_ap_.data(), d_state_.data(), gr_,
+                         stream_);
+    precond(d_r_.data(), d_z_.data(), 2);
+    launch_pcg_update_p(n_vec(), d_p_.data(), d_z_.data(), d_state_.data(), stream_);
+}
+
+void HybridSolver::launch_chunk(int iters)
+{
+    if (!p_.use_graphs) {
+        for (int k = 0; k < iters; ++k) iteration();
+        return;
+    }
+    if (!graph_exec_ || graph_iters_ != iters) {
+        invalidate_graph();
+        cudaGraph_t g = nullptr;
+        LSS_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        try {
+            for (int k = 0; k < iters; ++k) iteration();
+        } catch (...) {
+            cudaStreamEndCapture(stream_, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        LSS_CUDA(cudaStreamEndCapture(stream_, &g));
+        LSS_CUDA(cudaGraphInstantiate(&graph_exec_, g, 0));
+        cudaGraphDestroy(g);
+        graph_iters_ = iters;
+    }
+    LSS_CUDA(cudaGraphLaunch(graph_exec_, stream_));
+}
+
+void HybridSolver::run_pcg()
+{
+    const int64_t n = n_vec();
+    double *bb_d = d_scalar_.data();
+    launch_dot(n, d_b_.data(), d_b_.data(), bb_d, gr_, stream_);
+    double bb = 0.0;
+    LSS_CUDA(cudaMemcpyAsync(&bb, bb_d, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    if (!std::isfinite(bb)) fail(LSS_ERR_NONFINITE, "the right-hand side holds NaN or Inf values");
+    rhs_norm_ = std::sqrt(bb);
+    refinements_ = 0;
+    if (!(bb > 0.0)) {  // GPUHybrid.cu:1428-1439
+        d_x_.zero(stream_);
+        num_iterations_ = 0;
+        final_res_norm_ = 0.0;
+        stop_reason_ = STOP_CONVERGED_ABS;
+        LSS_CUDA(cudaStreamSynchronize(stream_));
+        return;
+    }
+    PcgState hs{};
+    hs.bb = bb;
+    hs.rel_eps = p_.rel_tol * p_.rel_tol;
+    hs.abs_eps = p_.abs_tol * p_.abs_tol;
+    hs.max_iter = p_.max_iter;
+    hs.iter = 0;
+    hs.done = STOP_RUNNING;
+    *h_state_ = hs;
+    LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
+    int launched = 0;
+    double res2 = 0.0;
+    for (int attempt = 0;; ++attempt) {
+        // r = b - A x; z = M r; p = z; gamma = r.z   (GPUHybrid.cu:1441-1451)
+        launch_residual_spmv(A_, d_b_.data(), d_x_.data(), d_r_.data(), false, nullptr, stream_);
+        if (p_.max_iter > 0) {
+            precond(d_r_.data(), d_z_.data(), 1);
+            launch_copy(n, d_z_.data(), d_p_.data(), nullptr, stream_);
+        }
+        while (launched < p_.max_iter) {
+            const int chunk = std::min(p_.check_every, p_.max_iter - launched);
+            launch_chunk(chunk);
+            launched += chunk;
+            LSS_CUDA(cudaMemcpyAsync(h_state_, d_state_.data(), sizeof(PcgState), cudaMemcpyDeviceToHost, stream_));
+            LSS_CUDA(cudaStreamSynchronize(stream_));
+            if (h_state_->done) break;
+        }
+        // true residual (GPUHybrid.cu:383-386)
+        launch_residual_spmv(A_, d_b_.data(), d_x_.data(), d_w_.data(), false, nullptr, stream_);
+        launch_dot(n, d_w_.data(), d_w_.data(), bb_d, gr_, stream_);
+        LSS_CUDA(cudaMemcpyAsync(&res2, bb_d, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+        LSS_CUDA(cudaMemcpyAsync(h_state_, d_state_.data(), sizeof(PcgState), cudaMemcpyDeviceToHost, stream_));
+        LSS_CUDA(cudaStreamSynchronize(stream_));
+        const int reason = h_state_->done;
+        const bool converged = reason == STOP_CONVERGED_REL || reason == STOP_CONVERGED_ABS;
+        const bool true_ok = !(hs.rel_eps > 0) || res2 / bb <= hs.rel_eps;
+        if (converged && !true_ok && attempt < p_.max_refinements && launched < p_.max_iter) {
+            // the recurrence residual drifted from the true one: restart from x
+            ++refinements_;
+            h_state_->done = STOP_RUNNING;
+            LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
+            continue;
+        }
+        break;
+    }
+    num_iterations_ = h_state_->iter;
+    stop_reason_ = h_state_->done ? h_state_->done : STOP_MAX_ITER;
+    final_res_norm_ = std::sqrt(res2);
+}
+
+void HybridSolver::solve_host(const double *b, double *x)
+{
+    if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "solve called before factorize");
+    if (!b || !x) fail(LSS_ERR_INVALID_ARGUMENT, "null vector");
+    auto t0 = clk::now();
+    const int64_t n = n_vec();
+    double *pin = (double *)pin_.get((size_t)n * sizeof(double) * 2);
+    std::memcpy(pin, b, (size_t)n * sizeof(double));
+    std::memcpy(pin + n, x, (size_t)n * sizeof(double));
+    LSS_CUDA(cudaMemcpyAsync(d_tmp_.data(), pin, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_b_.data(), true, stream_);
+    LSS_CUDA(cudaMemcpyAsync(d_tmp_.data(), pin + n, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_x_.data(), true, stream_);
+    run_pcg();
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_x_.data(), d_tmp_.data(), false, stream_);
+    LSS_CUDA(cudaMemcpyAsync(pin, d_tmp_.data(), (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    std::memcpy(x, pin, (size_t)n * sizeof(double));
+    stats_["time_solve"] = secs(t0);
+}
+
+void HybridSolver::solve_device(const double *d_b, double *d_x, cudaStream_t user)
+{
+    if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "solve called before factorize");
+    auto t0 = clk::now();
+    if (user) LSS_CUDA(cudaStreamSynchronize(user));
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_b, d_b_.data(), true, stream_);
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_x, d_x_.data(), true, stream_);
+    run_pcg();
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_x_.data(), d_x, false, stream_);
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    stats_["time_solve"] = secs(t0);
+}
+
+void HybridSolver::grad_pattern_device(const double *d_lambda, const double *d_x, double *d_dA, cudaStream_t user)
+{
+    if (!have_pattern_) fail(LSS_ERR_NOT_FACTORIZED, "no matrix pattern");
+    if (d_outer_.size() != h_outer_.size()) d_outer_.upload(h_outer_, stream_);
+    if (d_inner_.size() != h_inner_.size()) d_inner_.upload(h_inner_, stream_);
+    if (user) LSS_CUDA(cudaStreamSynchronize(user));
+    launch_grad_pattern(pat_.n, d_outer_.data(), d_inner_.data(), d_lambda, d_x, d_dA, stream_);
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void HybridSolver::grad_pattern_host(const double *lambda, const double *x, double *dA)
+{
+    if (!have_pattern_) fail(LSS_ERR_NOT_FACTORIZED, "no matrix pattern");
+    // dL/dA_ij = -lambda_i x_j on the stored pattern (outer index = row)
+    for (int32_t i = 0; i < pat_.n; ++i)
+        for (int32_t k = h_outer_[i]; k < h_outer_[i + 1]; ++k) dA[k] = -lambda[i] * x[h_inner_[k]];
+}
+
+// ------------------------------------------------------------------ operator access
+
+void HybridSolver::op_spmv(const double *x, double *y)
+{
+    if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "no factorized operator");
+    const int64_t n = n_vec();
+    LSS_CUDA(cudaMemcpyAsync(d_tmp_.data(), x, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_p_.data(), true, stream_);
+    launch_spmv(A_, d_p_.data(), d_ap_.data(), nullptr, stream_);
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_ap_.data(), d_tmp_.data(), false, stream_);
+    LSS_CUDA(cudaMemcpyAsync(y, d_tmp_.data(), n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void HybridSolver::op_mas(const double *r, double *z)
+{
+    if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "no factorized operator");
+    const int64_t n = n_vec();
+    PcgState hs{};
+    *h_state_ = hs;
+    LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
+    LSS_CUDA(cudaMemcpyAsync(d_tmp_.data(), r, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_r_.data(), true, stream_);
+    mas_apply(d_r_.data(), d_z_.data(), false, nullptr, 0);
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_z_.data(), d_tmp_.data(), false, stream_);
+    LSS_CUDA(cudaMemcpyAsync(z, d_tmp_.data(), n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void HybridSolver::op_precond(const double *r, double *z)
+{
+    if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "no factorized operator");
+    const int64_t n = n_vec();
+    PcgState hs{};
+    *h_state_ = hs;
+    LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
+    LSS_CUDA(cudaMemcpyAsync(d_tmp_.data(), r, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_r_.data(), true, stream_);
+    precond(d_r_.data(), d_z_.data(), 0);
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_z_.data(), d_tmp_.data(), false, stream_);
+    LSS_CUDA(cudaMemcpyAsync(z, d_tmp_.data(), n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
+{
+    if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "no factorized operator");
+    if (reps < 1) reps = 1;
+    const int64_t n = n_vec();
+    const int bd = pat_.bd;
+    const int64_t nnzb = pat_.rows.back();
+    PcgState hs{};
+    hs.bb = 1.0;
+    hs.max_iter = 1 << 30;
+    hs.gamma = 1.0;
+    *h_state_ = hs;
+    LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
+    // deterministic non-trivial operands
+    std::vector<double> h(n);
+    for (int64_t i = 0; i < n; ++i) h[i] = 1.0 + 1e-3 * (double)(i % 97);
+    LSS_CUDA(cudaMemcpyAsync(d_p_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    LSS_CUDA(cudaMemcpyAsync(d_r_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    LSS_CUDA(cudaMemcpyAsync(d_x_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    LSS_CUDA(cudaMemcpyAsync(d_z_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    auto body = [&]() {
+        switch (kind) {
+        case 0: launch_spmv(A_, d_p_.data(), d_ap_.data(), nullptr, stream_); break;
+        case 1: mas_apply(d_r_.data(), d_z_.data(), false, nullptr, 0); break;
+        case 2: precond(d_r_.data(), d_z_.data(), 0); break;
+        default: iteration(); break;
+        }
+    };
+    body();
+    cudaEvent_t e0, e1;
+    LSS_CUDA(cudaEventCreate(&e0));
+    LSS_CUDA(cudaEventCreate(&e1));
+    LSS_CUDA(cudaEventRecord(e0, stream_));
+    for (int k = 0; k < reps; ++k) body();
+    LSS_CUDA(cudaEventRecord(e1, stream_));
+    LSS_CUDA(cudaEventSynchronize(e1));
+    float t = 0.f;
+    LSS_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / reps;
+    const double spmv_bytes = (double)nnzb * (bd * bd * 8 + 4) + (pat_.nb + 1) * 4.0 + 2.0 * n * 8;
+    const double esz = mas_fp32_ ? 4.0 : 8.0;
+    const double mas_bytes = (double)(mas_.nparts + mas_.ncoarse) * mas_.tile_elems * esz + 2.0 * n * 8 +
+                             (double)pat_.nb * (1 + 4);
+    switch (kind) {
+    case 0: *bytes = spmv_bytes; break;
+    case 1: *bytes = mas_bytes; break;
+    default: *bytes = 0; break;
+    }
+}
+
+}  // namespace lss

@@ -1,0 +1,116 @@
+// The GPUHybrid-compatible solver object behind the C ABI.
+#pragma once
+
+#include <chrono>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "kernels.hpp"
+#include "lss_common.hpp"
+#include "pattern.hpp"
+#include "postproc.hpp"
+
+namespace lss {
+
+class HybridSolver {
+public:
+    explicit HybridSolver(const Params &p);
+    ~HybridSolver();
+    HybridSolver(const HybridSolver &) = delete;
+    HybridSolver &operator=(const HybridSolver &) = delete;
+
+    void set_parameters(const char *json);
+    std::string info_json() const;
+    std::string name() const;
+
+    void analyze(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner);
+    void factorize(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner, const double *values);
+    void set_problematic_dofs(const int32_t *idx, int32_t count);
+    void solve_host(const double *b, double *x);
+    void solve_device(const double *d_b, double *d_x, cudaStream_t user_stream);
+    void grad_pattern_host(const double *lambda, const double *x, double *dA);
+    void grad_pattern_device(const double *d_lambda, const double *d_x, double *d_dA, cudaStream_t user_stream);
+
+    // operator-level access (original ordering, host pointers)
+    void op_spmv(const double *x, double *y);
+    void op_mas(const double *r, double *z);
+    void op_precond(const double *r, double *z);
+    void op_time(int kind, int reps, double *ms, double *bytes);
+
+    const std::vector<int32_t> &gmm_selection() const { return gmm_sel_; }
+    const std::vector<std::vector<int32_t>> &subdomains() const { return subs_; }
+    std::vector<int32_t> selected() const;
+    const Pattern &pattern() const { return pat_; }
+    bool factorized() const { return factorized_; }
+    int32_t n() const { return pat_.n; }
+
+    std::string last_error;
+
+private:
+    void select_stiff(const CscView &A);
+    void setup_stiff();
+    void setup_mas();
+    void ensure_vectors();
+    void run_pcg();
+    void precond(const double *r, double *z, int dot_mode);
+    void mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode);
+    void iteration();
+    void launch_chunk(int iters);
+    void invalidate_graph();
+    void rz_dot(const double *r, const double *z, int dot_mode);
+    int64_t n_vec() const { return (int64_t)pat_.nb * pat_.bd; }
+
+    Params p_;
+    cudaStream_t stream_ = nullptr;
+    bool have_pattern_ = false;
+    bool factorized_ = false;
+    Pattern pat_;
+    CoarseSpace cs_;
+    std::vector<int32_t> user_dofs_;
+    std::vector<int32_t> h_outer_, h_inner_;  // copy of the analysed pattern (adjoint)
+    std::vector<int32_t> gmm_sel_;
+    std::vector<std::vector<int32_t>> subs_;
+    std::map<std::string, double> stats_;
+    std::map<std::string, std::string> sstats_;
+
+    // operator
+    BsrDev A_;
+    DBuf<int32_t> d_rows_, d_cols_, d_perm_, d_outer_, d_inner_;
+    DBuf<double> d_vals_, d_csc_;
+    DBuf<float> d_vals32_;
+    DBuf<int64_t> d_src_;
+    // MAS
+    MasDev mas_;
+    DBuf<int32_t> d_part_off_, d_cbase0_, d_part_of_, d_cmap_;
+    DBuf<uint8_t> d_key0_, d_ccnt0_;
+    std::vector<DBuf<uint8_t>> d_key_, d_ccnt_;
+    std::vector<DBuf<int32_t>> d_cbase_;
+    DBuf<char> d_inv0_, d_invc_, d_v_, d_u_;
+    bool mas_fp32_ = false;
+    // stiff blocks
+    StiffDev stiff_;
+    DBuf<int32_t> d_sdofs_, d_ssub_, d_soff_;
+    DBuf<int64_t> d_sinvoff_;
+    DBuf<double> d_sinv_, d_st_;
+    DBuf<float> d_sinv32_;
+    // PCG
+    DBuf<double> d_x_, d_b_, d_r_, d_p_, d_z_, d_ap_, d_w_, d_tmp_;
+    DBuf<PcgState> d_state_;
+    PcgState *h_state_ = nullptr;
+    DBuf<double> d_partials_, d_scalar_;
+    DBuf<unsigned> d_counter_;
+    DBuf<int> d_bad_;
+    GridReduce gr_;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    int graph_iters_ = 0;
+    PinnedBuf pin_;
+
+    // last solve
+    int num_iterations_ = 0;
+    double final_res_norm_ = 0.0, rhs_norm_ = 0.0;
+    int stop_reason_ = 0;
+    int refinements_ = 0;
+};
+
+}  // namespace lss

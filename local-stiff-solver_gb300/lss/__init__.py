@@ -1,0 +1,10 @@
+"""lss -- GB300-native locally-stiff linear solver (Python side).
+
+The solver itself is ``liblss.so`` (hand-written sm_103a CUDA + C++ host
+library + the C ABI of include/lss.h); this package loads it, mirrors the
+reference's linear-solver interface (``lss.Solver``), builds it in-tree
+(``lss.build``) and generates the synthetic workloads (``lss.gen``).
+"""
+from .solver import LssError, Solver, load, row_l1_norms  # noqa: F401
+
+__all__ = ["Solver", "LssError", "load", "row_l1_norms"]
