@@ -12,6 +12,11 @@ size_t &alloc_cap_bytes()
     static size_t cap = 0;
     return cap;
 }
+size_t &alloc_cap_base()
+{
+    static size_t base = 0;
+    return base;
+}
 size_t &alloc_live_bytes()
 {
     static size_t live = 0;
@@ -96,7 +101,10 @@ lss_status lss_create(const char *params_json, lss_solver **out)
     lss::HybridSolver *impl = nullptr;
     lss_status st = guarded(nullptr, [&]() {
         lss::Params p = lss::parse_params(params_json, lss::Params());
-        if (p.memory_cap_bytes) lss::alloc_cap_bytes() = p.memory_cap_bytes;
+        if (p.memory_cap_bytes) {
+            lss::alloc_cap_base() = lss::alloc_live_bytes();
+            lss::alloc_cap_bytes() = p.memory_cap_bytes;
+        }
         impl = new lss::HybridSolver(p);
     });
     if (st != LSS_OK) return st;
@@ -245,6 +253,10 @@ lss_status lss_op_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer, con
 {
     if (n <= 0 || nnz < 0 || !outer || !values || !rn) return LSS_ERR_INVALID_ARGUMENT;
     return guarded(nullptr, [&]() {
+        if (outer[0] != 0 || (int64_t)outer[n] != nnz)
+            lss::fail(LSS_ERR_INVALID_ARGUMENT, "outer index must start at 0 and end at nnz");
+        for (int32_t i = 0; i < n; ++i)
+            if (outer[i + 1] < outer[i]) lss::fail(LSS_ERR_INVALID_ARGUMENT, "outer index is not monotone");
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
             cudaGetLastError();
@@ -291,6 +303,7 @@ lss_status lss_op_time(lss_solver *s, int32_t kind, int32_t reps, double *ms_per
 
 lss_status lss_set_memory_cap(size_t bytes)
 {
+    lss::alloc_cap_base() = lss::alloc_live_bytes();
     lss::alloc_cap_bytes() = bytes;
     return LSS_OK;
 }

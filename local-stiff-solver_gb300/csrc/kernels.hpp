@@ -75,9 +75,12 @@ enum StopReason : int {
     STOP_NONFINITE = 7,
 };
 
+constexpr int PCG_HIST = 64;  // alpha / beta history kept for the Lanczos estimate
+
 struct PcgState {
     double bb, gamma, alpha, beta, pAp, rr, rel_eps, abs_eps;
     int iter, done, max_iter, pad;
+    double hist_alpha[PCG_HIST], hist_beta[PCG_HIST];
 };
 
 void launch_dot(int64_t n, const double *a, const double *b, double *out, GridReduce gr, cudaStream_t s);
@@ -129,9 +132,10 @@ void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, b
                        cudaStream_t s);
 // z = MAS^-1 xin (acc: z += MAS^-1 xin).  dot_mode 1: st->gamma = rdot.z;
 // dot_mode 2: st->beta = rdot.z / st->gamma, st->gamma = rdot.z.
+// z = scale * MAS^-1 xin, or z += scale * MAS^-1 xin with acc.
 void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
-                      const double *xin, double *z, bool acc, const double *rdot, PcgState *st, int dot_mode,
-                      GridReduce gr, const int *done, cudaStream_t s);
+                      const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
+                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s);
 
 // ---------------------------------------------------------------- stiff blocks
 struct StiffDev {

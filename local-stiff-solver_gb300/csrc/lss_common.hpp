@@ -40,8 +40,11 @@ inline void cuda_check(cudaError_t e, const char *what, const char *file, int li
 #define LSS_CUDA(call) ::lss::cuda_check((call), #call, __FILE__, __LINE__)
 #define LSS_LAUNCH_CHECK() ::lss::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
 
-// Optional allocation cap (bytes) for fault testing of the OOM path; 0 = none.
+// Optional allocation cap for fault testing of the OOM path: at most
+// alloc_cap_bytes() more bytes than were live when the cap was set
+// (alloc_cap_base()); 0 = no cap.
 size_t &alloc_cap_bytes();
+size_t &alloc_cap_base();
 size_t &alloc_live_bytes();
 
 // Owning device allocation (cudaMalloc), move-only.
@@ -66,7 +69,7 @@ public:
         release();
         if (n == 0) return;
         size_t bytes = n * sizeof(T);
-        if (alloc_cap_bytes() && alloc_live_bytes() + bytes > alloc_cap_bytes())
+        if (alloc_cap_bytes() && alloc_live_bytes() + bytes > alloc_cap_base() + alloc_cap_bytes())
             fail(LSS_ERR_OOM, "device allocation of " + std::to_string(bytes) +
                                   " bytes exceeds the configured memory cap");
         LSS_CUDA(cudaMalloc(&p_, bytes));
@@ -158,6 +161,9 @@ struct Params {
     bool mixed = false;             // FP32 MAS (+ FP32 operator inside the preconditioner)
     bool multiplicative = true;     // GPUHybrid composition; false = MASSolver additive form
     int max_coarse_levels = 4;      // MAS_MAX_COARSE_LEVEL (MASPreconditioner.hpp:11); <= 6
+    double mas_damping = 0.0;       // omega of MAS in the multiplicative form; <= 0: automatic
+    int omega_iters = 20;           // PCG-Lanczos steps of the automatic estimate
+    double omega_factor = 1.5;      // omega = omega_factor / lambda_max(MAS A)
     int check_every = 8;            // PCG iterations per host convergence poll
     int max_refinements = 2;        // true-residual restarts when the recurrence drifted
     int device = 0;

@@ -302,8 +302,8 @@ __global__ void __launch_bounds__(256) prolong_kernel(MasDev m, int l, T *__rest
 template <int BD, typename T, bool ACC, int DOT>
 __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restrict__ inv0, const T *__restrict__ u,
                                                     const double *__restrict__ xin, double *__restrict__ z,
-                                                    const double *__restrict__ rdot, PcgState *st, GridReduce gr,
-                                                    const int *done)
+                                                    double scale, const double *__restrict__ rdot, PcgState *st,
+                                                    GridReduce gr, const int *done)
 {
     if (done && *done) return;
     const int lane = threadIdx.x & 31;
@@ -325,6 +325,7 @@ __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restric
             for (int c = 0; c < BD; ++c) {
                 double val = (double)y[c];
                 if (cidx >= 0) val += (double)u1[cidx + c];
+                val *= scale;
                 const int64_t e = (int64_t)node * BD + c;
                 if (ACC) val += z[e];
                 z[e] = val;
@@ -337,7 +338,10 @@ __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restric
         if (grid_sum<1>(dot, gr, tot)) {
             // DOT == 1: initial gamma (GPUHybrid.cu:1450-1451); DOT == 2: new gamma and
             // beta = gamma_new / gamma_old (GPUHybrid.cu:1501-1504)
-            if (DOT == 2) st->beta = tot[0] / st->gamma;
+            if (DOT == 2) {
+                st->beta = tot[0] / st->gamma;
+                if (st->iter >= 1 && st->iter <= PCG_HIST) st->hist_beta[st->iter - 1] = st->beta;
+            }
             st->gamma = tot[0];
         }
     }
@@ -345,8 +349,8 @@ __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restric
 
 template <int BD, typename T>
 void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, const double *xin, double *z,
-                     bool acc, const double *rdot, PcgState *st, int dot_mode, GridReduce gr, const int *done,
-                     cudaStream_t s)
+                     bool acc, double scale, const double *rdot, PcgState *st, int dot_mode, GridReduce gr,
+                     const int *done, cudaStream_t s)
 {
     if (m.L > 1) {
         restrict0_kernel<BD, T><<<grid_for((int64_t)m.nparts * 32, 256, 152 * 16), 256, 0, s>>>(m, xin, v, done);
@@ -359,14 +363,14 @@ void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, 
     }
     const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
     if (dot_mode == 0) {
-        if (acc) symv0_kernel<BD, T, true, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
-        else symv0_kernel<BD, T, false, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
+        if (acc) symv0_kernel<BD, T, true, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
+        else symv0_kernel<BD, T, false, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
     } else if (dot_mode == 1) {
-        if (acc) symv0_kernel<BD, T, true, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
-        else symv0_kernel<BD, T, false, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
+        if (acc) symv0_kernel<BD, T, true, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
+        else symv0_kernel<BD, T, false, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
     } else {
-        if (acc) symv0_kernel<BD, T, true, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
-        else symv0_kernel<BD, T, false, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, rdot, st, gr, done);
+        if (acc) symv0_kernel<BD, T, true, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
+        else symv0_kernel<BD, T, false, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
     }
     LSS_LAUNCH_CHECK();
 }
@@ -428,12 +432,12 @@ void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, b
 }
 
 void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
-                      const double *xin, double *z, bool acc, const double *rdot, PcgState *st, int dot_mode,
-                      GridReduce gr, const int *done, cudaStream_t s)
+                      const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
+                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s)
 {
 #define LSS_MAS(BD_, T_)                                                                                          \
-    mas_apply_dot_t<BD_, T_>(m, (const T_ *)inv0, (const T_ *)invc, (T_ *)v, (T_ *)u, xin, z, acc, rdot, st,     \
-                             dot_mode, gr, done, s)
+    mas_apply_dot_t<BD_, T_>(m, (const T_ *)inv0, (const T_ *)invc, (T_ *)v, (T_ *)u, xin, z, acc, scale, rdot, \
+                             st, dot_mode, gr, done, s)
     if (fp32) {
         if (m.bd == 1) LSS_MAS(1, float);
         else if (m.bd == 2) LSS_MAS(2, float);

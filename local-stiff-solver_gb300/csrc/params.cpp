@@ -200,6 +200,9 @@ Params parse_params(const char *json, const Params &base)
                          "gb300.composition must be \"multiplicative\" or \"additive\"");
                 p.multiplicative = v.str == "multiplicative";
             } else if (k == "max_coarse_levels") p.max_coarse_levels = integer(v, kc);
+            else if (k == "mas_damping") p.mas_damping = num(v, kc);
+            else if (k == "omega_iters") p.omega_iters = integer(v, kc);
+            else if (k == "omega_factor") p.omega_factor = num(v, kc);
             else if (k == "check_every") p.check_every = integer(v, kc);
             else if (k == "max_refinements") p.max_refinements = integer(v, kc);
             else if (k == "device") p.device = integer(v, kc);
@@ -215,6 +218,9 @@ Params parse_params(const char *json, const Params &base)
     if (p.max_coarse_levels < 1 || p.max_coarse_levels > 6)
         fail(LSS_ERR_INVALID_ARGUMENT, "gb300.max_coarse_levels must be in [1, 6]");
     if (p.check_every < 1) p.check_every = 1;
+    if (p.omega_iters < 1 || p.omega_iters > 64) fail(LSS_ERR_INVALID_ARGUMENT, "gb300.omega_iters must be in [1, 64]");
+    if (!(p.omega_factor > 0.0) || p.omega_factor >= 2.0)
+        fail(LSS_ERR_INVALID_ARGUMENT, "gb300.omega_factor must be in (0, 2)");
     if (p.max_iter < 0) p.max_iter = 0;
     return p;
 }

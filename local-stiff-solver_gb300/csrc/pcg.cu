@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(256) spmv_alpha_kernel(BsrDev A, const double 
         if (alpha <= 0.0) { st->done = STOP_NEGATIVE_ALPHA; return; }
         if (alpha < DBL_MIN) { st->done = STOP_SUBNORMAL_ALPHA; return; }
         st->alpha = alpha;
+        if (st->iter <= PCG_HIST) st->hist_alpha[st->iter - 1] = alpha;
     }
 }
 
@@ -210,7 +211,10 @@ __global__ void __launch_bounds__(256) rz_kernel(int64_t n, const double *__rest
         s[0] += r[i] * z[i];
     double tot[1];
     if (grid_sum<1>(s, gr, tot)) {
-        if (mode == 2) st->beta = tot[0] / st->gamma;
+        if (mode == 2) {
+            st->beta = tot[0] / st->gamma;
+            if (st->iter >= 1 && st->iter <= PCG_HIST) st->hist_beta[st->iter - 1] = st->beta;
+        }
         st->gamma = tot[0];
     }
 }

@@ -118,6 +118,7 @@ std::string HybridSolver::info_json() const
     o << ", \"refinements\": " << refinements_;
     o << ", \"precision\": \"" << (p_.mixed ? "mixed" : "fp64") << "\"";
     o << ", \"composition\": \"" << (p_.multiplicative ? "multiplicative" : "additive") << "\"";
+    o << ", \"mas_omega\": " << omega_;
     int64_t nstiff = 0;
     for (const auto &s : subs_) nstiff += (int64_t)s.size();
     o << ", \"num_stiff_dofs\": " << nstiff << ", \"num_subdomains\": " << subs_.size();
@@ -280,6 +281,9 @@ void HybridSolver::factorize(int32_t n, int64_t nnz, const int32_t *outer, const
     ensure_vectors();
     d_csc_.release();
     factorized_ = true;
+    auto t5 = clk::now();
+    estimate_omega();
+    stats_["time_omega_estimate"] = secs(t5);
     stats_["time_factorize"] = secs(t0);
 }
 
@@ -460,10 +464,10 @@ void HybridSolver::ensure_vectors()
 
 // ------------------------------------------------------------------ preconditioner
 
-void HybridSolver::mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode)
+void HybridSolver::mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale)
 {
-    launch_mas_apply(mas_, d_inv0_.data(), d_invc_.data(), d_v_.data(), d_u_.data(), mas_fp32_, xin, z, acc, rdot,
-                     d_state_.data(), dot_mode, gr_, &d_state_.data()->done, stream_);
+    launch_mas_apply(mas_, d_inv0_.data(), d_invc_.data(), d_v_.data(), d_u_.data(), mas_fp32_, xin, z, acc, scale,
+                     rdot, d_state_.data(), dot_mode, gr_, &d_state_.data()->done, stream_);
 }
 
 void HybridSolver::rz_dot(const double *r, const double *z, int dot_mode)
@@ -475,24 +479,28 @@ void HybridSolver::rz_dot(const double *r, const double *z, int dot_mode)
 void HybridSolver::precond(const double *r, double *z, int dot_mode)
 {
     const int *done = &d_state_.data()->done;
-    const bool stiff = p_.do_hybrid && stiff_.ndof > 0;
+    const bool stiff = p_.do_hybrid && stiff_.ndof > 0 && !lanczos_mode_;
     if (!stiff) {  // GPUHybrid.cu:523-527
-        mas_apply(r, z, false, r, dot_mode);
+        mas_apply(r, z, false, r, dot_mode, 1.0);
         return;
     }
     if (!p_.multiplicative) {  // MASSolver.cu:583-615: z = M r + S^T A_SS^-1 S r
-        mas_apply(r, z, false, nullptr, 0);
+        mas_apply(r, z, false, nullptr, 0, 1.0);
         launch_stiff_gather(A_, stiff_, r, nullptr, false, done, stream_);
         launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_);
         if (dot_mode) rz_dot(r, z, dot_mode);
         return;
     }
-    // GPUHybrid.cu:528-540: z1 = M r; z2 = z1 + S^T A_SS^-1 S (r - A z1); z = z2 + M (r - A z2)
-    mas_apply(r, z, false, nullptr, 0);
+    // GPUHybrid.cu:528-540 with omega-damped MAS in place of the V-cycle:
+    // z1 = w M r; z2 = z1 + S^T A_SS^-1 S (r - A z1); z = z2 + w M (r - A z2).
+    // The symmetric product is SPD when I - w M A contracts in the A-norm;
+    // additive MAS has lambda_max(M A) of a few units, so w = omega_factor /
+    // lambda_max(M A) is estimated at factorize time (estimate_omega).
+    mas_apply(r, z, false, nullptr, 0, omega_);
     launch_stiff_gather(A_, stiff_, r, z, true, done, stream_);
     launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_);
     launch_residual_spmv(A_, r, z, d_w_.data(), p_.mixed, done, stream_);
-    mas_apply(d_w_.data(), z, true, r, dot_mode);
+    mas_apply(d_w_.data(), z, true, r, dot_mode, omega_);
 }
 
 // ------------------------------------------------------------------ PCG
@@ -599,6 +607,88 @@ void HybridSolver::run_pcg()
     final_res_norm_ = std::sqrt(res2);
 }
 
+// lambda_max(M A) for M = MAS alone from the Lanczos tridiagonal of a short
+// PCG run on a fixed probe vector (CG coefficients a_j, b_j give diagonal
+// 1/a_j + b_{j-1}/a_{j-1} and off-diagonal sqrt(b_j)/a_j); largest eigenvalue
+// of the tridiagonal by bisection on Sturm counts.
+static double tridiag_max_eig(int k, const double *d, const double *e)
+{
+    if (k <= 0) return 0.0;
+    double lo = d[0], hi = d[0];
+    for (int j = 0; j < k; ++j) {
+        const double r = (j > 0 ? std::fabs(e[j - 1]) : 0.0) + (j + 1 < k ? std::fabs(e[j]) : 0.0);
+        lo = std::min(lo, d[j] - r);
+        hi = std::max(hi, d[j] + r);
+    }
+    auto count_below = [&](double x) {
+        int c = 0;
+        double q = d[0] - x;
+        if (q < 0) ++c;
+        for (int j = 1; j < k; ++j) {
+            if (q == 0.0) q = 1e-300;
+            q = d[j] - x - e[j - 1] * e[j - 1] / q;
+            if (q < 0) ++c;
+        }
+        return c;
+    };
+    for (int it = 0; it < 200 && hi - lo > 1e-14 * std::fabs(hi); ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (count_below(mid) >= k) hi = mid;
+        else lo = mid;
+    }
+    return hi;
+}
+
+void HybridSolver::estimate_omega()
+{
+    omega_ = 1.0;
+    lambda_max_ = 0.0;
+    if (!(p_.do_hybrid && stiff_.ndof > 0 && p_.multiplicative)) return;
+    if (p_.mas_damping > 0) {
+        omega_ = p_.mas_damping;
+        return;
+    }
+    const int64_t n = n_vec();
+    const int k = p_.omega_iters;
+    // probe vector v_i = ((i * 2654435761) mod 2^32) / 2^32 - 0.5, original ordering
+    std::vector<double> h(n);
+    for (int64_t i = 0; i < n; ++i) h[i] = (double)(uint32_t)((uint64_t)(uint32_t)i * 2654435761u) / 4294967296.0 - 0.5;
+    LSS_CUDA(cudaMemcpyAsync(d_tmp_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_r_.data(), true, stream_);
+    PcgState hs{};
+    hs.bb = 1.0;
+    hs.max_iter = k;
+    *h_state_ = hs;
+    LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
+    d_x_.zero(stream_);
+    lanczos_mode_ = true;
+    try {
+        precond(d_r_.data(), d_z_.data(), 1);
+        launch_copy(n, d_z_.data(), d_p_.data(), nullptr, stream_);
+        for (int j = 0; j < k; ++j) iteration();
+    } catch (...) {
+        lanczos_mode_ = false;
+        throw;
+    }
+    lanczos_mode_ = false;
+    LSS_CUDA(cudaMemcpyAsync(h_state_, d_state_.data(), sizeof(PcgState), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    // usable steps: those with both coefficients recorded
+    int m = std::min(h_state_->iter, k);
+    std::vector<double> a(h_state_->hist_alpha, h_state_->hist_alpha + m);
+    std::vector<double> b(h_state_->hist_beta, h_state_->hist_beta + m);
+    int good = 0;
+    while (good < m && a[good] > 0 && std::isfinite(a[good]) && std::isfinite(b[good]) && b[good] >= 0) ++good;
+    std::vector<double> d(good), e(good > 0 ? good : 1);
+    for (int j = 0; j < good; ++j) {
+        d[j] = 1.0 / a[j] + (j > 0 ? b[j - 1] / a[j - 1] : 0.0);
+        if (j + 1 < good) e[j] = std::sqrt(b[j]) / a[j];
+    }
+    lambda_max_ = tridiag_max_eig(good, d.data(), e.data());
+    if (lambda_max_ > 0) omega_ = p_.omega_factor / lambda_max_;
+    stats_["mas_lambda_max"] = lambda_max_;
+}
+
 void HybridSolver::solve_host(const double *b, double *x)
 {
     if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "solve called before factorize");
@@ -674,7 +764,7 @@ void HybridSolver::op_mas(const double *r, double *z)
     LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
     LSS_CUDA(cudaMemcpyAsync(d_tmp_.data(), r, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
     launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_r_.data(), true, stream_);
-    mas_apply(d_r_.data(), d_z_.data(), false, nullptr, 0);
+    mas_apply(d_r_.data(), d_z_.data(), false, nullptr, 0, 1.0);
     launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_z_.data(), d_tmp_.data(), false, stream_);
     LSS_CUDA(cudaMemcpyAsync(z, d_tmp_.data(), n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
     LSS_CUDA(cudaStreamSynchronize(stream_));
@@ -718,7 +808,7 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
     auto body = [&]() {
         switch (kind) {
         case 0: launch_spmv(A_, d_p_.data(), d_ap_.data(), nullptr, stream_); break;
-        case 1: mas_apply(d_r_.data(), d_z_.data(), false, nullptr, 0); break;
+        case 1: mas_apply(d_r_.data(), d_z_.data(), false, nullptr, 0, 1.0); break;
         case 2: precond(d_r_.data(), d_z_.data(), 0); break;
         default: iteration(); break;
         }

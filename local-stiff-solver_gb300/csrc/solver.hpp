@@ -54,7 +54,8 @@ private:
     void ensure_vectors();
     void run_pcg();
     void precond(const double *r, double *z, int dot_mode);
-    void mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode);
+    void mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale);
+    void estimate_omega();
     void iteration();
     void launch_chunk(int iters);
     void invalidate_graph();
@@ -111,6 +112,8 @@ private:
     double final_res_norm_ = 0.0, rhs_norm_ = 0.0;
     int stop_reason_ = 0;
     int refinements_ = 0;
+    double omega_ = 1.0, lambda_max_ = 0.0;
+    bool lanczos_mode_ = false;
 };
 
 }  // namespace lss

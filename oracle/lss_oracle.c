@@ -658,6 +658,8 @@ int32_t lsso_greedy_partition(int32_t nb, const int32_t *rows, const int32_t *co
 /* Full CPU method                                                          */
 /* ===================================================================== */
 
+size_t lsso_params_size(void) { return sizeof(lsso_params); }
+
 void lsso_default_params(lsso_params *p)
 {
     /* linear-solver-spec.json defaults for /GPUHybrid (spec:646-747) */
@@ -1030,10 +1032,10 @@ void lsso_solver_precond(lsso_solver *s, const double *r, double *z)
     double *z2 = s->t0, *w = s->t1, *az = s->t2;
     if (s->p.additive) {
         mas_orig(s, r, z);
-        memset(w, 0, sizeof(double) * (size_t)n);
         memcpy(z2, z, sizeof(double) * (size_t)n);
-        stiff_correct(s, r, w, z2, 0);
+        stiff_correct(s, r, z, z2, 0);  /* z2 = M r + S^T A_SS^-1 S r */
         memcpy(z, z2, sizeof(double) * (size_t)n);
+        (void)w;
         return;
     }
     const double om = s->omega;

@@ -20,6 +20,7 @@
 #ifndef LSS_ORACLE_H
 #define LSS_ORACLE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -108,6 +109,7 @@ typedef struct {
 } lsso_params;
 
 void lsso_default_params(lsso_params *p);
+size_t lsso_params_size(void); /* sizeof(lsso_params), checked by the Python binding */
 
 typedef struct lsso_solver lsso_solver;
 /* Sets up selection + post-processing + partition + MAS + stiff factors.

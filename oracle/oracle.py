@@ -51,6 +51,8 @@ class Params(C.Structure):
         ("max_gmm_iterations", C.c_int32), ("cond_threshold", C.c_double),
         ("decompose", C.c_int32), ("min_sub", C.c_int32), ("max_sub", C.c_int32),
         ("expand", C.c_int32), ("max_coarse_levels", C.c_int32), ("threads", C.c_int32),
+        ("additive", C.c_int32), ("mas_omega", C.c_double), ("omega_iters", C.c_int32),
+        ("omega_factor", C.c_double),
     ]
 
 
@@ -94,6 +96,9 @@ def lib():
         L.lsso_mas_coarse_map.argtypes = [C.c_void_p, C.c_int32, _i32p]
         L.lsso_mas_destroy.argtypes = [C.c_void_p]
         L.lsso_default_params.argtypes = [C.POINTER(Params)]
+        L.lsso_params_size.restype = C.c_size_t
+        if L.lsso_params_size() != C.sizeof(Params):
+            raise RuntimeError("oracle.py Params does not match lsso_params in lss_oracle.h")
         L.lsso_solver_create.argtypes = [C.c_int32, _i32p, _i32p, _f64p, C.POINTER(Params),
                                          _i32p, C.c_int32, _i32p, _i32p]
         L.lsso_solver_create.restype = C.c_void_p
@@ -104,6 +109,13 @@ def lib():
         L.lsso_solver_num_subdomains.argtypes = [C.c_void_p]
         L.lsso_solver_num_subdomains.restype = C.c_int32
         L.lsso_solver_precond.argtypes = [C.c_void_p, _f64p, _f64p]
+        L.lsso_solver_omega.argtypes = [C.c_void_p]
+        L.lsso_solver_omega.restype = C.c_double
+        L.lsso_solver_lambda_max.argtypes = [C.c_void_p]
+        L.lsso_solver_lambda_max.restype = C.c_double
+        L.lsso_tridiag_max_eig.argtypes = [C.c_int32, _f64p, _f64p]
+        L.lsso_tridiag_max_eig.restype = C.c_double
+        L.lsso_probe_vector.argtypes = [C.c_int32, _f64p]
         L.lsso_solver_destroy.argtypes = [C.c_void_p]
         L.lsso_greedy_partition.argtypes = [C.c_int32, _i32p, _i32p, C.c_int32, _i32p]
         L.lsso_greedy_partition.restype = C.c_int32
@@ -375,7 +387,8 @@ class Mas:
             self.h = None
 
 
-def make_params(params: dict, threads=0, max_coarse_levels=4) -> Params:
+def make_params(params: dict, threads=0, max_coarse_levels=4, additive=False, mas_omega=0.0,
+                omega_iters=20, omega_factor=1.5) -> Params:
     p = dict(DEFAULTS)
     p.update(params)
     P = Params()
@@ -396,6 +409,10 @@ def make_params(params: dict, threads=0, max_coarse_levels=4) -> Params:
     P.expand = int(bool(p["expand_subdomains"]))
     P.max_coarse_levels = int(max_coarse_levels)
     P.threads = int(threads)
+    P.additive = int(bool(additive))
+    P.mas_omega = float(mas_omega)
+    P.omega_iters = int(omega_iters)
+    P.omega_factor = float(omega_factor)
     return P
 
 
@@ -403,10 +420,11 @@ class CpuSolver:
     """The full method on the CPU (selection, MAS, stiff Cholesky, PCG)."""
 
     def __init__(self, A, params: dict, perm=None, part_offsets=None, threads=0,
-                 max_coarse_levels=4):
+                 max_coarse_levels=4, additive=False, mas_omega=0.0, omega_iters=20, omega_factor=1.5):
         n, outer, inner, vals = _csc(A)
         self._keep = [outer, inner, vals]
-        P = make_params(params, threads, max_coarse_levels)
+        P = make_params(params, threads, max_coarse_levels, additive, mas_omega, omega_iters,
+                        omega_factor)
         st = C.c_int32(0)
         if perm is not None:
             perm = np.ascontiguousarray(perm, np.int32)
@@ -423,6 +441,14 @@ class CpuSolver:
     @property
     def num_stiff(self):
         return lib().lsso_solver_num_stiff(self.h)
+
+    @property
+    def omega(self):
+        return lib().lsso_solver_omega(self.h)
+
+    @property
+    def lambda_max(self):
+        return lib().lsso_solver_lambda_max(self.h)
 
     @property
     def num_subdomains(self):

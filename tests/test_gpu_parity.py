@@ -1,0 +1,280 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the oracle.
+
+Tolerances, stated per test:
+  * stiff-DOF index sets: identical (bit-exact integer parity);
+  * l1 row norms: 1e-13 relative (summation order differs);
+  * SpMV: 1e-13 of |A||x| per entry;
+  * MAS / hybrid preconditioner in FP64 against the oracle on the same
+    partition: 1e-8 relative (inverses computed in a different index order);
+  * FP32 MAS (mixed mode) against FP64: 2e-3 relative;
+  * solves: true relative residual <= 1e-8 and <= 1e-6 relative error against
+    scipy's FP64 sparse direct solve.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from conftest import GOLDEN, load_npz_matrix, reference_matrices
+
+pytestmark = pytest.mark.gpu
+
+PARAM_SETS = json.load(open(os.path.join(GOLDEN, "selection_golden.json")))["param_sets"]
+
+
+def _solver(params, gb300=None):
+    import lss
+    p = {"solver": "GPUHybrid", "GPUHybrid": dict(params)}
+    if gb300:
+        p["gb300"] = gb300
+    return lss.Solver.create(p)
+
+
+@pytest.fixture(scope="module")
+def elast20(built):
+    from lss import gen
+    A, b, _ = gen.workload_elasticity_inclusion(seed=0, nodes=20)
+    return A.tocsc(), b
+
+
+@pytest.fixture(scope="module")
+def lap(built):
+    from lss import gen
+    A, b, _ = gen.workload_delaunay_laplacian(seed=1, npts=30000)
+    return A.tocsc(), b
+
+
+def test_row_l1_norms_match_oracle(built):
+    import lss
+    from oracle import oracle as O
+    for name, path in reference_matrices().items():
+        A = load_npz_matrix(path)
+        g = lss.row_l1_norms(A)
+        c = O.c_row_l1_norms(A)
+        np.testing.assert_allclose(g, c, rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("name", sorted(reference_matrices()))
+@pytest.mark.parametrize("pname", sorted(PARAM_SETS))
+def test_selection_matches_golden(name, pname, golden):
+    A = load_npz_matrix(reference_matrices()[name])
+    s = _solver(dict(PARAM_SETS[pname], block_size=1))
+    s.factorize(A)
+    np.testing.assert_array_equal(s.gmm_selection(), golden[f"{name}/{pname}/gmm_selection"])
+    np.testing.assert_array_equal(s.selected_dofs(), golden[f"{name}/{pname}/selected"])
+    if PARAM_SETS[pname].get("decompose_subdomains", True):
+        offs = np.cumsum([0] + [len(x) for x in s.subdomains()])
+        np.testing.assert_array_equal(offs, golden[f"{name}/{pname}/sub_offsets"])
+    assert s.name() == "GPUHybrid"
+
+
+@pytest.mark.parametrize("case", ["elasticity", "laplacian", "lognormal_springs"])
+def test_selection_matches_oracle_on_workloads(case, built):
+    from lss import gen
+    from oracle import oracle as O
+    if case == "elasticity":
+        A, _, _ = gen.workload_elasticity_inclusion(seed=5, nodes=14, E_ratio=1e5)
+        params = {"block_size": 3, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4}
+    elif case == "laplacian":
+        A, _, _ = gen.workload_delaunay_laplacian(seed=2, npts=40000)
+        params = {"block_size": 1, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4}
+    else:
+        A, _, _ = gen.workload_elasticity_lognormal(seed=1, nodes=16)
+        params = {"block_size": 3, "gmm_jump_threshold": 10.0}
+    A = A.tocsc()
+    s = _solver(params)
+    s.factorize(A)
+    ref_all, ref_subs, _ = O.c_select_pipeline(A, params)
+    np.testing.assert_array_equal(s.selected_dofs(), ref_all)
+    got = s.subdomains()
+    assert len(got) == len(ref_subs)
+    for a, b in zip(got, ref_subs):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("bs", [1, 3])
+def test_spmv_matches_scipy(bs, elast20, lap):
+    A = elast20[0] if bs == 3 else lap[0]
+    s = _solver({"block_size": bs, "do_hybrid_precond": False})
+    s.factorize(A)
+    x = np.random.default_rng(0).standard_normal(A.shape[0])
+    y = s.spmv(x)
+    ref = A.tocsr() @ x  # outer index = row, like the reference (the matrix is symmetric)
+    bound = abs(A.tocsr()) @ abs(x)
+    assert np.all(np.abs(y - ref) <= 1e-13 * bound + 1e-300)
+
+
+def _oracle_with_product_partition(A, s, params, **kw):
+    from oracle import oracle as O
+    perm, offs = s.partition()
+    return O.CpuSolver(A, params, perm=perm, part_offsets=offs, **kw)
+
+
+@pytest.mark.parametrize("bs", [1, 3])
+def test_mas_apply_matches_oracle(bs, elast20, lap):
+    A = elast20[0] if bs == 3 else lap[0]
+    params = {"block_size": bs, "do_hybrid_precond": False}
+    s = _solver(params)
+    s.factorize(A)
+    o = _oracle_with_product_partition(A, s, params)
+    info = s.get_info()
+    r = np.random.default_rng(1).standard_normal(A.shape[0])
+    z = s.mas_apply(r)
+    zo = o.precond(r)
+    err = np.linalg.norm(z - zo) / np.linalg.norm(zo)
+    assert err < 1e-8, (err, info["mas_levels"])
+    # FP32 storage of the inverses (mixed precision mode)
+    s32 = _solver(params, {"precision": "mixed"})
+    s32.factorize(A)
+    z32 = s32.mas_apply(r)
+    assert np.linalg.norm(z32 - zo) / np.linalg.norm(zo) < 2e-3
+
+
+def test_hybrid_precond_matches_oracle(elast20):
+    A = elast20[0]
+    params = {"block_size": 3, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4}
+    s = _solver(params)
+    s.factorize(A)
+    omega = s.get_info()["mas_omega"]
+    o = _oracle_with_product_partition(A, s, params, mas_omega=omega)
+    assert o.num_stiff == len(s.selected_dofs()) > 0
+    r = np.random.default_rng(2).standard_normal(A.shape[0])
+    z = s.precond(r)
+    zo = o.precond(r)
+    assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < 1e-8
+    # the automatic damping agrees with the oracle's own estimate
+    o2 = _oracle_with_product_partition(A, s, params)
+    assert abs(o2.omega - omega) / omega < 1e-6
+    # additive composition (MASSolver.cu:583-615)
+    sa = _solver(params, {"composition": "additive"})
+    sa.factorize(A)
+    oa = _oracle_with_product_partition(A, sa, params, additive=True)
+    za, zoa = sa.precond(r), oa.precond(r)
+    assert np.linalg.norm(za - zoa) / np.linalg.norm(zoa) < 1e-8
+
+
+def _check_solution(A, b, x, rtol=1e-8, etol=1e-6):
+    rel = np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+    assert rel <= rtol, rel
+    xd = spla.spsolve(A.tocsc(), b)
+    err = np.linalg.norm(x - xd) / np.linalg.norm(xd)
+    assert err <= etol, err
+    return rel, err
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_elasticity_inclusion(precision, elast20):
+    A, b = elast20
+    s = _solver({"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0,
+                 "min_subdomain_size": 4}, {"precision": precision})
+    s.factorize(A)
+    x = s.solve(b)
+    _check_solution(A, b, x)
+    info = s.get_info()
+    assert info["status"] == "converged_rel" and info["num_iterations"] > 0
+    assert info["num_stiff_dofs"] > 0 and info["precision"] == precision
+
+
+def test_solve_reference_matrices(built):
+    for name, path in reference_matrices().items():
+        A = load_npz_matrix(path)
+        bs = 3 if name == "A_contact" else 1
+        b = np.random.default_rng(0).uniform(-1, 1, A.shape[0])
+        s = _solver({"block_size": bs, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0,
+                     "min_subdomain_size": 4, "max_iter": 20000})
+        s.factorize(A)
+        x = s.solve(b)
+        rel = np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+        assert rel <= 1e-8, (name, rel, s.get_info())
+
+
+def test_solve_laplacian_and_compositions(lap):
+    A, b = lap
+    for comp in ("multiplicative", "additive"):
+        s = _solver({"block_size": 1, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0},
+                    {"composition": comp})
+        s.factorize(A)
+        x = s.solve(b)
+        _check_solution(A, b, x)
+
+
+def test_initial_guess_and_zero_rhs(elast20):
+    A, b = elast20
+    s = _solver({"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0})
+    s.factorize(A)
+    x = s.solve(b)
+    it_cold = s.get_info()["num_iterations"]
+    x2 = s.solve(b, x.copy())  # GPUHybrid uses x as the initial guess (GPUHybrid.cu:347)
+    assert s.get_info()["num_iterations"] < it_cold
+    z = s.solve(np.zeros_like(b), np.ones_like(b))  # GPUHybrid.cu:1433-1439
+    assert np.all(z == 0) and s.get_info()["num_iterations"] == 0
+    assert np.linalg.norm(x2 - x) / np.linalg.norm(x) < 1e-6
+
+
+def test_max_iter_and_breakdown_status(elast20):
+    A, b = elast20
+    s = _solver({"block_size": 3, "relative_tolerance": 1e-14, "max_iter": 5, "gmm_jump_threshold": 10.0})
+    s.factorize(A)
+    s.solve(b)
+    info = s.get_info()
+    assert info["status"] == "max_iterations" and info["num_iterations"] == 5
+
+
+def test_problematic_dofs_and_plain_modes(elast20):
+    A, b = elast20
+    import lss
+    s = _solver({"block_size": 3, "relative_tolerance": 1e-8, "select_bad_dofs_from_l1_norm": False})
+    ref = _solver({"block_size": 3, "gmm_jump_threshold": 10.0})
+    ref.factorize(A)
+    s.set_problematic_dofs(ref.gmm_selection())
+    s.factorize(A)
+    assert s.name() == "GPUAMGF"
+    assert len(s.selected_dofs()) > 0
+    _check_solution(A, b, s.solve(b))
+    p = _solver({"block_size": 3, "relative_tolerance": 1e-8, "do_hybrid_precond": False})
+    p.factorize(A)
+    assert p.name() == "GPUAMG" and len(p.selected_dofs()) == 0
+    _check_solution(A, b, p.solve(b))
+
+
+def test_refactorize_same_pattern(elast20):
+    A, b = elast20
+    s = _solver({"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0})
+    s.analyze_pattern(A)
+    for scale in (1.0, 2.0):
+        A2 = (A * scale).tocsc()
+        s.factorize(A2)
+        _check_solution(A2, b, s.solve(b))
+
+
+def test_error_paths(elast20):
+    import lss
+    A, b = elast20
+    s = _solver({"block_size": 3})
+    with pytest.raises(lss.LssError) as e:
+        s.solve(b)
+    assert e.value.status == "LSS_ERR_NOT_FACTORIZED"
+    s.factorize(A)
+    bad = b.copy()
+    bad[3] = np.nan
+    with pytest.raises(lss.LssError) as e:
+        s.solve(bad)
+    assert e.value.status == "LSS_ERR_NONFINITE"
+    An = A.copy()
+    An.data[7] = np.inf
+    with pytest.raises(lss.LssError) as e:
+        s.factorize(An)
+    assert e.value.status == "LSS_ERR_NONFINITE"
+    # n not a multiple of the block size
+    with pytest.raises(lss.LssError) as e:
+        _solver({"block_size": 3}).factorize(sp.eye(10, format="csc"))
+    assert e.value.status == "LSS_ERR_INVALID_ARGUMENT"
+    # device memory cap: the out-of-memory path without exhausting the GPU
+    small = _solver({"block_size": 3}, {"memory_cap_bytes": 1 << 20})
+    with pytest.raises(lss.LssError) as e:
+        small.factorize(A)
+    assert e.value.status == "LSS_ERR_OOM"
+    lss.load().lss_set_memory_cap(0)
