@@ -89,6 +89,12 @@ lss_status lss_analyze_pattern(lss_solver *s, int32_t n, int64_t nnz, const int3
 lss_status lss_factorize(lss_solver *s, int32_t n, int64_t nnz, const int32_t *outer,
                          const int32_t *inner, const double *values);
 
+/* factorize with the values already in device memory (d_values[nnz] in the
+ * storage order of the analysed pattern), ordered on `stream` (a cudaStream_t;
+ * NULL = the solver's own stream).  Requires a previous analyze_pattern or
+ * factorize with the same pattern.  For callers that assemble on the GPU. */
+lss_status lss_factorize_device(lss_solver *s, const double *d_values, void *stream);
+
 /* GPUHybrid::set_problematic_dofs (GPUHybrid.hpp:69): the DOF set used
  * when select_bad_dofs_from_l1_norm is false.  idx need not be sorted. */
 lss_status lss_set_problematic_dofs(lss_solver *s, const int32_t *idx, int32_t count);
@@ -101,8 +107,8 @@ lss_status lss_set_problematic_dofs(lss_solver *s, const int32_t *idx, int32_t c
 lss_status lss_solve(lss_solver *s, const double *b, double *x, int32_t nrhs, int64_t ld);
 
 /* Same as lss_solve with device pointers (one right-hand side), ordered on
- * `stream` (a cudaStream_t, NULL = the legacy default stream).  Used by the
- * PyTorch extension. */
+ * `stream` (a cudaStream_t; NULL = the solver's own stream, synchronised
+ * before returning).  Used by the PyTorch extension. */
 lss_status lss_solve_device(lss_solver *s, const double *d_b, double *d_x, void *stream);
 
 /* Backward of x = A^-1 b (no counterpart in the reference): solves

@@ -151,6 +151,12 @@ lss_status lss_factorize(lss_solver *s, int32_t n, int64_t nnz, const int32_t *o
     return guarded(s, [&]() { s->impl->factorize(n, nnz, outer, inner, values); });
 }
 
+lss_status lss_factorize_device(lss_solver *s, const double *d_values, void *stream)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->factorize_device(d_values, (cudaStream_t)stream); });
+}
+
 lss_status lss_set_problematic_dofs(lss_solver *s, const int32_t *idx, int32_t count)
 {
     if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;

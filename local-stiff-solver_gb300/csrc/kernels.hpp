@@ -44,6 +44,13 @@ void launch_gmm_mark(int32_t n, const double *rn, const GmmState *st, double thr
 void launch_gmm_scatter(int32_t n, const double *rn, const GmmState *st, double threshold,
                         const int32_t *block_offset, int32_t *out, cudaStream_t s);
 
+// Gershgorin data of the selected rows (filter_subdomains, GPUHybrid.cu:936-958):
+// for every selected original row k, diag = A_kk and off = sum of |A_kj| over
+// selected j != k, read from the permuted operator.  sel: original scalar ids.
+void launch_gershgorin(int nb, int bd, const int32_t *rows, const int32_t *cols, const double *vals,
+                       const int32_t *perm, const int32_t *sel, int32_t nsel, uint8_t *mask, double *diag,
+                       double *off, cudaStream_t s);
+
 // ---------------------------------------------------------------- operator
 struct BsrDev {
     int32_t nb = 0, bd = 1;

@@ -71,6 +71,7 @@ void clear_g2l(std::vector<int32_t> &g2l, const std::vector<int32_t> &sel)
 }  // namespace
 
 std::vector<int32_t> filter_subdomains(const CscView &A, const std::vector<int32_t> &sel,
+                                       const std::vector<double> &diag, const std::vector<double> &offsum,
                                        int32_t min_size, int32_t max_size, double cond_threshold,
                                        FilterCounters *cnt)
 {
@@ -79,18 +80,10 @@ std::vector<int32_t> filter_subdomains(const CscView &A, const std::vector<int32
     std::vector<int64_t> size(nc, 0);
     std::vector<double> lmin(nc, DBL_MAX), lmax(nc, 0.0);
     for (size_t a = 0; a < sel.size(); ++a) {
-        const int32_t k = sel[a];
-        double diag = 0.0, off = 0.0;
-        for (int64_t e = A.outer[k]; e < A.outer[k + 1]; ++e) {
-            const int32_t r = A.inner[e];
-            if (g2l[r] < 0) continue;
-            if (r == k) diag = A.values[e];
-            else off += std::fabs(A.values[e]);
-        }
         const int32_t c = label[a];
         ++size[c];
-        lmin[c] = std::min(lmin[c], diag - off);
-        lmax[c] = std::max(lmax[c], diag + off);
+        lmin[c] = std::min(lmin[c], diag[a] - offsum[a]);
+        lmax[c] = std::max(lmax[c], diag[a] + offsum[a]);
     }
     std::vector<char> keep(nc, 0);
     FilterCounters fc;

@@ -22,7 +22,10 @@ struct FilterCounters {
 // Keep the connected components of `sel` (ascending) whose size lies in
 // [min_size, max_size] and whose Gershgorin bounds flag them as poorly
 // conditioned.  Result ascending.
+// diag[a], off[a]: A_kk and sum_{j in sel, j != k} |A_kj| of k = sel[a]
+// (computed on the device, launch_gershgorin).
 std::vector<int32_t> filter_subdomains(const CscView &A, const std::vector<int32_t> &sel,
+                                       const std::vector<double> &diag, const std::vector<double> &off,
                                        int32_t min_size, int32_t max_size, double cond_threshold,
                                        FilterCounters *cnt);
 

@@ -249,7 +249,66 @@ __global__ void __launch_bounds__(256) scatter_kernel(int32_t n, const double *_
     if (flag) out[wbase[wid] + __popc(b & ((1u << lane) - 1u))] = (int32_t)i;
 }
 
+__global__ void mark_selected_kernel(int bd, const int32_t *__restrict__ perm, const int32_t *__restrict__ sel,
+                                     int32_t nsel, uint8_t *__restrict__ mask)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nsel) return;
+    const int32_t k = sel[j];
+    mask[(int64_t)perm[k / bd] * bd + k % bd] = 1;
+}
+
+__global__ void __launch_bounds__(256) gershgorin_kernel(int bd, const int32_t *__restrict__ rows,
+                                                         const int32_t *__restrict__ cols,
+                                                         const double *__restrict__ vals,
+                                                         const int32_t *__restrict__ perm,
+                                                         const int32_t *__restrict__ sel, int32_t nsel,
+                                                         const uint8_t *__restrict__ mask, double *__restrict__ diag,
+                                                         double *__restrict__ off)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= nsel) return;
+    const int32_t k = sel[j];
+    const int64_t pk = (int64_t)perm[k / bd] * bd + k % bd;
+    const int32_t I = (int32_t)(pk / bd), comp = (int32_t)(pk % bd);
+    const int32_t b = rows[I], len = rows[I + 1] - b;
+    const double *v = vals + (int64_t)b * bd * bd;
+    double d = 0.0, o = 0.0;
+    int has_d = 0;
+    for (int32_t l = lane; l < len; l += 32) {
+        const int64_t J = cols[b + l];
+        for (int c = 0; c < bd; ++c) {
+            const int64_t col = J * bd + c;
+            if (!mask[col]) continue;
+            const double a = v[(int64_t)(comp * bd + c) * len + l];
+            if (col == pk) { d = a; has_d = 1; }
+            else o += fabs(a);
+        }
+    }
+    o = warp_sum(o);
+    const unsigned who = __ballot_sync(0xffffffffu, has_d);
+    const int src = who ? __ffs(who) - 1 : 0;
+    d = __shfl_sync(0xffffffffu, d, src);
+    if (lane == 0) {
+        diag[j] = who ? d : 0.0;
+        off[j] = o;
+    }
+}
+
 }  // namespace
+
+void launch_gershgorin(int nb, int bd, const int32_t *rows, const int32_t *cols, const double *vals,
+                       const int32_t *perm, const int32_t *sel, int32_t nsel, uint8_t *mask, double *diag,
+                       double *off, cudaStream_t s)
+{
+    (void)nb;
+    if (nsel == 0) return;
+    mark_selected_kernel<<<(nsel + 255) / 256, 256, 0, s>>>(bd, perm, sel, nsel, mask);
+    gershgorin_kernel<<<(unsigned)(((int64_t)nsel * 32 + 255) / 256), 256, 0, s>>>(bd, rows, cols, vals, perm, sel,
+                                                                                  nsel, mask, diag, off);
+    LSS_LAUNCH_CHECK();
+}
 
 void launch_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer, const double *vals, double *rn,
                          cudaStream_t s)

@@ -245,11 +245,37 @@ void HybridSolver::factorize(int32_t n, int64_t nnz, const int32_t *outer, const
     if (!have_pattern_ || pat_.n != n || pat_.nnz != nnz || pat_.hash != pattern_hash(n, nnz, outer, inner))
         analyze(n, nnz, outer, inner);
     auto t1 = clk::now();
-    // values -> device (pinned staging), gather into the BSR layout
+    // values -> device through pinned staging
     double *pin = (double *)pin_.get((size_t)nnz * sizeof(double));
     std::memcpy(pin, values, (size_t)nnz * sizeof(double));
     d_csc_.resize(nnz);
     LSS_CUDA(cudaMemcpyAsync(d_csc_.data(), pin, (size_t)nnz * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    factorize_common();
+    stats_["time_copy_matrix_to_gpu"] = secs(t1) - stats_["time_factorize_device"];
+    stats_["time_factorize"] = secs(t0);
+}
+
+void HybridSolver::factorize_device(const double *d_values, cudaStream_t user)
+{
+    if (!have_pattern_) fail(LSS_ERR_NOT_FACTORIZED, "factorize_device needs analyze_pattern first");
+    if (!d_values) fail(LSS_ERR_INVALID_ARGUMENT, "null values");
+    auto t0 = clk::now();
+    factorized_ = false;
+    invalidate_graph();
+    StreamScope scope(this, user);
+    d_csc_.resize(pat_.nnz);
+    LSS_CUDA(cudaMemcpyAsync(d_csc_.data(), d_values, (size_t)pat_.nnz * sizeof(double), cudaMemcpyDeviceToDevice,
+                             stream_));
+    factorize_common();
+    stats_["time_factorize"] = secs(t0);
+}
+
+// Everything after the values are in d_csc_: gather into the operator,
+// selection, stiff factors, MAS, damping estimate.  Needs no host values.
+void HybridSolver::factorize_common()
+{
+    auto t0 = clk::now();
+    const int64_t nnz = pat_.nnz;
     d_bad_.zero(stream_);
     launch_check_finite(nnz, d_csc_.data(), d_bad_.data(), stream_);
     mas_fp32_ = p_.mixed;
@@ -263,11 +289,8 @@ void HybridSolver::factorize(int32_t n, int64_t nnz, const int32_t *outer, const
     LSS_CUDA(cudaMemcpyAsync(&bad, d_bad_.data(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
     LSS_CUDA(cudaStreamSynchronize(stream_));
     if (bad) fail(LSS_ERR_NONFINITE, "the matrix holds NaN or Inf values");
-    stats_["time_copy_matrix_to_gpu"] = secs(t1);
-
-    // stiff DOFs
     auto t2 = clk::now();
-    CscView A{n, nnz, outer, inner, values};
+    CscView A{pat_.n, pat_.nnz, h_outer_.data(), h_inner_.data(), nullptr};
     select_stiff(A);
     stats_["time_bad_dof_selection"] = secs(t2);
     auto t3 = clk::now();
@@ -284,7 +307,7 @@ void HybridSolver::factorize(int32_t n, int64_t nnz, const int32_t *outer, const
     auto t5 = clk::now();
     estimate_omega();
     stats_["time_omega_estimate"] = secs(t5);
-    stats_["time_factorize"] = secs(t0);
+    stats_["time_factorize_device"] = secs(t0);
 }
 
 void HybridSolver::set_problematic_dofs(const int32_t *idx, int32_t count)
@@ -306,7 +329,7 @@ void HybridSolver::select_stiff(const CscView &A)
         DBuf<double> rn(n);
         DBuf<GmmState> st(1);
         st.zero(stream_);
-        if (d_outer_.size() != (size_t)n + 1) d_outer_.upload(A.outer, (size_t)n + 1, stream_);
+        if (d_outer_.size() != (size_t)n + 1) d_outer_.upload(h_outer_, stream_);
         launch_row_l1_norms(n, A.nnz, d_outer_.data(), d_csc_.data(), rn.data(), stream_);
         launch_gmm(n, rn.data(), st.data(), p_.max_gmm_iterations, p_.gmm_tol, gr_, stream_);
         const int nblk = (n + 255) / 256;
@@ -347,8 +370,21 @@ void HybridSolver::select_stiff(const CscView &A)
     gmm_sel_ = sel;
     // GPUHybrid.cu:221-238
     if (p_.decompose) {
+        const int32_t m = (int32_t)sel.size();
+        std::vector<double> diag(m), off(m);
+        if (m > 0) {
+            DBuf<int32_t> dsel;
+            dsel.upload(sel, stream_);
+            DBuf<uint8_t> mask((size_t)pat_.n);
+            mask.zero(stream_);
+            DBuf<double> ddiag(m), doff(m);
+            launch_gershgorin(pat_.nb, pat_.bd, d_rows_.data(), d_cols_.data(), d_vals_.data(), d_perm_.data(),
+                              dsel.data(), m, mask.data(), ddiag.data(), doff.data(), stream_);
+            diag = ddiag.download(stream_);
+            off = doff.download(stream_);
+        }
         FilterCounters fc;
-        sel = filter_subdomains(A, sel, p_.min_sub, p_.max_sub, p_.cond_threshold, &fc);
+        sel = filter_subdomains(A, sel, diag, off, p_.min_sub, p_.max_sub, p_.cond_threshold, &fc);
         stats_["filter_too_small"] = fc.too_small;
         stats_["filter_too_large"] = fc.too_large;
         stats_["filter_not_poorly_conditioned"] = fc.not_poorly_conditioned;
@@ -532,6 +568,8 @@ void HybridSolver::launch_chunk(int iters)
             throw;
         }
         LSS_CUDA(cudaStreamEndCapture(stream_, &g));
+        size_t nodes = 0;
+        if (cudaGraphGetNodes(g, nullptr, &nodes) == cudaSuccess) stats_["kernels_per_iteration"] = (double)nodes / iters;
         LSS_CUDA(cudaGraphInstantiate(&graph_exec_, g, 0));
         cudaGraphDestroy(g);
         graph_iters_ = iters;
@@ -568,7 +606,7 @@ void HybridSolver::run_pcg()
     *h_state_ = hs;
     LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
     int launched = 0;
-    double res2 = 0.0;
+    double res2 = 0.0, prev_res2 = INFINITY;
     for (int attempt = 0;; ++attempt) {
         // r = b - A x; z = M r; p = z; gamma = r.z   (GPUHybrid.cu:1441-1451)
         launch_residual_spmv(A_, d_b_.data(), d_x_.data(), d_r_.data(), false, nullptr, stream_);
@@ -593,7 +631,11 @@ void HybridSolver::run_pcg()
         const int reason = h_state_->done;
         const bool converged = reason == STOP_CONVERGED_REL || reason == STOP_CONVERGED_ABS;
         const bool true_ok = !(hs.rel_eps > 0) || res2 / bb <= hs.rel_eps;
-        if (converged && !true_ok && attempt < p_.max_refinements && launched < p_.max_iter) {
+        // restart only while restarting still pays: the true residual has a rounding
+        // floor of about eps * || |A| |x| || that no restart can go below
+        const bool improving = res2 < 0.25 * prev_res2;
+        prev_res2 = res2;
+        if (converged && !true_ok && improving && attempt < p_.max_refinements && launched < p_.max_iter) {
             // the recurrence residual drifted from the true one: restart from x
             ++refinements_;
             h_state_->done = STOP_RUNNING;
@@ -714,7 +756,7 @@ void HybridSolver::solve_device(const double *d_b, double *d_x, cudaStream_t use
 {
     if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "solve called before factorize");
     auto t0 = clk::now();
-    if (user) LSS_CUDA(cudaStreamSynchronize(user));
+    StreamScope scope(this, user);
     launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_b, d_b_.data(), true, stream_);
     launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_x, d_x_.data(), true, stream_);
     run_pcg();
@@ -726,9 +768,9 @@ void HybridSolver::solve_device(const double *d_b, double *d_x, cudaStream_t use
 void HybridSolver::grad_pattern_device(const double *d_lambda, const double *d_x, double *d_dA, cudaStream_t user)
 {
     if (!have_pattern_) fail(LSS_ERR_NOT_FACTORIZED, "no matrix pattern");
+    StreamScope scope(this, user);
     if (d_outer_.size() != h_outer_.size()) d_outer_.upload(h_outer_, stream_);
     if (d_inner_.size() != h_inner_.size()) d_inner_.upload(h_inner_, stream_);
-    if (user) LSS_CUDA(cudaStreamSynchronize(user));
     launch_grad_pattern(pat_.n, d_outer_.data(), d_inner_.data(), d_lambda, d_x, d_dA, stream_);
     LSS_CUDA(cudaStreamSynchronize(stream_));
 }

@@ -26,6 +26,8 @@ public:
 
     void analyze(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner);
     void factorize(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner, const double *values);
+    // values in device memory (input storage order), pattern from a previous analyze/factorize
+    void factorize_device(const double *d_values, cudaStream_t user_stream);
     void set_problematic_dofs(const int32_t *idx, int32_t count);
     void solve_host(const double *b, double *x);
     void solve_device(const double *d_b, double *d_x, cudaStream_t user_stream);
@@ -48,6 +50,21 @@ public:
     std::string last_error;
 
 private:
+    // Runs a device-pointer call on the caller's stream (a non-null stream);
+    // the internal stream otherwise.  Graphs captured on either replay on both.
+    struct StreamScope {
+        HybridSolver *s;
+        cudaStream_t saved;
+        StreamScope(HybridSolver *h, cudaStream_t user) : s(h), saved(h->stream_)
+        {
+            if (user) {
+                LSS_CUDA(cudaStreamSynchronize(saved));
+                s->stream_ = user;
+            }
+        }
+        ~StreamScope() { s->stream_ = saved; }
+    };
+    void factorize_common();
     void select_stiff(const CscView &A);
     void setup_stiff();
     void setup_mas();

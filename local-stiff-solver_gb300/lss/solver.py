@@ -32,7 +32,8 @@ STATUS = {
 # symbols declared in include/lss.h
 EXPORTS = [
     "lss_status_string", "lss_last_error", "lss_create", "lss_destroy", "lss_set_parameters",
-    "lss_get_info", "lss_name", "lss_analyze_pattern", "lss_factorize", "lss_set_problematic_dofs",
+    "lss_get_info", "lss_name", "lss_analyze_pattern", "lss_factorize", "lss_factorize_device",
+    "lss_set_problematic_dofs",
     "lss_solve", "lss_solve_device", "lss_solve_transpose", "lss_grad_A_pattern",
     "lss_grad_A_pattern_device", "lss_selected_dofs", "lss_gmm_selection", "lss_subdomains",
     "lss_partition", "lss_op_row_l1_norms", "lss_op_spmv", "lss_op_mas_apply", "lss_op_precond",
@@ -71,6 +72,7 @@ def load(path: str | None = None):
     L.lss_name.argtypes = [vp, C.c_char_p, C.c_size_t]
     L.lss_analyze_pattern.argtypes = [vp, C.c_int32, C.c_int64, _i32p, _i32p]
     L.lss_factorize.argtypes = [vp, C.c_int32, C.c_int64, _i32p, _i32p, _f64p]
+    L.lss_factorize_device.argtypes = [vp, vp, vp]
     L.lss_set_problematic_dofs.argtypes = [vp, _i32p, C.c_int32]
     L.lss_solve.argtypes = [vp, _f64p, _f64p, C.c_int32, C.c_int64]
     L.lss_solve_device.argtypes = [vp, vp, vp, vp]
@@ -193,6 +195,14 @@ class Solver:
                                           _p(vals, _f64p)))
         self._keep = (outer, inner)
         self._n = n
+
+    def factorize_device(self, values_ptr: int, stream: int = 0):
+        """Refactorize with the values in device memory (same pattern as before)."""
+        self._check(self._L.lss_factorize_device(self._h, C.c_void_p(values_ptr), C.c_void_p(stream)))
+
+    def solve_device(self, b_ptr: int, x_ptr: int, stream: int = 0):
+        """Solve with b and x (initial guess, overwritten) in device memory."""
+        self._check(self._L.lss_solve_device(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.c_void_p(stream)))
 
     def set_problematic_dofs(self, dofs):
         d = np.ascontiguousarray(sorted(set(int(v) for v in dofs)), np.int32)
