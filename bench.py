@@ -1,0 +1,429 @@
+#!/usr/bin/env python3
+"""Benchmark: time to 1e-8 relative residual, mixed precision vs plain FP64,
+on one GB300 (one process per GPU; N > 1 runs independent replicas).
+
+Workload (default ``elasticity_3m``): P1-tet linear elasticity on a
+100x100x100-node grid (3.0M DOFs, 3x3 blocks), Young's modulus lognormal(0, 1)
+per tet, penalty springs of stiffness 1e8 on a seeded 1% of the top-face nodes,
+z = 0 face clamped, RHS N(0, 1) -- the mixed-precision configuration.
+``--workload delaunay_1m`` runs the 2D Delaunay Laplacian (1,000,000 points,
+2% collapsed triangles) and ``elasticity_24k`` the 20^3-node inclusion cube.
+All inputs are synthetic (seeded numpy PCG64).
+
+One step = factorize (stiff-DOF selection, stiff-block inverses, MAS setup)
+with the matrix values resident in HBM and the pattern analysed beforehand,
+then the PCG solve to a true relative residual <= 1e-8 with b resident in HBM.
+``value`` is the mixed-precision ms per step (CUDA events on the solver's
+stream), ``e2e`` the same step through the C ABI with host arrays (the H2D
+copy of the values, b and x0 and the D2H copy of x inside the timed region).
+The plain-FP64 form of the same method is timed the same way and reported
+in ``config``.  Inputs exceed the 129 MB L2 (no flush needed).
+
+``--impl reference`` times the CPU restatement of the method (oracle/) on the
+host cores instead: a bounded sample (setup + a block of PCG iterations on the
+full system), scaled to time-to-solution with the iteration count estimated
+from the sampled residual decay.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "local-stiff-solver_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+def workload(name, seed):
+    from lss import gen
+    if name == "elasticity_3m":
+        A, b, info = gen.workload_elasticity_lognormal(seed=seed, nodes=100)
+        params = {"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0,
+                  "min_subdomain_size": 4, "max_iter": 20000}
+        desc = "elasticity_lognormal_100^3_nodes_springs1e8"
+    elif name == "delaunay_1m":
+        A, b, info = gen.workload_delaunay_laplacian(seed=seed, npts=1_000_000)
+        params = {"block_size": 1, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0,
+                  "min_subdomain_size": 4, "max_iter": 50000}
+        desc = "delaunay_laplacian_1M_points_2pct_collapsed"
+    elif name == "elasticity_24k":
+        A, b, info = gen.workload_elasticity_inclusion(seed=seed, nodes=20)
+        params = {"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0,
+                  "min_subdomain_size": 4, "max_iter": 20000}
+        desc = "elasticity_inclusion_20^3_nodes_E1e6"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return A.tocsc(), np.ascontiguousarray(b, np.float64), params, desc, info
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    """CPU restatement of the method on the host cores (bounded sample)."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from lss import build as B
+    from oracle import oracle as O
+    B.build_generator()
+    O.build()
+    A, b, params, desc, info = workload(args.workload, args.seed)
+    threads = os.cpu_count() or 1
+    setup_s, per_iter, res_hist = [], [], []
+    bnorm = float(np.linalg.norm(b))
+    block = args.ref_iters
+    total_steps = args.warmup + args.steps
+    t0 = time.perf_counter()
+    s = O.CpuSolver(A, params, threads=threads)
+    setup = time.perf_counter() - t0
+    # one step = a block of PCG iterations continued from the previous x
+    x = np.zeros_like(b)
+    r0 = bnorm
+    it_done = 0
+    for step in range(total_steps):
+        t1 = time.perf_counter()
+        x, inf = _oracle_block(O, s, b, x, block)
+        dt = time.perf_counter() - t1
+        it_done += inf["num_iterations"]
+        res_hist.append((it_done, inf["final_res_norm"]))
+        if step >= args.warmup:
+            per_iter.append(dt / max(inf["num_iterations"], 1))
+        if inf["final_res_norm"] / r0 <= 1e-8:
+            break
+    # iterations to 1e-8 from the observed true-residual decay (last half of the sample)
+    its = [h[0] for h in res_hist]
+    rs = [max(h[1], 1e-300) / r0 for h in res_hist]
+    if rs[-1] <= 1e-8:
+        n_est = its[-1]
+    else:
+        k0 = len(its) // 2
+        slope = (np.log(rs[-1]) - np.log(rs[k0])) / max(its[-1] - its[k0], 1) if len(its) > 1 else 0.0
+        n_est = its[-1] + (np.log(1e-8) - np.log(rs[-1])) / slope if slope < 0 else float("inf")
+    t_iter = statistics.mean(per_iter) if per_iter else float("nan")
+    value_ms = 1e3 * (setup + t_iter * n_est)
+    line = {"impl": "reference", "metric": "time_to_1e-8_rel_residual", "value": value_ms, "unit": "ms",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value_ms,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": desc, "n": int(A.shape[0]), "nnz": int(A.nnz),
+                                            "seed": args.seed},
+            "cpu_baseline": {"value": value_ms, "unit": "ms", "cores": threads, "kind": "port",
+                             "sample": f"CPU restatement (oracle/) on the full system: setup {setup:.2f} s, "
+                                       f"{its[-1]} PCG iterations in blocks of {block} "
+                                       f"({1e3 * t_iter:.2f} ms/iteration), iterations to 1e-8 "
+                                       f"{'measured' if rs[-1] <= 1e-8 else 'extrapolated from the residual decay'}"
+                                       f" = {n_est:.0f}"},
+            "e2e": {"value": value_ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _oracle_block(O, s, b, x0, block):
+    """Run `block` more PCG iterations of the CPU solver, restarted from x0."""
+    import ctypes as C
+    L = O.lib()
+    x = np.array(x0, np.float64, copy=True)
+    it = C.c_int32(0)
+    res = C.c_double(0)
+    L.lsso_solver_set_max_iter(s.h, block)
+    L.lsso_solver_solve(s.h, b.ctypes.data_as(C.POINTER(C.c_double)), x.ctypes.data_as(C.POINTER(C.c_double)),
+                        C.byref(it), C.byref(res))
+    return x, {"num_iterations": it.value, "final_res_norm": res.value}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="elasticity_3m",
+                    choices=["elasticity_3m", "delaunay_1m", "elasticity_24k"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--ref-iters", type=int, default=25, help="PCG iterations per reference-arm step")
+    ap.add_argument("--cpu-iters", type=int, default=10, help="PCG iterations of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one factorize + solve of the mixed solver only (for the ncu launch list)")
+    args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__ as g
+    g.build()
+    import lss
+
+    A, b, params, desc, info = workload(args.workload, args.seed + rank)
+    n = A.shape[0]
+    nnz = A.nnz
+    dev = torch.device("cuda", local)
+    gb300_common = {"device": local}
+
+    def make(precision):
+        p = {"solver": "GPUHybrid", "GPUHybrid": dict(params),
+             "gb300": dict(gb300_common, precision=precision)}
+        return lss.Solver.create(p)
+
+    t0 = time.perf_counter()
+    s_mixed = make("mixed")
+    s_mixed.analyze_pattern(A)
+    analyze_ms = 1e3 * (time.perf_counter() - t0)
+    s_mixed.factorize(A)
+    s_plain = make("fp64")
+    s_plain.factorize(A)
+
+    d_vals = torch.from_numpy(np.ascontiguousarray(A.data, np.float64)).to(dev)
+    d_b = torch.from_numpy(b).to(dev)
+    d_x = torch.zeros(n, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def step(s):
+        s.factorize_device(d_vals.data_ptr(), sh)
+        d_x.zero_()
+        s.solve_device(d_b.data_ptr(), d_x.data_ptr(), sh)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def timed(s, k, clocks=None):
+        for _ in range(args.warmup):
+            with torch.cuda.stream(stream):
+                step(s)
+        barrier()
+        l0 = s.get_info()["kernel_launches"]
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        ctx = clocks if clocks is not None else _Null()
+        with ctx:
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                for _ in range(k):
+                    step(s)
+                e1.record(stream)
+            barrier()
+        ms = e0.elapsed_time(e1) / k
+        launches = (s.get_info()["kernel_launches"] - l0) / k
+        return ms, launches
+
+    clocks = ClockSampler(local)
+    ms_mixed, launches = timed(s_mixed, args.steps, clocks)
+    info_m = s_mixed.get_info()
+    x_m = d_x.cpu().numpy()
+    ms_plain, _ = timed(s_plain, args.steps)
+    info_p = s_plain.get_info()
+    x_p = d_x.cpu().numpy()
+
+    # correctness of the timed solves (outer index = row, as the solver applies it)
+    import scipy.sparse as sp
+    Ar = sp.csr_matrix((A.data, A.indices, A.indptr), shape=A.shape)
+    bn = float(np.linalg.norm(b))
+    rel_m = float(np.linalg.norm(b - Ar @ x_m) / bn)
+    rel_p = float(np.linalg.norm(b - Ar @ x_p) / bn)
+
+    # end to end through the C ABI with host buffers (pattern analysed above)
+    e2e = []
+    for k in range(args.steps + 1):
+        barrier()
+        t1 = time.perf_counter()
+        s_mixed.factorize(A)
+        xh = s_mixed.solve(b)
+        barrier()
+        if k > 0:
+            e2e.append(1e3 * (time.perf_counter() - t1))
+    e2e_ms = statistics.mean(e2e)
+
+    # roofline of the dominant kernels (CUDA events inside the library, same stream)
+    kern = {}
+    for kind, name in ((0, "spmv_fp64"), (4, "mas_level0_symv"), (5, "residual_spmv_prec"), (1, "mas_apply")):
+        ms_k, by = s_mixed.time_op(kind, 30)
+        kern[name] = {"ms": ms_k, "bytes": by, "gbs": by / (ms_k * 1e-3) / 1e9 if ms_k > 0 else None}
+    pk, pk_src = peaks()
+    hbm = float(pk.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
+    # dominant: largest time per PCG iteration (SpMV once, MAS level-0 twice, residual SpMV once)
+    share = {"spmv_fp64": kern["spmv_fp64"]["ms"], "mas_level0_symv": 2 * kern["mas_level0_symv"]["ms"],
+             "residual_spmv_prec": kern["residual_spmv_prec"]["ms"]}
+    dom = max(share, key=share.get)
+    ach = kern[dom]["gbs"]
+    roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
+            "frac": ach / hbm if ach else None, "traffic": None, "peak_source": pk_src,
+            "per_kernel": kern}
+
+    # CPU baseline: the oracle's method on the host cores, same partition, bounded sample
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(A, b, params, s_mixed, info_m["num_iterations"], args.cpu_iters)
+
+    res = {"ms_mixed": ms_mixed, "ms_plain": ms_plain}
+    if ws > 1:
+        t = torch.tensor([ms_mixed, ms_plain, e2e_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_mixed, ms_plain, e2e_ms = [float(v) for v in t.cpu()]
+    if rank != 0:
+        return
+    h2d = nnz * 8 + 2 * n * 8
+    d2h = n * 8
+    line = {
+        "metric": "time_to_1e-8_rel_residual", "value": ms_mixed, "unit": "ms", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 outer PCG / f32 MAS",
+        "data": "synthetic (seeded, generated on the host)",
+        "config": {
+            "workload": desc, "n": n, "nnz": int(nnz), "block_size": params["block_size"],
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+            "l2": "inputs larger than L2 (matrix + MAS inverses > 129 MB), no flush",
+            "step": "factorize (values in HBM, pattern analysed once) + PCG solve to true rel. residual 1e-8",
+            "plain_fp64_ms": ms_plain, "mixed_speedup_vs_plain": ms_plain / ms_mixed,
+            "iterations_mixed": info_m["num_iterations"], "iterations_plain": info_p["num_iterations"],
+            "rel_residual_mixed": rel_m, "rel_residual_plain": rel_p,
+            "factorize_ms_mixed": 1e3 * info_m.get("time_factorize", 0.0),
+            "analyze_pattern_ms": analyze_ms,
+            "stiff_dofs": info_m["num_stiff_dofs"], "stiff_subdomains": info_m["num_subdomains"],
+            "mas_levels": info_m.get("mas_levels"), "mas_omega": info_m.get("mas_omega"),
+            "spmv_gbs": kern["spmv_fp64"]["gbs"],
+        },
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_profile(args):
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    import lss
+    A, b, params, desc, info = workload(args.workload, args.seed)
+    s = lss.Solver.create({"solver": "GPUHybrid", "GPUHybrid": dict(params), "gb300": {"precision": "mixed"}})
+    s.factorize(A)
+    x = s.solve(b)
+    torch.cuda.synchronize()
+    inf = s.get_info()
+    print(json.dumps({"profile": desc, "iterations": inf["num_iterations"], "status": inf["status"],
+                      "relative_residual": inf["relative_residual"]}), flush=True)
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def cpu_baseline(A, b, params, s_gpu, gpu_iters, iters):
+    """Oracle method on the host cores with the GPU's partition: setup + `iters`
+    PCG iterations, scaled to time-to-solution with the GPU's iteration count."""
+    from oracle import oracle as O
+    import ctypes as C
+    threads = os.cpu_count() or 1
+    perm, offs = s_gpu.partition()
+    t0 = time.perf_counter()
+    s = O.CpuSolver(A, params, perm=perm, part_offsets=offs, threads=threads)
+    setup = time.perf_counter() - t0
+    O.lib().lsso_solver_set_max_iter(s.h, iters)
+    x = np.zeros_like(b)
+    it = C.c_int32(0)
+    res = C.c_double(0)
+    t1 = time.perf_counter()
+    O.lib().lsso_solver_solve(s.h, b.ctypes.data_as(C.POINTER(C.c_double)),
+                              x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(it), C.byref(res))
+    dt = time.perf_counter() - t1
+    per_iter = dt / max(it.value, 1)
+    value = 1e3 * (setup + per_iter * gpu_iters)
+    return {"value": value, "unit": "ms", "cores": threads, "kind": "port",
+            "sample": f"CPU restatement (oracle/) with the GPU's partition on the full system: setup "
+                      f"{setup:.2f} s + {it.value} PCG iterations ({1e3 * per_iter:.1f} ms each), "
+                      f"scaled to the GPU solve's {gpu_iters} iterations"}
+
+
+if __name__ == "__main__":
+    main()

@@ -162,7 +162,8 @@ lss_status lss_op_precond(lss_solver *s, const double *r, double *z);
 
 /* Time `reps` launches of one kernel family on device-resident operands:
  * kind 0 = FP64 SpMV, 1 = MAS apply, 2 = full preconditioner, 3 = one PCG
- * iteration.  Writes the mean milliseconds per launch (CUDA events on the
+ * iteration, 4 = the level-0 bank SYMV kernel of MAS alone, 5 = the residual
+ * SpMV inside the preconditioner (FP32 operator in mixed precision).  Writes the mean milliseconds per launch (CUDA events on the
  * solver's stream) and the algorithmic bytes of one launch. */
 lss_status lss_op_time(lss_solver *s, int32_t kind, int32_t reps, double *ms_per_launch,
                        double *bytes_per_launch);

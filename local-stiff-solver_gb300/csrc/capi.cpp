@@ -17,6 +17,11 @@ size_t &alloc_cap_base()
     static size_t base = 0;
     return base;
 }
+unsigned long long &launch_count()
+{
+    static unsigned long long c = 0;
+    return c;
+}
 size_t &alloc_live_bytes()
 {
     static size_t live = 0;

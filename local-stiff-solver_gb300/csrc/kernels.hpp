@@ -144,6 +144,10 @@ void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void 
                       const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
                       int dot_mode, GridReduce gr, const int *done, cudaStream_t s);
 
+// level-0 bank SYMV alone (z = Inv_0 xin + coarse correction already in u), for timing
+void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp32, const double *xin, double *z,
+                       cudaStream_t s);
+
 // ---------------------------------------------------------------- stiff blocks
 struct StiffDev {
     int32_t nsub = 0, ndof = 0;

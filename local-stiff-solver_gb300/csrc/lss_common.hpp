@@ -37,8 +37,12 @@ inline void cuda_check(cudaError_t e, const char *what, const char *file, int li
     }
     throw Error(LSS_ERR_CUDA, msg);
 }
+// Kernel launch bookkeeping: launches issued by launcher functions plus the
+// kernel nodes of replayed CUDA graphs (reported by get_info).
+unsigned long long &launch_count();
 #define LSS_CUDA(call) ::lss::cuda_check((call), #call, __FILE__, __LINE__)
-#define LSS_LAUNCH_CHECK() ::lss::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+#define LSS_LAUNCH_CHECK() \
+    (::lss::launch_count()++, ::lss::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__))
 
 // Optional allocation cap for fault testing of the OOM path: at most
 // alloc_cap_bytes() more bytes than were live when the cap was set

@@ -431,6 +431,27 @@ void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, b
     }
 }
 
+void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp32, const double *xin, double *z,
+                       cudaStream_t s)
+{
+    const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
+    GridReduce gr{};
+#define LSS_L0(BD_, T_)                                                                                        \
+    symv0_kernel<BD_, T_, false, 0><<<grid, 256, 0, s>>>(m, (const T_ *)inv0, (const T_ *)u, xin, z, 1.0, nullptr, \
+                                                         nullptr, gr, nullptr)
+    if (fp32) {
+        if (m.bd == 1) LSS_L0(1, float);
+        else if (m.bd == 2) LSS_L0(2, float);
+        else LSS_L0(3, float);
+    } else {
+        if (m.bd == 1) LSS_L0(1, double);
+        else if (m.bd == 2) LSS_L0(2, double);
+        else LSS_L0(3, double);
+    }
+#undef LSS_L0
+    LSS_LAUNCH_CHECK();
+}
+
 void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
                       const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
                       int dot_mode, GridReduce gr, const int *done, cudaStream_t s)

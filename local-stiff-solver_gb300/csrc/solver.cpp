@@ -119,6 +119,7 @@ std::string HybridSolver::info_json() const
     o << ", \"precision\": \"" << (p_.mixed ? "mixed" : "fp64") << "\"";
     o << ", \"composition\": \"" << (p_.multiplicative ? "multiplicative" : "additive") << "\"";
     o << ", \"mas_omega\": " << omega_;
+    o << ", \"kernel_launches\": " << launch_count();
     int64_t nstiff = 0;
     for (const auto &s : subs_) nstiff += (int64_t)s.size();
     o << ", \"num_stiff_dofs\": " << nstiff << ", \"num_subdomains\": " << subs_.size();
@@ -570,11 +571,15 @@ void HybridSolver::launch_chunk(int iters)
         LSS_CUDA(cudaStreamEndCapture(stream_, &g));
         size_t nodes = 0;
         if (cudaGraphGetNodes(g, nullptr, &nodes) == cudaSuccess) stats_["kernels_per_iteration"] = (double)nodes / iters;
+        graph_nodes_ = nodes;
+        // the capture ran the launchers once without executing anything
+        launch_count() -= (unsigned long long)std::min<size_t>(launch_count(), nodes);
         LSS_CUDA(cudaGraphInstantiate(&graph_exec_, g, 0));
         cudaGraphDestroy(g);
         graph_iters_ = iters;
     }
     LSS_CUDA(cudaGraphLaunch(graph_exec_, stream_));
+    launch_count() += graph_nodes_;
 }
 
 void HybridSolver::run_pcg()
@@ -852,6 +857,9 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
         case 0: launch_spmv(A_, d_p_.data(), d_ap_.data(), nullptr, stream_); break;
         case 1: mas_apply(d_r_.data(), d_z_.data(), false, nullptr, 0, 1.0); break;
         case 2: precond(d_r_.data(), d_z_.data(), 0); break;
+        case 4: launch_mas_level0(mas_, d_inv0_.data(), d_u_.data(), mas_fp32_, d_r_.data(), d_z_.data(), stream_);
+            break;
+        case 5: launch_residual_spmv(A_, d_r_.data(), d_p_.data(), d_ap_.data(), p_.mixed, nullptr, stream_); break;
         default: iteration(); break;
         }
     };
@@ -872,9 +880,14 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
     const double esz = mas_fp32_ ? 4.0 : 8.0;
     const double mas_bytes = (double)(mas_.nparts + mas_.ncoarse) * mas_.tile_elems * esz + 2.0 * n * 8 +
                              (double)pat_.nb * (1 + 4);
+    const double vb = p_.mixed ? 4.0 : 8.0;  // operator value bytes of the residual SpMV
+    const double res_bytes = (double)nnzb * (bd * bd * vb + 4) + (pat_.nb + 1) * 4.0 + 3.0 * n * 8;
+    const double mas0_bytes = (double)mas_.nparts * mas_.tile_elems * esz + 2.0 * n * 8 + (double)pat_.nb * 5;
     switch (kind) {
     case 0: *bytes = spmv_bytes; break;
     case 1: *bytes = mas_bytes; break;
+    case 4: *bytes = mas0_bytes; break;
+    case 5: *bytes = res_bytes; break;
     default: *bytes = 0; break;
     }
 }

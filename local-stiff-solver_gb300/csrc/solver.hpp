@@ -122,6 +122,7 @@ private:
     GridReduce gr_;
     cudaGraphExec_t graph_exec_ = nullptr;
     int graph_iters_ = 0;
+    size_t graph_nodes_ = 0;
     PinnedBuf pin_;
 
     // last solve

@@ -66,8 +66,15 @@ def build(force: bool = False, verbose: bool = False) -> dict:
     lib = _paths.lib_path()
     if force or jobs or _stale(lib, objs):
         _run([nvcc, *ARCH, "-shared", "-o", lib, *objs, "-lpthread"], verbose)
+    glib = build_generator(force, verbose)
+    return {"lib": lib, "gen": glib}
+
+
+def build_generator(force: bool = False, verbose: bool = False) -> str:
+    """Host-only assembler of the synthetic elasticity systems (no CUDA)."""
+    os.makedirs(_paths.BUILD_DIR, exist_ok=True)
     gsrc = os.path.join(_paths.CSRC, "gen_elasticity.cpp")
     glib = _paths.gen_lib_path()
     if force or _stale(glib, [gsrc]):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", gsrc, "-o", glib], verbose)
-    return {"lib": lib, "gen": glib}
+    return glib

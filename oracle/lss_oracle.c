@@ -978,6 +978,7 @@ lsso_solver *lsso_solver_create(int32_t n, const int32_t *outer, const int32_t *
 
 int32_t lsso_solver_num_stiff(const lsso_solver *s) { return s->nstiff; }
 double lsso_solver_omega(const lsso_solver *s) { return s->omega; }
+void lsso_solver_set_max_iter(lsso_solver *s, int32_t max_iter) { s->p.max_iter = max_iter; }
 double lsso_solver_lambda_max(const lsso_solver *s) { return s->lambda_max; }
 int32_t lsso_solver_num_subdomains(const lsso_solver *s) { return s->nsub; }
 

@@ -124,6 +124,7 @@ int32_t lsso_solver_solve(lsso_solver *s, const double *b, double *x, int32_t *i
                           double *final_res_norm);
 int32_t lsso_solver_num_stiff(const lsso_solver *s);
 double lsso_solver_omega(const lsso_solver *s);
+void lsso_solver_set_max_iter(lsso_solver *s, int32_t max_iter);
 double lsso_solver_lambda_max(const lsso_solver *s);
 
 /* Largest eigenvalue of the symmetric tridiagonal with diagonal d[0..k) and

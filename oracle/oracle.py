@@ -109,6 +109,7 @@ def lib():
         L.lsso_solver_num_subdomains.argtypes = [C.c_void_p]
         L.lsso_solver_num_subdomains.restype = C.c_int32
         L.lsso_solver_precond.argtypes = [C.c_void_p, _f64p, _f64p]
+        L.lsso_solver_set_max_iter.argtypes = [C.c_void_p, C.c_int32]
         L.lsso_solver_omega.argtypes = [C.c_void_p]
         L.lsso_solver_omega.restype = C.c_double
         L.lsso_solver_lambda_max.argtypes = [C.c_void_p]
