@@ -53,15 +53,19 @@ def peaks():
 
 def workload(name, seed):
     from lss import gen
-    if name == "elasticity_3m":
-        A, b, info = gen.workload_elasticity_lognormal(seed=seed, nodes=100)
-        params = {"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0,
-                  "min_subdomain_size": 4, "max_iter": 20000}
-        desc = "elasticity_lognormal_100^3_nodes_springs1e8"
+    # GPUHybrid parameters: linear-solver-spec.json defaults, except that the
+    # isolated spring nodes of the elasticity workloads need decompose_subdomains
+    # = false (a lone stiff node is a 3-DOF, well-conditioned component that the
+    # size and Gershgorin filters would drop) and the small cube uses the
+    # reference's example configuration (spec/CPUHybrid.json).
+    if name in ("elasticity_3m", "elasticity_650k"):
+        nodes = 100 if name == "elasticity_3m" else 60
+        A, b, info = gen.workload_elasticity_lognormal(seed=seed, nodes=nodes)
+        params = {"block_size": 3, "relative_tolerance": 1e-8, "decompose_subdomains": False, "max_iter": 20000}
+        desc = f"elasticity_lognormal_{nodes}^3_nodes_springs1e8"
     elif name == "delaunay_1m":
         A, b, info = gen.workload_delaunay_laplacian(seed=seed, npts=1_000_000)
-        params = {"block_size": 1, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0,
-                  "min_subdomain_size": 4, "max_iter": 50000}
+        params = {"block_size": 1, "relative_tolerance": 1e-8, "max_iter": 50000}
         desc = "delaunay_laplacian_1M_points_2pct_collapsed"
     elif name == "elasticity_24k":
         A, b, info = gen.workload_elasticity_inclusion(seed=seed, nodes=20)
@@ -212,7 +216,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="elasticity_3m",
-                    choices=["elasticity_3m", "delaunay_1m", "elasticity_24k"])
+                    choices=["elasticity_3m", "delaunay_1m", "elasticity_24k", "elasticity_650k"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--ref-iters", type=int, default=25, help="PCG iterations per reference-arm step")
     ap.add_argument("--cpu-iters", type=int, default=10, help="PCG iterations of the CPU-baseline sample")

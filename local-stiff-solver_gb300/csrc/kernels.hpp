@@ -54,7 +54,8 @@ void launch_gershgorin(int nb, int bd, const int32_t *rows, const int32_t *cols,
 // ---------------------------------------------------------------- operator
 struct BsrDev {
     int32_t nb = 0, bd = 1;
-    int lanes = 8;                 // threads per block row in SpMV
+    int lanes = 4;                 // threads per block row of the FP64 SpMV (autotuned)
+    int lanes32 = 4;               // threads per block row of the FP32 residual SpMV (autotuned)
     const int32_t *rows = nullptr;
     const int32_t *cols = nullptr;
     const double *vals = nullptr;  // row-sliced layout (spmv.cuh)

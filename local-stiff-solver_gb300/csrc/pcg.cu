@@ -232,6 +232,7 @@ void spmv_dispatch(const BsrDev &A, const double *x, double *y, const int *done,
 {
     const int grid = grid_for((int64_t)A.nb * A.lanes, 256, 152 * 16);
     switch (A.lanes) {
+    case 1: spmv_kernel<BD, 1><<<grid, 256, 0, s>>>(A, x, y, done); break;
     case 2: spmv_kernel<BD, 2><<<grid, 256, 0, s>>>(A, x, y, done); break;
     case 4: spmv_kernel<BD, 4><<<grid, 256, 0, s>>>(A, x, y, done); break;
     case 8: spmv_kernel<BD, 8><<<grid, 256, 0, s>>>(A, x, y, done); break;
@@ -244,8 +245,10 @@ template <int BD, typename VT, typename ACC>
 void residual_dispatch(const BsrDev &A, const VT *vals, const double *r, const double *x, double *y,
                        const int *done, cudaStream_t s)
 {
-    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, 152 * 16);
-    switch (A.lanes) {
+    const int lanes = sizeof(VT) == 4 ? A.lanes32 : A.lanes;
+    const int grid = grid_for((int64_t)A.nb * lanes, 256, 152 * 16);
+    switch (lanes) {
+    case 1: residual_kernel<BD, 1, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
     case 2: residual_kernel<BD, 2, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
     case 4: residual_kernel<BD, 4, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
     case 8: residual_kernel<BD, 8, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
@@ -259,6 +262,7 @@ void spmv_alpha_dispatch(const BsrDev &A, const double *p, double *Ap, PcgState 
 {
     const int grid = grid_for((int64_t)A.nb * A.lanes, 256, GRID_MAX);
     switch (A.lanes) {
+    case 1: spmv_alpha_kernel<BD, 1><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
     case 2: spmv_alpha_kernel<BD, 2><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
     case 4: spmv_alpha_kernel<BD, 4><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
     case 8: spmv_alpha_kernel<BD, 8><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;

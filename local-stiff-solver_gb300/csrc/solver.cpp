@@ -127,7 +127,7 @@ std::string HybridSolver::info_json() const
     if (have_pattern_) {
         o << ", \"num_parts\": " << (pat_.part.part_offsets.size() - 1) << ", \"mas_levels\": " << cs_.L;
         o << ", \"block_size\": " << pat_.bd << ", \"nnz_blocks\": " << pat_.rows.back();
-        o << ", \"spmv_lanes\": " << A_.lanes;
+        o << ", \"spmv_lanes\": " << A_.lanes << ", \"spmv_lanes_fp32\": " << A_.lanes32;
     }
     for (const auto &kv : stats_) o << ", \"" << kv.first << "\": " << kv.second;
     for (const auto &kv : sstats_) o << ", \"" << kv.first << "\": \"" << kv.second << "\"";
@@ -175,14 +175,9 @@ void HybridSolver::analyze(int32_t n, int64_t nnz, const int32_t *outer, const i
     A_.rows = d_rows_.data();
     A_.cols = d_cols_.data();
     A_.vals = d_vals_.data();
-    if (p_.spmv_lanes > 0) A_.lanes = p_.spmv_lanes;
-    else {
-        // lanes per block row: smallest power of two >= mean blocks per row, in [2, 32]
-        const double m = pat_.mean_blocks_per_row;
-        int l = 2;
-        while (l < 32 && l < m) l <<= 1;
-        A_.lanes = l;
-    }
+    // lanes per block row: autotuned at the first factorize of this pattern
+    A_.lanes = A_.lanes32 = p_.spmv_lanes > 0 ? p_.spmv_lanes : 4;
+    lanes_tuned_ = p_.spmv_lanes > 0;
     // MAS device maps
     const int32_t nparts = (int32_t)pat_.part.part_offsets.size() - 1;
     d_part_off_.upload(pat_.part.part_offsets, stream_);
@@ -305,6 +300,7 @@ void HybridSolver::factorize_common()
     ensure_vectors();
     d_csc_.release();
     factorized_ = true;
+    if (!lanes_tuned_) autotune_spmv();
     auto t5 = clk::now();
     estimate_omega();
     stats_["time_omega_estimate"] = secs(t5);
@@ -652,6 +648,55 @@ void HybridSolver::run_pcg()
     num_iterations_ = h_state_->iter;
     stop_reason_ = h_state_->done ? h_state_->done : STOP_MAX_ITER;
     final_res_norm_ = std::sqrt(res2);
+}
+
+// Autotuner of the SpMV launch shape: threads per block row in {1, 2, 4, 8, 16}
+// for the FP64 operator and the FP32 copy, timed with CUDA events on the real
+// matrix once per pattern.  Fewer lanes mean more blocks per lane (more
+// independent loads in flight) and a shallower cross-lane FP64 reduction --
+// which matters on a GPU whose FP64 rate is 1/57 of its FP32 rate.
+void HybridSolver::autotune_spmv()
+{
+    const int64_t n = n_vec();
+    std::vector<double> h(n);
+    for (int64_t i = 0; i < n; ++i) h[i] = 1.0 + 1e-3 * (double)(i % 89);
+    LSS_CUDA(cudaMemcpyAsync(d_p_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    LSS_CUDA(cudaMemcpyAsync(d_r_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    cudaEvent_t e0, e1;
+    LSS_CUDA(cudaEventCreate(&e0));
+    LSS_CUDA(cudaEventCreate(&e1));
+    auto time_it = [&](auto &&launch) {
+        launch();
+        LSS_CUDA(cudaEventRecord(e0, stream_));
+        for (int k = 0; k < 5; ++k) launch();
+        LSS_CUDA(cudaEventRecord(e1, stream_));
+        LSS_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        LSS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        return ms;
+    };
+    std::string log;
+    for (int pass = 0; pass < (A_.vals32 ? 2 : 1); ++pass) {
+        float best = 1e30f;
+        int best_l = 4;
+        for (int l : {1, 2, 4, 8, 16}) {
+            BsrDev T = A_;
+            T.lanes = T.lanes32 = l;
+            const float ms = pass == 0 ? time_it([&]() { launch_spmv(T, d_p_.data(), d_ap_.data(), nullptr, stream_); })
+                                       : time_it([&]() {
+                                             launch_residual_spmv(T, d_r_.data(), d_p_.data(), d_ap_.data(), true,
+                                                                  nullptr, stream_);
+                                         });
+            log += (pass ? " f32:" : " f64:") + std::to_string(l) + "=" + std::to_string(ms / 5);
+            if (ms < best) { best = ms; best_l = l; }
+        }
+        if (pass == 0) A_.lanes = best_l;
+        else A_.lanes32 = best_l;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    lanes_tuned_ = true;
+    sstats_["spmv_autotune_ms"] = log;
 }
 
 // lambda_max(M A) for M = MAS alone from the Lanczos tridiagonal of a short

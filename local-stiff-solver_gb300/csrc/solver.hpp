@@ -73,6 +73,7 @@ private:
     void precond(const double *r, double *z, int dot_mode);
     void mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale);
     void estimate_omega();
+    void autotune_spmv();
     void iteration();
     void launch_chunk(int iters);
     void invalidate_graph();
@@ -132,6 +133,7 @@ private:
     int refinements_ = 0;
     double omega_ = 1.0, lambda_max_ = 0.0;
     bool lanczos_mode_ = false;
+    bool lanes_tuned_ = false;
 };
 
 }  // namespace lss
