@@ -124,6 +124,16 @@ lss_status lss_grad_A_pattern(lss_solver *s, const double *lambda, const double 
 lss_status lss_grad_A_pattern_device(lss_solver *s, const double *d_lambda, const double *d_x,
                                      double *d_dA_values, void *stream);
 
+/* Fused adjoint scatter to element parameters (no counterpart in the
+ * reference): for a linear parameterisation A.values = M theta + c, with M^T
+ * given in CSR (n_params rows; column indices are stored-entry indices of A in
+ * the input storage order; values are d(A.values[v]) / d(theta[e])), writes
+ * dtheta[e] = sum_v M[v][e] * (-lambda[row(v)] * x[col(v)]) -- the chain rule
+ * of dL/dA_ij = -lambda_i x_j without forming dL/dA.  Device pointers. */
+lss_status lss_grad_params_device(lss_solver *s, const double *d_lambda, const double *d_x, int32_t n_params,
+                                  const int64_t *d_mt_rowptr, const int32_t *d_mt_cols,
+                                  const double *d_mt_vals, double *d_dtheta, void *stream);
+
 /* The selected stiff DOF set after post-processing (the union of the stiff
  * subdomains, ascending; GPUHybrid.cu:240-262 d_all_bad_dofs).  With
  * out == NULL only *count is written. */

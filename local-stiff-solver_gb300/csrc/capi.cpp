@@ -203,6 +203,17 @@ lss_status lss_grad_A_pattern_device(lss_solver *s, const double *d_lambda, cons
     return guarded(s, [&]() { s->impl->grad_pattern_device(d_lambda, d_x, d_dA_values, (cudaStream_t)stream); });
 }
 
+lss_status lss_grad_params_device(lss_solver *s, const double *d_lambda, const double *d_x, int32_t n_params,
+                                  const int64_t *d_mt_rowptr, const int32_t *d_mt_cols, const double *d_mt_vals,
+                                  double *d_dtheta, void *stream)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() {
+        s->impl->grad_params_device(d_lambda, d_x, n_params, d_mt_rowptr, d_mt_cols, d_mt_vals, d_dtheta,
+                                    (cudaStream_t)stream);
+    });
+}
+
 lss_status lss_selected_dofs(const lss_solver *s, int32_t *out, int32_t cap, int32_t *count)
 {
     if (!valid(s) || !count) return LSS_ERR_INVALID_ARGUMENT;

@@ -105,6 +105,11 @@ void launch_permute(int64_t nb, int bd, const int32_t *perm, const double *src, 
                     cudaStream_t s);
 void launch_grad_pattern(int32_t n, const int32_t *outer, const int32_t *inner, const double *lambda,
                          const double *x, double *dA, cudaStream_t s);
+// dtheta[e] = sum_k Mt_vals[k] * (-lambda[row(v)] * x[inner[v]]), v = Mt_cols[k], over the CSR row e of Mt
+void launch_grad_params(int32_t nparams, const int64_t *mt_rowptr, const int32_t *mt_cols, const double *mt_vals,
+                        const int32_t *row_of, const int32_t *inner, const double *lambda, const double *x,
+                        double *dtheta, cudaStream_t s);
+void launch_row_of(int32_t n, const int32_t *outer, int32_t *row_of, cudaStream_t s);
 
 // ---------------------------------------------------------------- MAS
 constexpr int MAS_MAXL = 7;

@@ -227,6 +227,40 @@ __global__ void check_finite_kernel(int64_t n, const double *__restrict__ v, int
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
 
+// Fused adjoint scatter: the pattern gradient -lambda_i x_j is formed on the
+// fly for the stored entries an element touches and reduced into its
+// parameter (one warp per parameter row of the element -> entry map).
+__global__ void __launch_bounds__(256) grad_params_kernel(int32_t nparams, const int64_t *__restrict__ rp,
+                                                          const int32_t *__restrict__ cols,
+                                                          const double *__restrict__ vals,
+                                                          const int32_t *__restrict__ row_of,
+                                                          const int32_t *__restrict__ inner,
+                                                          const double *__restrict__ lambda,
+                                                          const double *__restrict__ x, double *__restrict__ dtheta)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t e = w0; e < nparams; e += nw) {
+        double acc = 0.0;
+        for (int64_t k = rp[e] + lane; k < rp[e + 1]; k += 32) {
+            const int32_t v = cols[k];
+            acc -= vals[k] * lambda[row_of[v]] * x[inner[v]];
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) dtheta[e] = acc;
+    }
+}
+
+__global__ void row_of_kernel(int32_t n, const int32_t *__restrict__ outer, int32_t *__restrict__ row_of)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = w0; i < n; i += nw)
+        for (int32_t k = outer[i] + lane; k < outer[i + 1]; k += 32) row_of[k] = (int32_t)i;
+}
+
 template <int BD>
 void spmv_dispatch(const BsrDev &A, const double *x, double *y, const int *done, cudaStream_t s)
 {
@@ -355,6 +389,22 @@ void launch_check_finite(int64_t n, const double *v, int *flag, cudaStream_t s)
 {
     if (n == 0) return;
     check_finite_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, v, flag);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_grad_params(int32_t nparams, const int64_t *mt_rowptr, const int32_t *mt_cols, const double *mt_vals,
+                        const int32_t *row_of, const int32_t *inner, const double *lambda, const double *x,
+                        double *dtheta, cudaStream_t s)
+{
+    if (nparams <= 0) return;
+    grad_params_kernel<<<grid_for((int64_t)nparams * 32, 256, 152 * 16), 256, 0, s>>>(
+        nparams, mt_rowptr, mt_cols, mt_vals, row_of, inner, lambda, x, dtheta);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_row_of(int32_t n, const int32_t *outer, int32_t *row_of, cudaStream_t s)
+{
+    row_of_kernel<<<grid_for((int64_t)n * 32, 256, 152 * 16), 256, 0, s>>>(n, outer, row_of);
     LSS_LAUNCH_CHECK();
 }
 

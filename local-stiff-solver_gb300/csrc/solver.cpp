@@ -158,6 +158,7 @@ void HybridSolver::analyze(int32_t n, int64_t nnz, const int32_t *outer, const i
     h_inner_.assign(inner, inner + nnz);
     d_outer_.release();
     d_inner_.release();
+    d_row_of_.release();
     stats_["time_partition_and_layout"] = secs(t0);
     auto t1 = clk::now();
     cs_ = build_coarse_space(pat_, p_.max_coarse_levels);
@@ -822,6 +823,25 @@ void HybridSolver::grad_pattern_device(const double *d_lambda, const double *d_x
     if (d_outer_.size() != h_outer_.size()) d_outer_.upload(h_outer_, stream_);
     if (d_inner_.size() != h_inner_.size()) d_inner_.upload(h_inner_, stream_);
     launch_grad_pattern(pat_.n, d_outer_.data(), d_inner_.data(), d_lambda, d_x, d_dA, stream_);
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void HybridSolver::grad_params_device(const double *d_lambda, const double *d_x, int32_t nparams,
+                                      const int64_t *d_rowptr, const int32_t *d_cols, const double *d_vals,
+                                      double *d_dtheta, cudaStream_t user)
+{
+    if (!have_pattern_) fail(LSS_ERR_NOT_FACTORIZED, "no matrix pattern");
+    if (nparams < 0 || (nparams > 0 && (!d_rowptr || !d_cols || !d_vals || !d_dtheta)))
+        fail(LSS_ERR_INVALID_ARGUMENT, "invalid parameter map");
+    StreamScope scope(this, user);
+    if (d_outer_.size() != h_outer_.size()) d_outer_.upload(h_outer_, stream_);
+    if (d_inner_.size() != h_inner_.size()) d_inner_.upload(h_inner_, stream_);
+    if (d_row_of_.size() != (size_t)pat_.nnz) {
+        d_row_of_.resize(pat_.nnz);
+        launch_row_of(pat_.n, d_outer_.data(), d_row_of_.data(), stream_);
+    }
+    launch_grad_params(nparams, d_rowptr, d_cols, d_vals, d_row_of_.data(), d_inner_.data(), d_lambda, d_x, d_dtheta,
+                       stream_);
     LSS_CUDA(cudaStreamSynchronize(stream_));
 }
 

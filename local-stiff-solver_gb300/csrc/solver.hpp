@@ -33,6 +33,8 @@ public:
     void solve_device(const double *d_b, double *d_x, cudaStream_t user_stream);
     void grad_pattern_host(const double *lambda, const double *x, double *dA);
     void grad_pattern_device(const double *d_lambda, const double *d_x, double *d_dA, cudaStream_t user_stream);
+    void grad_params_device(const double *d_lambda, const double *d_x, int32_t nparams, const int64_t *d_rowptr,
+                            const int32_t *d_cols, const double *d_vals, double *d_dtheta, cudaStream_t user_stream);
 
     // operator-level access (original ordering, host pointers)
     void op_spmv(const double *x, double *y);
@@ -95,7 +97,7 @@ private:
 
     // operator
     BsrDev A_;
-    DBuf<int32_t> d_rows_, d_cols_, d_perm_, d_outer_, d_inner_;
+    DBuf<int32_t> d_rows_, d_cols_, d_perm_, d_outer_, d_inner_, d_row_of_;
     DBuf<double> d_vals_, d_csc_;
     DBuf<float> d_vals32_;
     DBuf<int64_t> d_src_;

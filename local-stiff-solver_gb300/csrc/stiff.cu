@@ -5,7 +5,7 @@
 // (GPUHybrid.cu:993-1411), and applies next_z = z + S^T A_SS^-1 S (r - A z)
 // (dss_precond_iter, GPUHybrid.cu:544-675).  Here every subdomain is gathered
 // into a dense FP64 block, inverted in FP64 by the symmetric sweep (one CTA in
-// shared memory up to 128 DOFs, a per-pivot grid-wide update beyond), and
+// shared memory up to 128 DOFs, a blocked multi-CTA sweep beyond), and
 // applied as a warp-per-row GEMV fused with the scatter.  The residual rows
 // r - A z are only computed on the stiff rows (the reference forms the full
 // product and gathers it).
@@ -102,7 +102,14 @@ __global__ void __launch_bounds__(256) invert_small_kernel(const int32_t *__rest
     }
 }
 
-// large subdomains: grid-wide sweep, two launches per pivot
+// Large subdomains: blocked symmetric sweep.  Sweeping the pivots of a block
+// K at once is the same operator as sweeping them one by one:
+//   P = S[:,K] D^-1 (D = S[K,K]);  S[I,J] -= P[I] S[K,J]  (I, J outside K);
+//   S[I,K] = P[I];  S[K,J] = P[J]^T;  S[K,K] = -D^-1.
+// After every block has been swept S holds -A^-1.  Four launches per block of
+// SW_T pivots; the trailing update is a tiled FP64 rank-SW_T product.
+constexpr int SW_T = 32;
+
 __global__ void symmetrize_kernel(double *__restrict__ S, int m)
 {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -111,43 +118,90 @@ __global__ void symmetrize_kernel(double *__restrict__ S, int m)
     if (r > c) S[idx] = S[(int64_t)c * m + r];
 }
 
-__global__ void sweep_update_kernel(double *__restrict__ S, int m, int p, int *bad)
+// D^-1 of the pivot block by the scalar sweep in shared memory (one CTA)
+__global__ void __launch_bounds__(256) blk_diag_kernel(const double *__restrict__ S, int m, int k0, int t,
+                                                       double *__restrict__ Dinv, int *bad)
+{
+    __shared__ double D[SW_T * (SW_T + 1)], col[SW_T], scol[SW_T];
+    const int ld = SW_T + 1;
+    for (int e = threadIdx.x; e < t * t; e += blockDim.x) {
+        const int r = e / t, c = e % t;
+        D[r * ld + c] = S[(int64_t)(k0 + r) * m + k0 + c];
+    }
+    __syncthreads();
+    sweep_invert_small(D, ld, t, col, scol, bad);
+    for (int e = threadIdx.x; e < t * t; e += blockDim.x) {
+        const int r = e / t, c = e % t;
+        Dinv[r * SW_T + c] = -D[r * ld + c];  // the sweep leaves -D^-1
+    }
+}
+
+// P[i][c] = sum_s S[i][k0+s] Dinv[s][c] for every row i (rows inside K unused)
+__global__ void __launch_bounds__(256) blk_panel_kernel(const double *__restrict__ S, int m, int k0, int t,
+                                                        const double *__restrict__ Dinv, double *__restrict__ P)
 {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)m * m) return;
-    const int t = (int)(idx / m), c = (int)(idx % m);
-    const double piv = S[(int64_t)p * m + p];
-    if (idx == 0 && (!isfinite(piv) || piv == 0.0)) atomicOr(bad, 4);
-    if (t == p || c == p) return;
-    S[idx] -= (S[(int64_t)t * m + p] / piv) * S[(int64_t)p * m + c];
+    if (idx >= (int64_t)m * SW_T) return;
+    const int i = (int)(idx / SW_T), c = (int)(idx % SW_T);
+    if (c >= t) return;
+    const double *row = S + (int64_t)i * m + k0;
+    double acc = 0.0;
+    for (int q = 0; q < t; ++q) acc += row[q] * Dinv[q * SW_T + c];
+    P[(int64_t)i * SW_T + c] = acc;
 }
 
-__global__ void sweep_pivot_kernel(double *__restrict__ S, int m, int p)
+// S[i][j] -= sum_s P[i][s] S[k0+s][j] for i, j outside K; 32x32 output tiles
+__global__ void __launch_bounds__(256) blk_update_kernel(double *__restrict__ S, int m, int k0, int t,
+                                                         const double *__restrict__ P)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= m) return;
-    const double piv = S[(int64_t)p * m + p];
-    if (t == p) return;
-    const double v = S[(int64_t)t * m + p] / piv;
-    S[(int64_t)t * m + p] = v;
-    S[(int64_t)p * m + t] = v;
+    __shared__ double Pt[32][SW_T + 1], Kt[SW_T][33];
+    const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+    for (int e = threadIdx.x; e < 32 * SW_T; e += blockDim.x) {
+        const int r = e / SW_T, q = e % SW_T;
+        const int i = i0 + r;
+        Pt[r][q] = (i < m && q < t) ? P[(int64_t)i * SW_T + q] : 0.0;
+        const int qq = e / 32, cc = e % 32;
+        const int j = j0 + cc;
+        Kt[qq][cc] = (j < m && qq < t) ? S[(int64_t)(k0 + qq) * m + j] : 0.0;
+    }
+    __syncthreads();
+    const int cc = threadIdx.x & 31;
+    const int j = j0 + cc;
+    for (int r = threadIdx.x >> 5; r < 32; r += blockDim.x >> 5) {
+        const int i = i0 + r;
+        if (i >= m || j >= m) continue;
+        if ((i >= k0 && i < k0 + t) || (j >= k0 && j < k0 + t)) continue;
+        double acc = 0.0;
+#pragma unroll 8
+        for (int q = 0; q < SW_T; ++q) acc += Pt[r][q] * Kt[q][cc];
+        S[(int64_t)i * m + j] -= acc;
+    }
 }
 
-__global__ void sweep_finish_kernel(double *__restrict__ S, int m, int p_last_done, int *bad)
+// write the swept pivot rows/columns: S[i][K] = P[i], S[K][i] = P[i]^T, S[K][K] = -Dinv
+__global__ void __launch_bounds__(256) blk_write_kernel(double *__restrict__ S, int m, int k0, int t,
+                                                        const double *__restrict__ P,
+                                                        const double *__restrict__ Dinv)
 {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)m * m) return;
-    (void)p_last_done;
-    const double v = -S[idx];
-    if (!isfinite(v)) atomicOr(bad, 8);
-    S[idx] = v;
+    if (idx >= (int64_t)m * SW_T) return;
+    const int i = (int)(idx / SW_T), c = (int)(idx % SW_T);
+    if (c >= t) return;
+    if (i >= k0 && i < k0 + t) {
+        S[(int64_t)i * m + k0 + c] = -Dinv[(i - k0) * SW_T + c];
+    } else {
+        const double v = P[(int64_t)i * SW_T + c];
+        S[(int64_t)i * m + k0 + c] = v;
+        S[(int64_t)(k0 + c) * m + i] = v;
+    }
 }
 
-__global__ void set_pivot_kernel(double *__restrict__ S, int m, int p)
+__global__ void negate_check_kernel(double *__restrict__ S, int64_t count, int *bad)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        const double piv = S[(int64_t)p * m + p];
-        S[(int64_t)p * m + p] = -1.0 / piv;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = -S[i];
+        if (!isfinite(v)) atomicOr(bad, 8);
+        S[i] = v;
     }
 }
 
@@ -228,20 +282,29 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
         hoff[q] = acc;
         acc += (int64_t)(h_off[q + 1] - h_off[q]) * (h_off[q + 1] - h_off[q]);
     }
-    for (int32_t q = 0; q < nsub; ++q) {
-        const int m = h_off[q + 1] - h_off[q];
-        if (m <= SMALL) continue;
-        double *Sq = inv + hoff[q];
-        const int64_t mm = (int64_t)m * m;
-        const unsigned g = (unsigned)((mm + 255) / 256);
-        symmetrize_kernel<<<g, 256, 0, s>>>(Sq, m);
-        for (int p = 0; p < m; ++p) {
-            sweep_update_kernel<<<g, 256, 0, s>>>(Sq, m, p, bad);
-            sweep_pivot_kernel<<<(m + 255) / 256, 256, 0, s>>>(Sq, m, p);
-            set_pivot_kernel<<<1, 32, 0, s>>>(Sq, m, p);
+    int maxm = 0;
+    for (int32_t q = 0; q < nsub; ++q) maxm = std::max(maxm, h_off[q + 1] - h_off[q]);
+    if (maxm > SMALL) {
+        DBuf<double> Dinv((size_t)SW_T * SW_T), P((size_t)maxm * SW_T);
+        for (int32_t q = 0; q < nsub; ++q) {
+            const int m = h_off[q + 1] - h_off[q];
+            if (m <= SMALL) continue;
+            double *Sq = inv + hoff[q];
+            const int64_t mm = (int64_t)m * m;
+            symmetrize_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, s>>>(Sq, m);
+            const unsigned gp = (unsigned)(((int64_t)m * SW_T + 255) / 256);
+            const dim3 gu((m + 31) / 32, (m + 31) / 32);
+            for (int k0 = 0; k0 < m; k0 += SW_T) {
+                const int t = std::min(SW_T, m - k0);
+                blk_diag_kernel<<<1, 256, 0, s>>>(Sq, m, k0, t, Dinv.data(), bad);
+                blk_panel_kernel<<<gp, 256, 0, s>>>(Sq, m, k0, t, Dinv.data(), P.data());
+                blk_update_kernel<<<gu, 256, 0, s>>>(Sq, m, k0, t, P.data());
+                blk_write_kernel<<<gp, 256, 0, s>>>(Sq, m, k0, t, P.data(), Dinv.data());
+            }
+            negate_check_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, s>>>(Sq, mm, bad);
+            LSS_LAUNCH_CHECK();
         }
-        sweep_finish_kernel<<<g, 256, 0, s>>>(Sq, m, m, bad);
-        LSS_LAUNCH_CHECK();
+        LSS_CUDA(cudaStreamSynchronize(s));  // Dinv and P are freed at scope exit
     }
 }
 

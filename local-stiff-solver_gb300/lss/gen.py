@@ -216,3 +216,93 @@ def workload_batched(seed=0, count=64, dof_lo=5_000, dof_hi=200_000, nrhs=16, ra
         B = rng.standard_normal((A.shape[0], nrhs))
         systems.append((A, B, {"nodes": m, "E_ratio": ratio}))
     return systems
+
+
+# ---------------------------------------------------------------------------
+# parametric elasticity: A(theta) = M theta + c (differentiation workload)
+# ---------------------------------------------------------------------------
+
+_KUHN = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+
+
+def _tet_offsets(p):
+    v = [np.zeros(3, int)]
+    for a in range(3):
+        w = v[-1].copy()
+        w[_KUHN[p][a]] += 1
+        v.append(w)
+    return np.array(v)  # 4 x 3 vertex offsets (in cells)
+
+
+def _tet_stiffness_ref(p, h, nu):
+    """12x12 P1-tet stiffness of Kuhn tet p for E = 1 (same formulas as the
+    native assembler)."""
+    X = _tet_offsets(p) * h
+    J = (X[1:] - X[0]).T
+    inv = np.linalg.inv(J)
+    g = np.zeros((4, 3))
+    g[1:] = inv
+    g[0] = -g[1:].sum(axis=0)
+    vol = abs(np.linalg.det(J)) / 6.0
+    lam = nu / ((1 + nu) * (1 - 2 * nu))
+    mu = 1.0 / (2 * (1 + nu))
+    B = np.zeros((6, 12))
+    for a in range(4):
+        gx, gy, gz = g[a]
+        B[0, 3 * a] = gx
+        B[1, 3 * a + 1] = gy
+        B[2, 3 * a + 2] = gz
+        B[3, 3 * a + 1], B[3, 3 * a + 2] = gz, gy
+        B[4, 3 * a], B[4, 3 * a + 2] = gz, gx
+        B[5, 3 * a], B[5, 3 * a + 1] = gy, gx
+    D = np.zeros((6, 6))
+    D[:3, :3] = lam
+    D[np.arange(3), np.arange(3)] += 2 * mu
+    D[np.arange(3, 6), np.arange(3, 6)] = mu
+    return vol * B.T @ D @ B
+
+
+def elasticity_parametric(nodes, nu=0.3, clamp_z0=True):
+    """Structure of A(theta) = sum_e theta_e K_e + c for the Kuhn-tet cube with
+    one Young's modulus per tet.  Returns (pattern, M, c): pattern is a CSR
+    matrix (values = A(1)), M the (nnz x ntets) map with A.values = M @ theta + c,
+    c the identity entries of clamped DOFs.  No entry is pruned, so the pattern
+    holds for every theta."""
+    n = nodes
+    N = n ** 3
+    h = np.full(3, 1.0 / (n - 1))
+    ck, cj, ci = np.meshgrid(np.arange(n - 1), np.arange(n - 1), np.arange(n - 1), indexing="ij")
+    origin = np.stack([ci.ravel(), cj.ravel(), ck.ravel()], axis=1)
+    ncell = origin.shape[0]
+    rows, cols, vals, tet = [], [], [], []
+    clamped = np.zeros(N, bool)
+    if clamp_z0:
+        clamped[: n * n] = True
+    for p in range(6):
+        K = _tet_stiffness_ref(p, h, nu)
+        off = _tet_offsets(p)
+        nodes_p = origin[:, None, :] + off[None, :, :]  # ncell x 4 x 3
+        nid = nodes_p[..., 0] + n * (nodes_p[..., 1] + n * nodes_p[..., 2])
+        dof = (3 * nid[:, :, None] + np.arange(3)[None, None, :]).reshape(ncell, 12)
+        r = np.repeat(dof, 12, axis=1)
+        c_ = np.tile(dof, (1, 12))
+        v = np.broadcast_to(K.ravel(), (ncell, 144))
+        t = np.repeat((np.arange(ncell) * 6 + p)[:, None], 144, axis=1)
+        keep = (v != 0) & ~clamped[r // 3] & ~clamped[c_ // 3]
+        rows.append(r[keep]); cols.append(c_[keep]); vals.append(v[keep]); tet.append(t[keep])
+    rows = np.concatenate(rows); cols = np.concatenate(cols); vals = np.concatenate(vals); tet = np.concatenate(tet)
+    cd = np.nonzero(np.repeat(clamped, 3))[0]
+    keys = np.concatenate([rows.astype(np.int64) * (3 * N) + cols, cd.astype(np.int64) * (3 * N) + cd])
+    ukeys, inv = np.unique(keys, return_inverse=True)
+    nnz = len(ukeys)
+    prow = (ukeys // (3 * N)).astype(np.int32)
+    pcol = (ukeys % (3 * N)).astype(np.int32)
+    ntet = 6 * ncell
+    M = sp.csr_matrix((vals, (inv[: len(vals)], tet)), shape=(nnz, ntet))
+    c = np.zeros(nnz)
+    c[inv[len(vals):]] = 1.0
+    indptr = np.zeros(3 * N + 1, np.int64)
+    np.add.at(indptr, prow + 1, 1)
+    indptr = np.cumsum(indptr)
+    pattern = sp.csr_matrix((M @ np.ones(ntet) + c, pcol, indptr), shape=(3 * N, 3 * N))
+    return pattern, M, c

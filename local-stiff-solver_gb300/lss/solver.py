@@ -35,7 +35,7 @@ EXPORTS = [
     "lss_get_info", "lss_name", "lss_analyze_pattern", "lss_factorize", "lss_factorize_device",
     "lss_set_problematic_dofs",
     "lss_solve", "lss_solve_device", "lss_solve_transpose", "lss_grad_A_pattern",
-    "lss_grad_A_pattern_device", "lss_selected_dofs", "lss_gmm_selection", "lss_subdomains",
+    "lss_grad_A_pattern_device", "lss_grad_params_device", "lss_selected_dofs", "lss_gmm_selection", "lss_subdomains",
     "lss_partition", "lss_op_row_l1_norms", "lss_op_spmv", "lss_op_mas_apply", "lss_op_precond",
     "lss_op_time", "lss_set_memory_cap",
 ]
@@ -79,6 +79,7 @@ def load(path: str | None = None):
     L.lss_solve_transpose.argtypes = [vp, _f64p, _f64p]
     L.lss_grad_A_pattern.argtypes = [vp, _f64p, _f64p, _f64p]
     L.lss_grad_A_pattern_device.argtypes = [vp, vp, vp, vp, vp]
+    L.lss_grad_params_device.argtypes = [vp, vp, vp, C.c_int32, vp, vp, vp, vp, vp]
     L.lss_selected_dofs.argtypes = [vp, _i32p, C.c_int32, _i32p]
     L.lss_gmm_selection.argtypes = [vp, _i32p, C.c_int32, _i32p]
     L.lss_subdomains.argtypes = [vp, _i32p, C.c_int32, _i32p, C.c_int32, _i32p, _i32p]
@@ -238,6 +239,11 @@ class Solver:
         out = np.empty(len(self._keep[1]))
         self._check(self._L.lss_grad_A_pattern(self._h, _p(lam, _f64p), _p(x, _f64p), _p(out, _f64p)))
         return out
+
+    def grad_params_device(self, lam_ptr, x_ptr, n_params, rowptr_ptr, cols_ptr, vals_ptr, out_ptr, stream=0):
+        self._check(self._L.lss_grad_params_device(self._h, C.c_void_p(lam_ptr), C.c_void_p(x_ptr), n_params,
+                                                   C.c_void_p(rowptr_ptr), C.c_void_p(cols_ptr),
+                                                   C.c_void_p(vals_ptr), C.c_void_p(out_ptr), C.c_void_p(stream)))
 
     # --- inspection (parity tests)
     def selected_dofs(self) -> np.ndarray:
