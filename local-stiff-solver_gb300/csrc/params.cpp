@@ -218,6 +218,8 @@ Params parse_params(const char *json, const Params &base)
     if (p.max_coarse_levels < 1 || p.max_coarse_levels > 6)
         fail(LSS_ERR_INVALID_ARGUMENT, "gb300.max_coarse_levels must be in [1, 6]");
     if (p.check_every < 1) p.check_every = 1;
+    if (p.spmv_lanes != 0 && (p.spmv_lanes < 1 || p.spmv_lanes > 32 || (p.spmv_lanes & (p.spmv_lanes - 1))))
+        fail(LSS_ERR_INVALID_ARGUMENT, "gb300.spmv_lanes must be 0 (autotune) or a power of two <= 32");
     if (p.omega_iters < 1 || p.omega_iters > 64) fail(LSS_ERR_INVALID_ARGUMENT, "gb300.omega_iters must be in [1, 64]");
     if (!(p.omega_factor > 0.0) || p.omega_factor >= 2.0)
         fail(LSS_ERR_INVALID_ARGUMENT, "gb300.omega_factor must be in (0, 2)");

@@ -45,12 +45,12 @@ __global__ void __launch_bounds__(256) spmv_kernel(BsrDev A, const double *__res
         const bool valid = i < A.nb;
         double acc[BD];
         bsr_block_row<BD, LANES, double, double, double>(A.rows, A.cols, A.vals, (int32_t)i, valid, x, lane, acc);
-        if (valid && lane < BD) {
-            double o = acc[0];
+        // lane l of the group stores the components k with k % LANES == l
+        // (all BD of them when LANES == 1)
+        if (valid) {
 #pragma unroll
-            for (int k = 1; k < BD; ++k)
-                if (lane == k) o = acc[k];
-            y[i * BD + lane] = o;
+            for (int k = 0; k < BD; ++k)
+                if (k % LANES == lane) y[i * BD + k] = acc[k];
         }
     }
 }
@@ -72,12 +72,10 @@ __global__ void __launch_bounds__(256) residual_kernel(BsrDev A, const VT *__res
         const bool valid = i < A.nb;
         ACC acc[BD];
         bsr_block_row<BD, LANES, VT, double, ACC>(A.rows, A.cols, vals, (int32_t)i, valid, x, lane, acc);
-        if (valid && lane < BD) {
-            ACC o = acc[0];
+        if (valid) {
 #pragma unroll
-            for (int k = 1; k < BD; ++k)
-                if (lane == k) o = acc[k];
-            y[i * BD + lane] = r[i * BD + lane] - (double)o;
+            for (int k = 0; k < BD; ++k)
+                if (k % LANES == lane) y[i * BD + k] = r[i * BD + k] - (double)acc[k];
         }
     }
 }
@@ -99,13 +97,13 @@ __global__ void __launch_bounds__(256) spmv_alpha_kernel(BsrDev A, const double 
         const bool valid = i < A.nb;
         double acc[BD];
         bsr_block_row<BD, LANES, double, double, double>(A.rows, A.cols, A.vals, (int32_t)i, valid, p, lane, acc);
-        if (valid && lane < BD) {
-            double o = acc[0];
+        if (valid) {
 #pragma unroll
-            for (int k = 1; k < BD; ++k)
-                if (lane == k) o = acc[k];
-            Ap[i * BD + lane] = o;
-            dot[0] += p[i * BD + lane] * o;
+            for (int k = 0; k < BD; ++k)
+                if (k % LANES == lane) {
+                    Ap[i * BD + k] = acc[k];
+                    dot[0] += p[i * BD + k] * acc[k];
+                }
         }
     }
     double tot[1];

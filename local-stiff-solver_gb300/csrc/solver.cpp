@@ -780,6 +780,9 @@ void HybridSolver::estimate_omega()
     lambda_max_ = tridiag_max_eig(good, d.data(), e.data());
     if (lambda_max_ > 0) omega_ = p_.omega_factor / lambda_max_;
     stats_["mas_lambda_max"] = lambda_max_;
+    std::string hist;
+    for (int j = 0; j < m; ++j) hist += (j ? " " : "") + std::to_string(a[j]) + "/" + std::to_string(b[j]);
+    sstats_["omega_lanczos_alpha_beta"] = hist;
 }
 
 void HybridSolver::solve_host(const double *b, double *x)

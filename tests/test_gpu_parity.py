@@ -100,11 +100,17 @@ def test_selection_matches_oracle_on_workloads(case, built):
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("lanes", [0, 1, 2, 4, 8, 16, 32])
 @pytest.mark.parametrize("bs", [1, 3])
-def test_spmv_matches_scipy(bs, elast20, lap):
+def test_spmv_matches_scipy(bs, lanes, elast20, lap):
+    """Every launch shape (threads per block row; 0 = autotuned), including
+    groups narrower than the block size, where one thread stores several
+    components of the block row."""
     A = elast20[0] if bs == 3 else lap[0]
-    s = _solver({"block_size": bs, "do_hybrid_precond": False})
+    s = _solver({"block_size": bs, "do_hybrid_precond": False}, {"spmv_lanes": lanes} if lanes else None)
     s.factorize(A)
+    if lanes:
+        assert s.get_info()["spmv_lanes"] == lanes
     x = np.random.default_rng(0).standard_normal(A.shape[0])
     y = s.spmv(x)
     ref = A.tocsr() @ x  # outer index = row, like the reference (the matrix is symmetric)
@@ -159,6 +165,58 @@ def test_hybrid_precond_matches_oracle(elast20):
     oa = _oracle_with_product_partition(A, sa, params, additive=True)
     za, zoa = sa.precond(r), oa.precond(r)
     assert np.linalg.norm(za - zoa) / np.linalg.norm(zoa) < 1e-7
+
+
+@pytest.fixture(scope="module")
+def springs16(built):
+    from lss import gen
+    A, b, _ = gen.workload_elasticity_lognormal(seed=0, nodes=16)
+    return A.tocsc(), b
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4])
+def test_mixed_precond_every_residual_shape(lanes, springs16):
+    """Mixed mode: the FP32 residual SpMV inside the multiplicative
+    composition at each launch shape; FP32 MAS against the FP64 oracle with the
+    same damping: 2e-3 relative.  (The FP32 copy of A rounds every term of
+    r - A z, so rows whose terms cancel from a much larger scale -- the rim of
+    a 1e6 inclusion -- carry errors of 6e-8 times that scale; the lognormal
+    moduli with diagonal penalty springs have no such rows.)"""
+    A = springs16[0]
+    params = {"block_size": 3, "decompose_subdomains": False}
+    s = _solver(params, {"precision": "mixed", "spmv_lanes": lanes})
+    s.factorize(A)
+    info = s.get_info()
+    assert info["spmv_lanes"] == info["spmv_lanes_fp32"] == lanes
+    assert len(s.selected_dofs()) > 0  # the composition runs its residual SpMV
+    o = _oracle_with_product_partition(A, s, params, mas_omega=info["mas_omega"])
+    r = np.random.default_rng(2).standard_normal(A.shape[0])
+    z, zo = s.precond(r), o.precond(r)
+    assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < 2e-3
+
+
+def test_mixed_matches_fp64_on_penalty_springs(built):
+    """Lognormal moduli and 1e8 diagonal penalty springs: the mixed mode
+    converges like the FP64 mode (same damping estimate within 1e-4, at most
+    10% more iterations) at every launch shape of the FP32 residual."""
+    from lss import gen
+    A, b, _ = gen.workload_elasticity_lognormal(seed=0, nodes=24)
+    A = A.tocsc()
+    params = {"block_size": 3, "relative_tolerance": 1e-8, "decompose_subdomains": False}
+    ref = _solver(params)
+    ref.factorize(A)
+    ref.solve(b)
+    i64 = ref.get_info()
+    assert i64["status"] == "converged_rel"
+    for lanes in [1, 2, 4]:
+        s = _solver(params, {"precision": "mixed", "spmv_lanes": lanes})
+        s.factorize(A)
+        x = s.solve(b)
+        inf = s.get_info()
+        assert inf["status"] == "converged_rel", (lanes, inf["status"])
+        assert abs(inf["mas_lambda_max"] - i64["mas_lambda_max"]) <= 1e-4 * i64["mas_lambda_max"]
+        assert inf["num_iterations"] <= 1.1 * i64["num_iterations"] + 2, (lanes, inf["num_iterations"])
+        _check_solution(A, b, x)
 
 
 def _outer_as_row(A):
