@@ -182,6 +182,36 @@ lss_status lss_op_time(lss_solver *s, int32_t kind, int32_t reps, double *ms_per
  * exercises the out-of-memory path without exhausting the GPU. */
 lss_status lss_set_memory_cap(size_t bytes);
 
+/* ---- allocation-free entry point ----------------------------------------- */
+
+/* Largest n accepted by lss_gmm_select_device_noalloc. */
+#define LSS_NOALLOC_MAX_ROWS (1 << 20)
+
+/* No counterpart in the reference: an allocation-free form of the selection
+ * that lss_gmm_selection reports (l1 row norms GPUHybrid.cu:753-765, GMM
+ * GPUHybrid.cu:767-879), for callers that cannot allocate (pre-reserved
+ * memory, allocator-free contexts).  Same kernels, same result: the selected
+ * rows, ascending, bit-identical to lss_gmm_selection of a solver factorized
+ * with the same matrix and GMM parameters.
+ *   - n <= LSS_NOALLOC_MAX_ROWS, else LSS_ERR_INVALID_ARGUMENT before any
+ *     device work;
+ *   - d_outer[n+1], d_values[nnz]: device arrays of the matrix (CSC, or CSR:
+ *     the matrix is symmetric); d_selected[n] receives the rows, d_count[1]
+ *     their number; all on the current device;
+ *   - stream: a cudaStream_t of the current device (NULL = legacy default).
+ * Allocates nothing: every intermediate lives in one static device scratch
+ * area of 8,610,304 bytes inside liblss.so.  The first call on a device
+ * resolves the scratch address (cudaGetSymbolAddress, which can load the
+ * module): make it before any stream capture.  Calls share the scratch, so
+ * calls that can overlap (other streams or threads) race and must be
+ * serialised by the caller.  Only the scratch's grid-reduction arrival counter
+ * must start at zero: it is zero at module load and every reduction leaves it
+ * at zero.  Stream-ordered; no host synchronisation. */
+lss_status lss_gmm_select_device_noalloc(int32_t n, int64_t nnz, const int32_t *d_outer,
+                                         const double *d_values, double gmm_jump_threshold,
+                                         double gmm_tol, int32_t max_gmm_iterations,
+                                         int32_t *d_selected, int32_t *d_count, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

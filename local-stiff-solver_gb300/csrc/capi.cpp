@@ -4,6 +4,7 @@
 #include <new>
 #include <string>
 
+#include "noalloc.hpp"
 #include "solver.hpp"
 
 namespace lss {
@@ -331,3 +332,13 @@ lss_status lss_set_memory_cap(size_t bytes)
 }
 
 }  // extern "C"
+
+lss_status lss_gmm_select_device_noalloc(int32_t n, int64_t nnz, const int32_t *d_outer, const double *d_values,
+                                         double gmm_jump_threshold, double gmm_tol, int32_t max_gmm_iterations,
+                                         int32_t *d_selected, int32_t *d_count, void *stream)
+{
+    return guarded(nullptr, [&]() {
+        lss::noalloc_gmm_select(n, nnz, d_outer, d_values, gmm_jump_threshold, gmm_tol, max_gmm_iterations,
+                                d_selected, d_count, (cudaStream_t)stream);
+    });
+}

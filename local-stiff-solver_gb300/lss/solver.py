@@ -37,7 +37,7 @@ EXPORTS = [
     "lss_solve", "lss_solve_device", "lss_solve_transpose", "lss_grad_A_pattern",
     "lss_grad_A_pattern_device", "lss_grad_params_device", "lss_selected_dofs", "lss_gmm_selection", "lss_subdomains",
     "lss_partition", "lss_op_row_l1_norms", "lss_op_spmv", "lss_op_mas_apply", "lss_op_precond",
-    "lss_op_time", "lss_set_memory_cap",
+    "lss_op_time", "lss_set_memory_cap", "lss_gmm_select_device_noalloc",
 ]
 
 
@@ -90,6 +90,8 @@ def load(path: str | None = None):
     L.lss_op_precond.argtypes = [vp, _f64p, _f64p]
     L.lss_op_time.argtypes = [vp, C.c_int32, C.c_int32, _f64p, _f64p]
     L.lss_set_memory_cap.argtypes = [C.c_size_t]
+    L.lss_gmm_select_device_noalloc.argtypes = [C.c_int32, C.c_int64, vp, vp, C.c_double, C.c_double, C.c_int32,
+                                                vp, vp, vp]
     for name in EXPORTS:
         fn = getattr(L, name)
         if fn.restype is C.c_int or fn.restype is None:
