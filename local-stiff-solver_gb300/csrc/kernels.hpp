@@ -70,6 +70,10 @@ void launch_spmv(const BsrDev &A, const double *x, double *y, const int *done, c
 // y = r - A x, FP64 (fp32 == false) or with the FP32 operator copy (fp32 == true)
 void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, double *y, bool fp32,
                           const int *done, cudaStream_t s);
+// The same with the FP32 operator copy and an FP32 x (no FP64-pipe conversions
+// in the product); r and y stay FP64.
+void launch_residual_spmv_x32(const BsrDev &A, const double *r, const float *x32, double *y, const int *done,
+                              cudaStream_t s);
 
 // ---------------------------------------------------------------- PCG
 enum StopReason : int {
@@ -146,9 +150,10 @@ void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, b
 // z = MAS^-1 xin (acc: z += MAS^-1 xin).  dot_mode 1: st->gamma = rdot.z;
 // dot_mode 2: st->beta = rdot.z / st->gamma, st->gamma = rdot.z.
 // z = scale * MAS^-1 xin, or z += scale * MAS^-1 xin with acc.
+// z32 (optional): also store z rounded to FP32 (the input of the FP32 residual)
 void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
                       const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
-                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s);
+                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s, float *z32 = nullptr);
 
 // level-0 bank SYMV alone (z = Inv_0 xin + coarse correction already in u), for timing
 void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp32, const double *xin, double *z,
@@ -174,6 +179,8 @@ void launch_stiff_to_fp32(int64_t count, const double *src, float *dst, cudaStre
 void launch_stiff_gather(const BsrDev &A, const StiffDev &S, const double *r, const double *z, bool residual,
                          const int *done, cudaStream_t s);
 // z_S += Inv t
-void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done, cudaStream_t s);
+// z32 (optional): FP32 shadow of z, updated at the DOFs the correction changes
+void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done, cudaStream_t s,
+                        float *z32 = nullptr);
 
 }  // namespace lss

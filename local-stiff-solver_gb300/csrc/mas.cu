@@ -197,38 +197,52 @@ __global__ void __launch_bounds__(256) mas_invert_kernel(const double *__restric
 
 // ------------------------------------------------------------------ apply
 
+// Segmented sums of one bank: 32 items (values staged item-major in xs, the
+// target aggregate of each item in ks) into ncc aggregates.  Output slot
+// s = k * BD + c (aggregate k, component c) belongs to lane s % 32, which adds
+// the items of aggregate k in item order: no FP64 shuffles (each costs 16
+// cycles of the SM's FP64 pipe on this part), a fixed summation order, and in
+// FP32 mode no FP64 instruction at all.
+template <int BD, typename T>
+__device__ __forceinline__ void bank_segment_sums(const T *xs, const uint8_t *ks, int ncc, T *__restrict__ out,
+                                                  int lane)
+{
+    for (int sl = lane; sl < ncc * BD; sl += 32) {
+        const int k = sl / BD, c = sl - k * BD;
+        T acc = T(0);
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j)
+            if (ks[j] == k) acc += xs[j * BD + c];
+        out[(int64_t)k * BD + c] = acc;
+    }
+}
+
 // level 0 -> level 1: per-part component sums of r
 template <int BD, typename T>
 __global__ void __launch_bounds__(256) restrict0_kernel(MasDev m, const double *__restrict__ r, T *__restrict__ v,
                                                         const int *done)
 {
     if (done && *done) return;
-    const int lane = threadIdx.x & 31;
+    __shared__ T xs_all[8][32 * BD];
+    __shared__ uint8_t ks_all[8][32];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    T *xs = xs_all[wl];
+    uint8_t *ks = ks_all[wl];
     const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     T *v1 = v + m.voff[1];
     for (int64_t p = w0; p < m.nparts; p += nw) {
-        const int32_t lo = m.part_off[p], node = lo + lane;
-        const bool valid = node < m.part_off[p + 1];
-        double x[BD];
-        int key = 255;
-        if (valid) {
-            key = m.key0[node];
+        const int32_t lo = m.part_off[p], cnt = m.part_off[p + 1] - lo;
+        // the part's values are one contiguous run: coalesced loads
 #pragma unroll
-            for (int c = 0; c < BD; ++c) x[c] = r[(int64_t)node * BD + c];
-        } else {
-#pragma unroll
-            for (int c = 0; c < BD; ++c) x[c] = 0.0;
+        for (int q = 0; q < BD; ++q) {
+            const int e = q * 32 + lane;
+            xs[e] = e < cnt * BD ? (T)r[(int64_t)lo * BD + e] : T(0);
         }
-        const int ncc = m.ccnt0[p];
-        const int32_t base = m.cbase0[p];
-        for (int k = 0; k < ncc; ++k) {
-#pragma unroll
-            for (int c = 0; c < BD; ++c) {
-                const double s = warp_sum(key == k ? x[c] : 0.0);
-                if (lane == c) v1[(int64_t)(base + k) * BD + c] = (T)s;
-            }
-        }
+        ks[lane] = lane < cnt ? m.key0[lo + lane] : (uint8_t)0xff;
+        __syncwarp();
+        bank_segment_sums<BD, T>(xs, ks, m.ccnt0[p], v1 + (int64_t)m.cbase0[p] * BD, lane);
+        __syncwarp();
     }
 }
 
@@ -237,28 +251,31 @@ template <int BD, typename T>
 __global__ void __launch_bounds__(256) restrict_kernel(MasDev m, int l, T *__restrict__ v, const int *done)
 {
     if (done && *done) return;
-    const int lane = threadIdx.x & 31;
+    __shared__ T xs_all[8][32 * BD];
+    __shared__ uint8_t ks_all[8][32];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    T *xs = xs_all[wl];
+    uint8_t *ks = ks_all[wl];
     const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const T *vl = v + m.voff[l];
     T *vn = v + m.voff[l + 1];
     const uint8_t *key_l = m.key[l];
+    const uint8_t *ccnt_l = m.ccnt[l];
+    const int32_t *cbase_l = m.cbase[l];
+    const int32_t nitems = m.nitems[l];
     for (int64_t b = w0; b < m.nbanks[l]; b += nw) {
-        const int64_t item = b * 32 + lane;
-        const bool valid = item < m.nitems[l];
-        double x[BD];
+        const int64_t i0 = b * 32;
+        const int cnt = nitems - i0 < 32 ? (int)(nitems - i0) : 32;
 #pragma unroll
-        for (int c = 0; c < BD; ++c) x[c] = valid ? (double)vl[item * BD + c] : 0.0;
-        const int key = valid ? key_l[item] : 255;
-        const int ncc = m.ccnt[l][b];
-        const int32_t base = m.cbase[l][b];
-        for (int k = 0; k < ncc; ++k) {
-#pragma unroll
-            for (int c = 0; c < BD; ++c) {
-                const double s = warp_sum(key == k ? x[c] : 0.0);
-                if (lane == c) vn[(int64_t)(base + k) * BD + c] = (T)s;
-            }
+        for (int q = 0; q < BD; ++q) {
+            const int e = q * 32 + lane;
+            xs[e] = e < cnt * BD ? vl[i0 * BD + e] : T(0);
         }
+        ks[lane] = lane < cnt ? key_l[i0 + lane] : (uint8_t)0xff;
+        __syncwarp();
+        bank_segment_sums<BD, T>(xs, ks, ccnt_l[b], vn + (int64_t)cbase_l[b] * BD, lane);
+        __syncwarp();
     }
 }
 
@@ -286,16 +303,24 @@ __global__ void __launch_bounds__(256) symv_coarse_kernel(MasDev m, const T *__r
     }
 }
 
-// u_l += P u_{l+1} (top-down, one level per launch)
+// u_1 += P (u_2 + P (u_3 + ...)): every level-1 item gathers its ancestors'
+// corrections and sums them from the top level down, as level-by-level
+// prolongation would, in one launch.
 template <int BD, typename T>
-__global__ void __launch_bounds__(256) prolong_kernel(MasDev m, int l, T *__restrict__ u, const int *done)
+__global__ void __launch_bounds__(256) prolong_all_kernel(MasDev m, T *__restrict__ u, const int *done)
 {
     if (done && *done) return;
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= m.nitems[l]) return;
-    const int64_t parent = m.cbase[l][k >> 5] + m.key[l][k];
+    if (k >= m.nitems[1]) return;
+    int64_t item[MAS_MAXL];
+    item[1] = k;
+    for (int l = 1; l + 1 < m.L; ++l) item[l + 1] = m.cbase[l][item[l] >> 5] + m.key[l][item[l]];
 #pragma unroll
-    for (int c = 0; c < BD; ++c) u[m.voff[l] + k * BD + c] += u[m.voff[l + 1] + parent * BD + c];
+    for (int c = 0; c < BD; ++c) {
+        T acc = u[m.voff[m.L - 1] + item[m.L - 1] * BD + c];
+        for (int l = m.L - 2; l >= 1; --l) acc = u[m.voff[l] + item[l] * BD + c] + acc;
+        u[m.voff[1] + k * BD + c] = acc;
+    }
 }
 
 // level 0: z = Inv_0 x (+ coarse correction u_1), optional accumulate and r.z
@@ -303,7 +328,7 @@ template <int BD, typename T, bool ACC, int DOT>
 __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restrict__ inv0, const T *__restrict__ u,
                                                     const double *__restrict__ xin, double *__restrict__ z,
                                                     double scale, const double *__restrict__ rdot, PcgState *st,
-                                                    GridReduce gr, const int *done)
+                                                    GridReduce gr, const int *done, float *__restrict__ z32)
 {
     if (done && *done) return;
     const int lane = threadIdx.x & 31;
@@ -329,6 +354,7 @@ __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restric
                 const int64_t e = (int64_t)node * BD + c;
                 if (ACC) val += z[e];
                 z[e] = val;
+                if (z32) z32[e] = (float)val;
                 if (DOT) dot[0] += rdot[e] * val;
             }
         }
@@ -350,7 +376,7 @@ __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restric
 template <int BD, typename T>
 void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, const double *xin, double *z,
                      bool acc, double scale, const double *rdot, PcgState *st, int dot_mode, GridReduce gr,
-                     const int *done, cudaStream_t s)
+                     const int *done, cudaStream_t s, float *z32)
 {
     if (m.L > 1) {
         restrict0_kernel<BD, T><<<grid_for((int64_t)m.nparts * 32, 256, 152 * 16), 256, 0, s>>>(m, xin, v, done);
@@ -358,19 +384,19 @@ void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, 
             restrict_kernel<BD, T><<<grid_for((int64_t)m.nbanks[l] * 32, 256, 152 * 16), 256, 0, s>>>(m, l, v, done);
         symv_coarse_kernel<BD, T><<<grid_for((int64_t)m.ncoarse * 32, 256, 152 * 16), 256, 0, s>>>(m, invc, v, u,
                                                                                                    done);
-        for (int l = m.L - 2; l >= 1; --l)
-            prolong_kernel<BD, T><<<grid_for(m.nitems[l], 256, 1 << 30), 256, 0, s>>>(m, l, u, done);
+        if (m.L > 2)
+            prolong_all_kernel<BD, T><<<grid_for(m.nitems[1], 256, 1 << 30), 256, 0, s>>>(m, u, done);
     }
     const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
     if (dot_mode == 0) {
-        if (acc) symv0_kernel<BD, T, true, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
-        else symv0_kernel<BD, T, false, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
+        if (acc) symv0_kernel<BD, T, true, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
+        else symv0_kernel<BD, T, false, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
     } else if (dot_mode == 1) {
-        if (acc) symv0_kernel<BD, T, true, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
-        else symv0_kernel<BD, T, false, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
+        if (acc) symv0_kernel<BD, T, true, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
+        else symv0_kernel<BD, T, false, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
     } else {
-        if (acc) symv0_kernel<BD, T, true, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
-        else symv0_kernel<BD, T, false, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done);
+        if (acc) symv0_kernel<BD, T, true, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
+        else symv0_kernel<BD, T, false, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
     }
     LSS_LAUNCH_CHECK();
 }
@@ -438,7 +464,7 @@ void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp
     GridReduce gr{};
 #define LSS_L0(BD_, T_)                                                                                        \
     symv0_kernel<BD_, T_, false, 0><<<grid, 256, 0, s>>>(m, (const T_ *)inv0, (const T_ *)u, xin, z, 1.0, nullptr, \
-                                                         nullptr, gr, nullptr)
+                                                         nullptr, gr, nullptr, nullptr)
     if (fp32) {
         if (m.bd == 1) LSS_L0(1, float);
         else if (m.bd == 2) LSS_L0(2, float);
@@ -454,11 +480,11 @@ void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp
 
 void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
                       const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
-                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s)
+                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s, float *z32)
 {
 #define LSS_MAS(BD_, T_)                                                                                          \
     mas_apply_dot_t<BD_, T_>(m, (const T_ *)inv0, (const T_ *)invc, (T_ *)v, (T_ *)u, xin, z, acc, scale, rdot, \
-                             st, dot_mode, gr, done, s)
+                             st, dot_mode, gr, done, s, z32)
     if (fp32) {
         if (m.bd == 1) LSS_MAS(1, float);
         else if (m.bd == 2) LSS_MAS(2, float);

@@ -56,9 +56,9 @@ __global__ void __launch_bounds__(256) spmv_kernel(BsrDev A, const double *__res
 }
 
 // y = r - A x, operator in VT precision, accumulation in ACC
-template <int BD, int LANES, typename VT, typename ACC>
+template <int BD, int LANES, typename VT, typename ACC, typename XT>
 __global__ void __launch_bounds__(256) residual_kernel(BsrDev A, const VT *__restrict__ vals,
-                                                       const double *__restrict__ r, const double *__restrict__ x,
+                                                       const double *__restrict__ r, const XT *__restrict__ x,
                                                        double *__restrict__ y, const int *done)
 {
     if (done && *done) return;
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) residual_kernel(BsrDev A, const VT *__res
         const int64_t i = wr + (threadIdx.x & 31) / LANES;
         const bool valid = i < A.nb;
         ACC acc[BD];
-        bsr_block_row<BD, LANES, VT, double, ACC>(A.rows, A.cols, vals, (int32_t)i, valid, x, lane, acc);
+        bsr_block_row<BD, LANES, VT, XT, ACC>(A.rows, A.cols, vals, (int32_t)i, valid, x, lane, acc);
         if (valid) {
 #pragma unroll
             for (int k = 0; k < BD; ++k)
@@ -273,19 +273,19 @@ void spmv_dispatch(const BsrDev &A, const double *x, double *y, const int *done,
     }
 }
 
-template <int BD, typename VT, typename ACC>
-void residual_dispatch(const BsrDev &A, const VT *vals, const double *r, const double *x, double *y,
+template <int BD, typename VT, typename ACC, typename XT>
+void residual_dispatch(const BsrDev &A, const VT *vals, const double *r, const XT *x, double *y,
                        const int *done, cudaStream_t s)
 {
     const int lanes = sizeof(VT) == 4 ? A.lanes32 : A.lanes;
     const int grid = grid_for((int64_t)A.nb * lanes, 256, 152 * 16);
     switch (lanes) {
-    case 1: residual_kernel<BD, 1, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
-    case 2: residual_kernel<BD, 2, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
-    case 4: residual_kernel<BD, 4, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
-    case 8: residual_kernel<BD, 8, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
-    case 16: residual_kernel<BD, 16, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
-    default: residual_kernel<BD, 32, VT, ACC><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    case 1: residual_kernel<BD, 1, VT, ACC, XT><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    case 2: residual_kernel<BD, 2, VT, ACC, XT><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    case 4: residual_kernel<BD, 4, VT, ACC, XT><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    case 8: residual_kernel<BD, 8, VT, ACC, XT><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    case 16: residual_kernel<BD, 16, VT, ACC, XT><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
+    default: residual_kernel<BD, 32, VT, ACC, XT><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
     }
 }
 
@@ -325,14 +325,23 @@ void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, dou
                           cudaStream_t s)
 {
     if (fp32) {
-        if (A.bd == 1) residual_dispatch<1, float, float>(A, A.vals32, r, x, y, done, s);
-        else if (A.bd == 2) residual_dispatch<2, float, float>(A, A.vals32, r, x, y, done, s);
-        else residual_dispatch<3, float, float>(A, A.vals32, r, x, y, done, s);
+        if (A.bd == 1) residual_dispatch<1, float, float, double>(A, A.vals32, r, x, y, done, s);
+        else if (A.bd == 2) residual_dispatch<2, float, float, double>(A, A.vals32, r, x, y, done, s);
+        else residual_dispatch<3, float, float, double>(A, A.vals32, r, x, y, done, s);
     } else {
-        if (A.bd == 1) residual_dispatch<1, double, double>(A, A.vals, r, x, y, done, s);
-        else if (A.bd == 2) residual_dispatch<2, double, double>(A, A.vals, r, x, y, done, s);
-        else residual_dispatch<3, double, double>(A, A.vals, r, x, y, done, s);
+        if (A.bd == 1) residual_dispatch<1, double, double, double>(A, A.vals, r, x, y, done, s);
+        else if (A.bd == 2) residual_dispatch<2, double, double, double>(A, A.vals, r, x, y, done, s);
+        else residual_dispatch<3, double, double, double>(A, A.vals, r, x, y, done, s);
     }
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_residual_spmv_x32(const BsrDev &A, const double *r, const float *x32, double *y, const int *done,
+                              cudaStream_t s)
+{
+    if (A.bd == 1) residual_dispatch<1, float, float, float>(A, A.vals32, r, x32, y, done, s);
+    else if (A.bd == 2) residual_dispatch<2, float, float, float>(A, A.vals32, r, x32, y, done, s);
+    else residual_dispatch<3, float, float, float>(A, A.vals32, r, x32, y, done, s);
     LSS_LAUNCH_CHECK();
 }
 

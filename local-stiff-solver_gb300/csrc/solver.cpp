@@ -494,14 +494,17 @@ void HybridSolver::ensure_vectors()
 {
     const int64_t n = n_vec();
     for (DBuf<double> *b : {&d_x_, &d_b_, &d_r_, &d_p_, &d_z_, &d_ap_, &d_w_, &d_tmp_}) b->resize(n);
+    if (p_.mixed) d_z32_.resize(n);
+    else d_z32_.release();
 }
 
 // ------------------------------------------------------------------ preconditioner
 
-void HybridSolver::mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale)
+void HybridSolver::mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale,
+                             float *z32)
 {
     launch_mas_apply(mas_, d_inv0_.data(), d_invc_.data(), d_v_.data(), d_u_.data(), mas_fp32_, xin, z, acc, scale,
-                     rdot, d_state_.data(), dot_mode, gr_, &d_state_.data()->done, stream_);
+                     rdot, d_state_.data(), dot_mode, gr_, &d_state_.data()->done, stream_, z32);
 }
 
 void HybridSolver::rz_dot(const double *r, const double *z, int dot_mode)
@@ -530,10 +533,14 @@ void HybridSolver::precond(const double *r, double *z, int dot_mode)
     // The symmetric product is SPD when I - w M A contracts in the A-norm;
     // additive MAS has lambda_max(M A) of a few units, so w = omega_factor /
     // lambda_max(M A) is estimated at factorize time (estimate_omega).
-    mas_apply(r, z, false, nullptr, 0, omega_);
+    // mixed precision: z also goes out rounded to FP32 (the stiff correction
+    // keeps that copy current), so the FP32 residual SpMV converts nothing
+    float *z32 = p_.mixed ? d_z32_.data() : nullptr;
+    mas_apply(r, z, false, nullptr, 0, omega_, z32);
     launch_stiff_gather(A_, stiff_, r, z, true, done, stream_);
-    launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_);
-    launch_residual_spmv(A_, r, z, d_w_.data(), p_.mixed, done, stream_);
+    launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_, z32);
+    if (z32) launch_residual_spmv_x32(A_, r, z32, d_w_.data(), done, stream_);
+    else launch_residual_spmv(A_, r, z, d_w_.data(), false, done, stream_);
     mas_apply(d_w_.data(), z, true, r, dot_mode, omega_);
 }
 
@@ -663,6 +670,7 @@ void HybridSolver::autotune_spmv()
     for (int64_t i = 0; i < n; ++i) h[i] = 1.0 + 1e-3 * (double)(i % 89);
     LSS_CUDA(cudaMemcpyAsync(d_p_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
     LSS_CUDA(cudaMemcpyAsync(d_r_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    if (A_.vals32) launch_stiff_to_fp32(n, d_p_.data(), d_z32_.data(), stream_);
     cudaEvent_t e0, e1;
     LSS_CUDA(cudaEventCreate(&e0));
     LSS_CUDA(cudaEventCreate(&e1));
@@ -685,8 +693,8 @@ void HybridSolver::autotune_spmv()
             T.lanes = T.lanes32 = l;
             const float ms = pass == 0 ? time_it([&]() { launch_spmv(T, d_p_.data(), d_ap_.data(), nullptr, stream_); })
                                        : time_it([&]() {
-                                             launch_residual_spmv(T, d_r_.data(), d_p_.data(), d_ap_.data(), true,
-                                                                  nullptr, stream_);
+                                             launch_residual_spmv_x32(T, d_r_.data(), d_z32_.data(), d_ap_.data(),
+                                                                      nullptr, stream_);
                                          });
             log += (pass ? " f32:" : " f64:") + std::to_string(l) + "=" + std::to_string(ms / 5);
             if (ms < best) { best = ms; best_l = l; }
@@ -920,6 +928,7 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
     LSS_CUDA(cudaMemcpyAsync(d_r_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
     LSS_CUDA(cudaMemcpyAsync(d_x_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
     LSS_CUDA(cudaMemcpyAsync(d_z_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    if (p_.mixed) launch_stiff_to_fp32(n, d_p_.data(), d_z32_.data(), stream_);
     auto body = [&]() {
         switch (kind) {
         case 0: launch_spmv(A_, d_p_.data(), d_ap_.data(), nullptr, stream_); break;
@@ -927,7 +936,10 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
         case 2: precond(d_r_.data(), d_z_.data(), 0); break;
         case 4: launch_mas_level0(mas_, d_inv0_.data(), d_u_.data(), mas_fp32_, d_r_.data(), d_z_.data(), stream_);
             break;
-        case 5: launch_residual_spmv(A_, d_r_.data(), d_p_.data(), d_ap_.data(), p_.mixed, nullptr, stream_); break;
+        case 5:
+            if (p_.mixed) launch_residual_spmv_x32(A_, d_r_.data(), d_z32_.data(), d_ap_.data(), nullptr, stream_);
+            else launch_residual_spmv(A_, d_r_.data(), d_p_.data(), d_ap_.data(), false, nullptr, stream_);
+            break;
         default: iteration(); break;
         }
     };
@@ -949,7 +961,8 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
     const double mas_bytes = (double)(mas_.nparts + mas_.ncoarse) * mas_.tile_elems * esz + 2.0 * n * 8 +
                              (double)pat_.nb * (1 + 4);
     const double vb = p_.mixed ? 4.0 : 8.0;  // operator value bytes of the residual SpMV
-    const double res_bytes = (double)nnzb * (bd * bd * vb + 4) + (pat_.nb + 1) * 4.0 + 3.0 * n * 8;
+    // r and y in FP64; x in FP32 in mixed precision (the shadow of z), FP64 otherwise
+    const double res_bytes = (double)nnzb * (bd * bd * vb + 4) + (pat_.nb + 1) * 4.0 + (p_.mixed ? 20.0 : 24.0) * n;
     const double mas0_bytes = (double)mas_.nparts * mas_.tile_elems * esz + 2.0 * n * 8 + (double)pat_.nb * 5;
     switch (kind) {
     case 0: *bytes = spmv_bytes; break;

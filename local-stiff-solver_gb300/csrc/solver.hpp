@@ -73,7 +73,8 @@ private:
     void ensure_vectors();
     void run_pcg();
     void precond(const double *r, double *z, int dot_mode);
-    void mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale);
+    void mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale,
+                   float *z32 = nullptr);
     void estimate_omega();
     void autotune_spmv();
     void iteration();
@@ -117,6 +118,7 @@ private:
     DBuf<float> d_sinv32_;
     // PCG
     DBuf<double> d_x_, d_b_, d_r_, d_p_, d_z_, d_ap_, d_w_, d_tmp_;
+    DBuf<float> d_z32_;  // mixed precision: FP32 shadow of z, input of the FP32 residual SpMV
     DBuf<PcgState> d_state_;
     PcgState *h_state_ = nullptr;
     DBuf<double> d_partials_, d_scalar_;

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) gather_kernel(BsrDev A, StiffDev S, const
 
 template <typename VT>
 __global__ void __launch_bounds__(256) apply_kernel(StiffDev S, const VT *__restrict__ inv, double *__restrict__ z,
-                                                    const int *done)
+                                                    float *__restrict__ z32, const int *done)
 {
     if (done && *done) return;
     const int lane = threadIdx.x & 31;
@@ -233,7 +233,12 @@ __global__ void __launch_bounds__(256) apply_kernel(StiffDev S, const VT *__rest
     double acc = 0.0;
     for (int32_t k = lane; k < m; k += 32) acc += (double)row[k] * t[k];
     acc = warp_sum(acc);
-    if (lane == 0) z[S.dofs[j]] += acc;
+    if (lane == 0) {
+        const int32_t d = S.dofs[j];
+        const double nz = z[d] + acc;
+        z[d] = nz;
+        if (z32) z32[d] = (float)nz;
+    }
 }
 
 __global__ void to_fp32_kernel(int64_t count, const double *__restrict__ src, float *__restrict__ dst)
@@ -328,12 +333,12 @@ void launch_stiff_gather(const BsrDev &A, const StiffDev &S, const double *r, co
     LSS_LAUNCH_CHECK();
 }
 
-void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done, cudaStream_t s)
+void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done, cudaStream_t s, float *z32)
 {
     if (S.ndof == 0) return;
     const int grid = (int)(((int64_t)S.ndof * 32 + 255) / 256);
-    if (fp32) apply_kernel<float><<<grid, 256, 0, s>>>(S, S.inv32, z, done);
-    else apply_kernel<double><<<grid, 256, 0, s>>>(S, S.inv, z, done);
+    if (fp32) apply_kernel<float><<<grid, 256, 0, s>>>(S, S.inv32, z, z32, done);
+    else apply_kernel<double><<<grid, 256, 0, s>>>(S, S.inv, z, z32, done);
     LSS_LAUNCH_CHECK();
 }
 
