@@ -163,6 +163,11 @@ lss_status lss_op_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer,
 /* y = A x with the factorized FP64 operator (original ordering). */
 lss_status lss_op_spmv(lss_solver *s, const double *x, double *y);
 
+/* y = A x with the PCG's own operator product (the A p of pcg_solve,
+ * GPUHybrid.cu:1458): FP64, or double-float on the FP32 pipe when
+ * gb300.outer_spmv resolves to "df32". */
+lss_status lss_op_spmv_outer(lss_solver *s, const double *x, double *y);
+
 /* z = MAS^-1 r alone (MASPreconditioner::apply, MASPreconditioner.cu:1099). */
 lss_status lss_op_mas_apply(lss_solver *s, const double *r, double *z);
 
@@ -173,8 +178,11 @@ lss_status lss_op_precond(lss_solver *s, const double *r, double *z);
 /* Time `reps` launches of one kernel family on device-resident operands:
  * kind 0 = FP64 SpMV, 1 = MAS apply, 2 = full preconditioner, 3 = one PCG
  * iteration, 4 = the level-0 bank SYMV kernel of MAS alone, 5 = the residual
- * SpMV inside the preconditioner (FP32 operator in mixed precision).  Writes the mean milliseconds per launch (CUDA events on the
- * solver's stream) and the algorithmic bytes of one launch. */
+ * SpMV inside the preconditioner (FP32 operator in mixed precision), 6 = the
+ * PCG's own A p with p.Ap (FP64, or double-float on the FP32 pipe when
+ * gb300.outer_spmv resolves to "df32").  Writes the mean milliseconds per
+ * launch (CUDA events on the solver's stream) and the algorithmic bytes of
+ * one launch. */
 lss_status lss_op_time(lss_solver *s, int32_t kind, int32_t reps, double *ms_per_launch,
                        double *bytes_per_launch);
 

@@ -306,6 +306,12 @@ lss_status lss_op_spmv(lss_solver *s, const double *x, double *y)
     return guarded(s, [&]() { s->impl->op_spmv(x, y); });
 }
 
+lss_status lss_op_spmv_outer(lss_solver *s, const double *x, double *y)
+{
+    if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->op_spmv_outer(x, y); });
+}
+
 lss_status lss_op_mas_apply(lss_solver *s, const double *r, double *z)
 {
     if (!valid(s)) return LSS_ERR_INVALID_ARGUMENT;

@@ -60,20 +60,21 @@ struct BsrDev {
     const int32_t *cols = nullptr;
     const double *vals = nullptr;  // row-sliced layout (spmv.cuh)
     const float *vals32 = nullptr; // FP32 copy (mixed precision preconditioner)
+    const float2 *vals_df = nullptr; // df32 pairs (hi, lo): vals = hi + lo to 2^-48 relative
 };
 
 // vals[j] = src >= 0 ? csc[src] : 0  (BSR slot gather)
 void launch_gather_values(int64_t count, const int64_t *src, const double *csc, double *vals, float *vals32,
-                          cudaStream_t s);
+                          cudaStream_t s, float2 *vals_df = nullptr);
 // y = A x  (FP64)
 void launch_spmv(const BsrDev &A, const double *x, double *y, const int *done, cudaStream_t s);
 // y = r - A x, FP64 (fp32 == false) or with the FP32 operator copy (fp32 == true)
 void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, double *y, bool fp32,
                           const int *done, cudaStream_t s);
-// The same with the FP32 operator copy and an FP32 x (no FP64-pipe conversions
-// in the product); r and y stay FP64.
-void launch_residual_spmv_x32(const BsrDev &A, const double *r, const float *x32, double *y, const int *done,
-                              cudaStream_t s);
+// y32 = r32 - A x32 entirely in FP32 with the FP32 operator copy (no FP64
+// instruction; the mixed preconditioner's residual)
+void launch_residual32(const BsrDev &A, const float *r32, const float *x32, float *y32, const int *done,
+                       cudaStream_t s);
 
 // ---------------------------------------------------------------- PCG
 enum StopReason : int {
@@ -100,10 +101,25 @@ void launch_dot(int64_t n, const double *a, const double *b, double *out, GridRe
 void launch_pcg_spmv_alpha(const BsrDev &A, const double *p, double *Ap, PcgState *st, GridReduce gr,
                            cudaStream_t s);
 // x += alpha p; r -= alpha Ap; rr = r.r; convergence tests
+// r32 (optional): also r rounded to FP32
 void launch_pcg_update_xr(int64_t n, double *x, double *r, const double *p, const double *Ap, PcgState *st,
-                          GridReduce gr, cudaStream_t s);
+                          GridReduce gr, cudaStream_t s, float *r32 = nullptr);
+// the same with A p as df32 (hi, lo) pairs
+void launch_pcg_update_xr_df(int64_t n, double *x, double *r, const double *p, const float2 *Ap_df, PcgState *st,
+                             GridReduce gr, cudaStream_t s, float *r32 = nullptr);
+void launch_df_to_double(int64_t n, const float2 *src, double *dst, cudaStream_t s);
 // p = z + beta p
-void launch_pcg_update_p(int64_t n, double *p, const double *z, const PcgState *st, cudaStream_t s);
+// p_df (optional): the df32 split of the new p, the x operand of the df32 SpMV
+void launch_pcg_update_p(int64_t n, double *p, const double *z, const PcgState *st, cudaStream_t s,
+                         float2 *p_df = nullptr);
+// dst = (fl32(src), fl32(src - fl32(src)))
+void launch_split(int64_t n, const double *src, float2 *dst, cudaStream_t s);
+// Ap = A p, p.Ap and alpha like launch_pcg_spmv_alpha, with the products and
+// row sums in double-float arithmetic on the FP32 pipe: A and p as (hi, lo)
+// FP32 pairs (both to 2^-48 relative), error-free products and sums
+// (TwoProd / TwoSum), the result rounded to FP64 once per row component.
+void launch_pcg_spmv_alpha_df(const BsrDev &A, const float2 *p_df, float2 *Ap_df, PcgState *st, GridReduce gr,
+                              cudaStream_t s);
 void launch_copy(int64_t n, const double *src, double *dst, const int *done, cudaStream_t s);
 void launch_permute(int64_t nb, int bd, const int32_t *perm, const double *src, double *dst, bool to_new,
                     cudaStream_t s);
@@ -150,10 +166,12 @@ void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, b
 // z = MAS^-1 xin (acc: z += MAS^-1 xin).  dot_mode 1: st->gamma = rdot.z;
 // dot_mode 2: st->beta = rdot.z / st->gamma, st->gamma = rdot.z.
 // z = scale * MAS^-1 xin, or z += scale * MAS^-1 xin with acc.
-// z32 (optional): also store z rounded to FP32 (the input of the FP32 residual)
+// z32 (optional): also store z rounded to FP32 (the input of the FP32 residual).
+// xin32 (optional, FP32 MAS only): an FP32 input used in place of xin.
 void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
                       const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
-                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s, float *z32 = nullptr);
+                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s, float *z32 = nullptr,
+                      const float *xin32 = nullptr);
 
 // level-0 bank SYMV alone (z = Inv_0 xin + coarse correction already in u), for timing
 void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp32, const double *xin, double *z,

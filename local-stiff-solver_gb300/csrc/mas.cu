@@ -218,8 +218,8 @@ __device__ __forceinline__ void bank_segment_sums(const T *xs, const uint8_t *ks
 }
 
 // level 0 -> level 1: per-part component sums of r
-template <int BD, typename T>
-__global__ void __launch_bounds__(256) restrict0_kernel(MasDev m, const double *__restrict__ r, T *__restrict__ v,
+template <int BD, typename T, typename XT>
+__global__ void __launch_bounds__(256) restrict0_kernel(MasDev m, const XT *__restrict__ r, T *__restrict__ v,
                                                         const int *done)
 {
     if (done && *done) return;
@@ -323,10 +323,11 @@ __global__ void __launch_bounds__(256) prolong_all_kernel(MasDev m, T *__restric
     }
 }
 
-// level 0: z = Inv_0 x (+ coarse correction u_1), optional accumulate and r.z
-template <int BD, typename T, bool ACC, int DOT>
+// level 0: z = Inv_0 x (+ coarse correction u_1), optional accumulate and r.z;
+// x in FP64, or in FP32 (XT = float) when it comes from the FP32 residual
+template <int BD, typename T, bool ACC, int DOT, typename XT>
 __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restrict__ inv0, const T *__restrict__ u,
-                                                    const double *__restrict__ xin, double *__restrict__ z,
+                                                    const XT *__restrict__ xin, double *__restrict__ z,
                                                     double scale, const double *__restrict__ rdot, PcgState *st,
                                                     GridReduce gr, const int *done, float *__restrict__ z32)
 {
@@ -373,13 +374,13 @@ __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restric
     }
 }
 
-template <int BD, typename T>
-void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, const double *xin, double *z,
+template <int BD, typename T, typename XT>
+void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, const XT *xin, double *z,
                      bool acc, double scale, const double *rdot, PcgState *st, int dot_mode, GridReduce gr,
                      const int *done, cudaStream_t s, float *z32)
 {
     if (m.L > 1) {
-        restrict0_kernel<BD, T><<<grid_for((int64_t)m.nparts * 32, 256, 152 * 16), 256, 0, s>>>(m, xin, v, done);
+        restrict0_kernel<BD, T, XT><<<grid_for((int64_t)m.nparts * 32, 256, 152 * 16), 256, 0, s>>>(m, xin, v, done);
         for (int l = 1; l + 1 < m.L; ++l)
             restrict_kernel<BD, T><<<grid_for((int64_t)m.nbanks[l] * 32, 256, 152 * 16), 256, 0, s>>>(m, l, v, done);
         symv_coarse_kernel<BD, T><<<grid_for((int64_t)m.ncoarse * 32, 256, 152 * 16), 256, 0, s>>>(m, invc, v, u,
@@ -388,16 +389,19 @@ void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, 
             prolong_all_kernel<BD, T><<<grid_for(m.nitems[1], 256, 1 << 30), 256, 0, s>>>(m, u, done);
     }
     const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
+#define LSS_S0(A_, D_) \
+    symv0_kernel<BD, T, A_, D_, XT><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32)
     if (dot_mode == 0) {
-        if (acc) symv0_kernel<BD, T, true, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
-        else symv0_kernel<BD, T, false, 0><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
+        if (acc) LSS_S0(true, 0);
+        else LSS_S0(false, 0);
     } else if (dot_mode == 1) {
-        if (acc) symv0_kernel<BD, T, true, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
-        else symv0_kernel<BD, T, false, 1><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
+        if (acc) LSS_S0(true, 1);
+        else LSS_S0(false, 1);
     } else {
-        if (acc) symv0_kernel<BD, T, true, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
-        else symv0_kernel<BD, T, false, 2><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32);
+        if (acc) LSS_S0(true, 2);
+        else LSS_S0(false, 2);
     }
+#undef LSS_S0
     LSS_LAUNCH_CHECK();
 }
 
@@ -463,8 +467,8 @@ void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp
     const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
     GridReduce gr{};
 #define LSS_L0(BD_, T_)                                                                                        \
-    symv0_kernel<BD_, T_, false, 0><<<grid, 256, 0, s>>>(m, (const T_ *)inv0, (const T_ *)u, xin, z, 1.0, nullptr, \
-                                                         nullptr, gr, nullptr, nullptr)
+    symv0_kernel<BD_, T_, false, 0, double><<<grid, 256, 0, s>>>(m, (const T_ *)inv0, (const T_ *)u, xin, z, 1.0,   \
+                                                                 nullptr, nullptr, gr, nullptr, nullptr)
     if (fp32) {
         if (m.bd == 1) LSS_L0(1, float);
         else if (m.bd == 2) LSS_L0(2, float);
@@ -480,11 +484,21 @@ void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp
 
 void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
                       const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
-                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s, float *z32)
+                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s, float *z32, const float *xin32)
 {
 #define LSS_MAS(BD_, T_)                                                                                          \
-    mas_apply_dot_t<BD_, T_>(m, (const T_ *)inv0, (const T_ *)invc, (T_ *)v, (T_ *)u, xin, z, acc, scale, rdot, \
-                             st, dot_mode, gr, done, s, z32)
+    mas_apply_dot_t<BD_, T_, double>(m, (const T_ *)inv0, (const T_ *)invc, (T_ *)v, (T_ *)u, xin, z, acc, scale, \
+                                     rdot, st, dot_mode, gr, done, s, z32)
+#define LSS_MAS32(BD_)                                                                                            \
+    mas_apply_dot_t<BD_, float, float>(m, (const float *)inv0, (const float *)invc, (float *)v, (float *)u, xin32, \
+                                       z, acc, scale, rdot, st, dot_mode, gr, done, s, z32)
+    if (xin32) {
+        if (!fp32) fail(LSS_ERR_INTERNAL, "an FP32 input needs the FP32 MAS");
+        if (m.bd == 1) LSS_MAS32(1);
+        else if (m.bd == 2) LSS_MAS32(2);
+        else LSS_MAS32(3);
+        return;
+    }
     if (fp32) {
         if (m.bd == 1) LSS_MAS(1, float);
         else if (m.bd == 2) LSS_MAS(2, float);
@@ -495,6 +509,7 @@ void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void 
         else LSS_MAS(3, double);
     }
 #undef LSS_MAS
+#undef LSS_MAS32
 }
 
 }  // namespace lss

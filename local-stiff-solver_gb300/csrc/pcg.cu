@@ -18,7 +18,8 @@ namespace lss {
 namespace {
 
 __global__ void gather_values_kernel(int64_t count, const int64_t *__restrict__ src, const double *__restrict__ csc,
-                                     double *__restrict__ vals, float *__restrict__ vals32)
+                                     double *__restrict__ vals, float *__restrict__ vals32,
+                                     float2 *__restrict__ vals_df)
 {
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count;
          j += (int64_t)gridDim.x * blockDim.x) {
@@ -26,6 +27,10 @@ __global__ void gather_values_kernel(int64_t count, const int64_t *__restrict__ 
         const double v = k >= 0 ? csc[k] : 0.0;
         vals[j] = v;
         if (vals32) vals32[j] = (float)v;
+        if (vals_df) {
+            const float h = (float)v;
+            vals_df[j] = make_float2(h, (float)(v - (double)h));
+        }
     }
 }
 
@@ -80,6 +85,31 @@ __global__ void __launch_bounds__(256) residual_kernel(BsrDev A, const VT *__res
     }
 }
 
+// y32 = r32 - A32 x32 entirely in FP32 (the mixed preconditioner's residual:
+// its result feeds the FP32 MAS, and no FP64 instruction is issued)
+template <int BD, int LANES>
+__global__ void __launch_bounds__(256) residual32_kernel(BsrDev A, const float *__restrict__ r32,
+                                                         const float *__restrict__ x32, float *__restrict__ y32,
+                                                         const int *done)
+{
+    if (done && *done) return;
+    const int lane = threadIdx.x % LANES;
+    constexpr int RPW = 32 / LANES;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t wr = w0 * RPW; wr < A.nb; wr += nw * RPW) {
+        const int64_t i = wr + (threadIdx.x & 31) / LANES;
+        const bool valid = i < A.nb;
+        float acc[BD];
+        bsr_block_row<BD, LANES, float, float, float>(A.rows, A.cols, A.vals32, (int32_t)i, valid, x32, lane, acc);
+        if (valid) {
+#pragma unroll
+            for (int k = 0; k < BD; ++k)
+                if (k % LANES == lane) y32[i * BD + k] = r32[i * BD + k] - acc[k];
+        }
+    }
+}
+
 // Ap = A p, p.Ap, then alpha with the breakdown tests (GPUHybrid.cu:1458-1480)
 template <int BD, int LANES>
 __global__ void __launch_bounds__(256) spmv_alpha_kernel(BsrDev A, const double *__restrict__ p,
@@ -122,17 +152,26 @@ __global__ void __launch_bounds__(256) spmv_alpha_kernel(BsrDev A, const double 
 }
 
 // x += alpha p; r -= alpha Ap; rr; convergence (GPUHybrid.cu:1482-1496)
+__device__ __forceinline__ double as_double(double v) { return v; }
+__device__ __forceinline__ double as_double(float2 v) { return (double)v.x + (double)v.y; }
+
+// AT: double, or float2 for the (hi, lo) product of the df32 SpMV.  r32
+// (optional): r rounded to FP32, the input of the mixed preconditioner's
+// FP32 residual -- converted here, where every lane of a warp converts one
+// entry (a partly predicated FP64 instruction costs the pipe a full warp).
+template <typename AT>
 __global__ void __launch_bounds__(256) update_xr_kernel(int64_t n, double *__restrict__ x, double *__restrict__ r,
-                                                        const double *__restrict__ p, const double *__restrict__ Ap,
-                                                        PcgState *st, GridReduce gr)
+                                                        const double *__restrict__ p, const AT *__restrict__ Ap,
+                                                        PcgState *st, GridReduce gr, float *__restrict__ r32)
 {
     if (st->done) return;
     const double alpha = st->alpha;
     double s[1] = {0.0};
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         x[i] += alpha * p[i];
-        const double ri = r[i] - alpha * Ap[i];
+        const double ri = r[i] - alpha * as_double(Ap[i]);
         r[i] = ri;
+        if (r32) r32[i] = (float)ri;
         s[0] += ri * ri;
     }
     double tot[1];
@@ -146,14 +185,74 @@ __global__ void __launch_bounds__(256) update_xr_kernel(int64_t n, double *__res
     }
 }
 
-// p = z + beta p (GPUHybrid.cu:1506-1507)
+// p = z + beta p (GPUHybrid.cu:1506-1507); optionally also its df32 split
 __global__ void __launch_bounds__(256) update_p_kernel(int64_t n, double *__restrict__ p, const double *__restrict__ z,
-                                                       const PcgState *st)
+                                                       const PcgState *st, float2 *__restrict__ p_df)
 {
     if (st->done) return;
     const double beta = st->beta;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p[i] = z[i] + beta * p[i];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = z[i] + beta * p[i];
+        p[i] = v;
+        if (p_df) {
+            const float h = (float)v;
+            p_df[i] = make_float2(h, (float)(v - (double)h));
+        }
+    }
+}
+
+__global__ void split_kernel(int64_t n, const double *__restrict__ src, float2 *__restrict__ dst)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = src[i];
+        const float h = (float)v;
+        dst[i] = make_float2(h, (float)(v - (double)h));
+    }
+}
+
+// spmv_alpha_kernel with the SpMV in double-float on the FP32 pipe.  A p
+// leaves as (hi, lo) pairs and p.Ap accumulates in double-float, so the loop
+// issues no FP64 instruction: the storing lanes (k % LANES == lane) would
+// run them as partly predicated warps, each costing the FP64 pipe a full warp.
+template <int BD, int LANES>
+__global__ void __launch_bounds__(256) spmv_alpha_df_kernel(BsrDev A, const float2 *__restrict__ p_df,
+                                                            float2 *__restrict__ Ap, PcgState *st, GridReduce gr)
+{
+    if (st->done) return;
+    const int lane = threadIdx.x % LANES;
+    constexpr int RPW = 32 / LANES;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    float dh = 0.f, dl = 0.f;
+    for (int64_t wr = w0 * RPW; wr < A.nb; wr += nw * RPW) {
+        const int64_t i = wr + (threadIdx.x & 31) / LANES;
+        const bool valid = i < A.nb;
+        float sh[BD], sl[BD];
+        bsr_block_row_df<BD, LANES>(A.rows, A.cols, A.vals_df, (int32_t)i, valid, p_df, lane, sh, sl);
+        if (valid) {
+#pragma unroll
+            for (int k = 0; k < BD; ++k)
+                if (k % LANES == lane) {
+                    Ap[i * BD + k] = make_float2(sh[k], sl[k]);
+                    const float2 pk = p_df[i * BD + k];
+                    df_fma(dh, dl, pk.x, pk.y, sh[k], sl[k]);
+                }
+        }
+    }
+    double dot[1] = {(double)dh + (double)dl};
+    double tot[1];
+    if (grid_sum<1>(dot, gr, tot)) {
+        st->iter += 1;
+        const double pAp = tot[0];
+        st->pAp = pAp;
+        if (pAp == 0.0) { st->done = STOP_ZERO_PAP; return; }
+        const double alpha = st->gamma / pAp;
+        if (!(alpha == alpha) || isinf(alpha)) { st->done = STOP_NONFINITE; return; }
+        if (alpha <= 0.0) { st->done = STOP_NEGATIVE_ALPHA; return; }
+        if (alpha < DBL_MIN) { st->done = STOP_SUBNORMAL_ALPHA; return; }
+        st->alpha = alpha;
+        if (st->iter <= PCG_HIST) st->hist_alpha[st->iter - 1] = alpha;
+    }
 }
 
 __global__ void __launch_bounds__(256) dot_kernel(int64_t n, const double *__restrict__ a, const double *__restrict__ b,
@@ -306,10 +405,10 @@ void spmv_alpha_dispatch(const BsrDev &A, const double *p, double *Ap, PcgState 
 }  // namespace
 
 void launch_gather_values(int64_t count, const int64_t *src, const double *csc, double *vals, float *vals32,
-                          cudaStream_t s)
+                          cudaStream_t s, float2 *vals_df)
 {
     if (count == 0) return;
-    gather_values_kernel<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(count, src, csc, vals, vals32);
+    gather_values_kernel<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(count, src, csc, vals, vals32, vals_df);
     LSS_LAUNCH_CHECK();
 }
 
@@ -336,12 +435,29 @@ void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, dou
     LSS_LAUNCH_CHECK();
 }
 
-void launch_residual_spmv_x32(const BsrDev &A, const double *r, const float *x32, double *y, const int *done,
-                              cudaStream_t s)
+template <int BD>
+void residual32_dispatch(const BsrDev &A, const float *r32, const float *x32, float *y32, const int *done,
+                         cudaStream_t s)
 {
-    if (A.bd == 1) residual_dispatch<1, float, float, float>(A, A.vals32, r, x32, y, done, s);
-    else if (A.bd == 2) residual_dispatch<2, float, float, float>(A, A.vals32, r, x32, y, done, s);
-    else residual_dispatch<3, float, float, float>(A, A.vals32, r, x32, y, done, s);
+    const int grid = grid_for((int64_t)A.nb * A.lanes32, 256, 152 * 16);
+    switch (A.lanes32) {
+    case 1: residual32_kernel<BD, 1><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
+    case 2: residual32_kernel<BD, 2><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
+    case 4: residual32_kernel<BD, 4><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
+    case 8: residual32_kernel<BD, 8><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
+    case 16: residual32_kernel<BD, 16><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
+    default: residual32_kernel<BD, 32><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
+    }
+}
+
+void launch_residual32(const BsrDev &A, const float *r32, const float *x32, float *y32, const int *done,
+                       cudaStream_t s)
+{
+    if (A.nb > 0 && (!A.vals32 || !r32 || !x32 || !y32))
+        fail(LSS_ERR_INTERNAL, "FP32 residual SpMV launched without its operand arrays");
+    if (A.bd == 1) residual32_dispatch<1>(A, r32, x32, y32, done, s);
+    else if (A.bd == 2) residual32_dispatch<2>(A, r32, x32, y32, done, s);
+    else residual32_dispatch<3>(A, r32, x32, y32, done, s);
     LSS_LAUNCH_CHECK();
 }
 
@@ -359,16 +475,70 @@ void launch_pcg_spmv_alpha(const BsrDev &A, const double *p, double *Ap, PcgStat
     LSS_LAUNCH_CHECK();
 }
 
-void launch_pcg_update_xr(int64_t n, double *x, double *r, const double *p, const double *Ap, PcgState *st,
-                          GridReduce gr, cudaStream_t s)
+template <int BD>
+void spmv_alpha_df_dispatch(const BsrDev &A, const float2 *pd, float2 *Ap, PcgState *st, GridReduce gr,
+                            cudaStream_t s)
 {
-    update_xr_kernel<<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, x, r, p, Ap, st, gr);
+    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, GRID_MAX);
+    switch (A.lanes) {
+    case 1: spmv_alpha_df_kernel<BD, 1><<<grid, 256, 0, s>>>(A, pd, Ap, st, gr); break;
+    case 2: spmv_alpha_df_kernel<BD, 2><<<grid, 256, 0, s>>>(A, pd, Ap, st, gr); break;
+    case 4: spmv_alpha_df_kernel<BD, 4><<<grid, 256, 0, s>>>(A, pd, Ap, st, gr); break;
+    case 8: spmv_alpha_df_kernel<BD, 8><<<grid, 256, 0, s>>>(A, pd, Ap, st, gr); break;
+    case 16: spmv_alpha_df_kernel<BD, 16><<<grid, 256, 0, s>>>(A, pd, Ap, st, gr); break;
+    default: spmv_alpha_df_kernel<BD, 32><<<grid, 256, 0, s>>>(A, pd, Ap, st, gr); break;
+    }
+}
+
+void launch_pcg_spmv_alpha_df(const BsrDev &A, const float2 *p_df, float2 *Ap_df, PcgState *st, GridReduce gr,
+                              cudaStream_t s)
+{
+    if (A.nb > 0 && (!A.vals_df || !p_df || !Ap_df))
+        fail(LSS_ERR_INTERNAL, "df32 SpMV launched without its operand arrays");
+    if (A.bd == 1) spmv_alpha_df_dispatch<1>(A, p_df, Ap_df, st, gr, s);
+    else if (A.bd == 2) spmv_alpha_df_dispatch<2>(A, p_df, Ap_df, st, gr, s);
+    else spmv_alpha_df_dispatch<3>(A, p_df, Ap_df, st, gr, s);
     LSS_LAUNCH_CHECK();
 }
 
-void launch_pcg_update_p(int64_t n, double *p, const double *z, const PcgState *st, cudaStream_t s)
+__global__ void df_to_double_kernel(int64_t n, const float2 *__restrict__ src, double *__restrict__ dst)
 {
-    update_p_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, p, z, st);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = as_double(src[i]);
+}
+
+void launch_df_to_double(int64_t n, const float2 *src, double *dst, cudaStream_t s)
+{
+    if (n == 0) return;
+    df_to_double_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, src, dst);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_split(int64_t n, const double *src, float2 *dst, cudaStream_t s)
+{
+    if (n == 0) return;
+    if (!src || !dst) fail(LSS_ERR_INTERNAL, "split launched without its arrays");
+    split_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, src, dst);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_pcg_update_xr(int64_t n, double *x, double *r, const double *p, const double *Ap, PcgState *st,
+                          GridReduce gr, cudaStream_t s, float *r32)
+{
+    update_xr_kernel<double><<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, x, r, p, Ap, st, gr, r32);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_pcg_update_xr_df(int64_t n, double *x, double *r, const double *p, const float2 *Ap_df, PcgState *st,
+                             GridReduce gr, cudaStream_t s, float *r32)
+{
+    update_xr_kernel<float2><<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, x, r, p, Ap_df, st, gr, r32);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_pcg_update_p(int64_t n, double *p, const double *z, const PcgState *st, cudaStream_t s, float2 *p_df)
+{
+    update_p_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, p, z, st, p_df);
     LSS_LAUNCH_CHECK();
 }
 

@@ -86,7 +86,7 @@ void HybridSolver::set_parameters(const char *json)
                                  np.cond_threshold != p_.cond_threshold || np.decompose != p_.decompose ||
                                  np.min_sub != p_.min_sub || np.max_sub != p_.max_sub || np.expand != p_.expand ||
                                  np.float_subdomains != p_.float_subdomains ||
-                                 np.multiplicative != p_.multiplicative;
+                                 np.multiplicative != p_.multiplicative || np.outer_spmv != p_.outer_spmv;
     p_ = np;
     if (pattern_affecting) have_pattern_ = false;
     if (value_affecting) factorized_ = false;
@@ -117,6 +117,7 @@ std::string HybridSolver::info_json() const
     o << ", \"status\": \"" << stop_name(stop_reason_) << "\"";
     o << ", \"refinements\": " << refinements_;
     o << ", \"precision\": \"" << (p_.mixed ? "mixed" : "fp64") << "\"";
+    o << ", \"outer_spmv\": \"" << (df32() ? "df32" : "fp64") << "\"";
     o << ", \"composition\": \"" << (p_.multiplicative ? "multiplicative" : "additive") << "\"";
     o << ", \"mas_omega\": " << omega_;
     o << ", \"kernel_launches\": " << launch_count();
@@ -276,12 +277,16 @@ void HybridSolver::factorize_common()
     d_bad_.zero(stream_);
     launch_check_finite(nnz, d_csc_.data(), d_bad_.data(), stream_);
     mas_fp32_ = p_.mixed;
+    const bool df = df32();
     if (p_.mixed) d_vals32_.resize(pat_.src.size());
     else d_vals32_.release();
+    if (df) d_vals_df_.resize(pat_.src.size());
+    else d_vals_df_.release();
     launch_gather_values((int64_t)pat_.src.size(), d_src_.data(), d_csc_.data(), d_vals_.data(),
-                         p_.mixed ? d_vals32_.data() : nullptr, stream_);
+                         p_.mixed ? d_vals32_.data() : nullptr, stream_, df ? d_vals_df_.data() : nullptr);
     A_.vals = d_vals_.data();
     A_.vals32 = p_.mixed ? d_vals32_.data() : nullptr;
+    A_.vals_df = df ? d_vals_df_.data() : nullptr;
     int bad = 0;
     LSS_CUDA(cudaMemcpyAsync(&bad, d_bad_.data(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
     LSS_CUDA(cudaStreamSynchronize(stream_));
@@ -494,17 +499,23 @@ void HybridSolver::ensure_vectors()
 {
     const int64_t n = n_vec();
     for (DBuf<double> *b : {&d_x_, &d_b_, &d_r_, &d_p_, &d_z_, &d_ap_, &d_w_, &d_tmp_}) b->resize(n);
-    if (p_.mixed) d_z32_.resize(n);
-    else d_z32_.release();
+    for (DBuf<float> *b : {&d_z32_, &d_r32_, &d_w32_}) {
+        if (p_.mixed) b->resize(n);
+        else b->release();
+    }
+    for (DBuf<float2> *b : {&d_p_df_, &d_ap_df_}) {
+        if (df32()) b->resize(n);
+        else b->release();
+    }
 }
 
 // ------------------------------------------------------------------ preconditioner
 
 void HybridSolver::mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale,
-                             float *z32)
+                             float *z32, const float *xin32)
 {
     launch_mas_apply(mas_, d_inv0_.data(), d_invc_.data(), d_v_.data(), d_u_.data(), mas_fp32_, xin, z, acc, scale,
-                     rdot, d_state_.data(), dot_mode, gr_, &d_state_.data()->done, stream_, z32);
+                     rdot, d_state_.data(), dot_mode, gr_, &d_state_.data()->done, stream_, z32, xin32);
 }
 
 void HybridSolver::rz_dot(const double *r, const double *z, int dot_mode)
@@ -513,7 +524,7 @@ void HybridSolver::rz_dot(const double *r, const double *z, int dot_mode)
 }
 
 // z = M^-1 r.  dot_mode 0: nothing; 1: gamma = r.z; 2: beta, gamma update.
-void HybridSolver::precond(const double *r, double *z, int dot_mode)
+void HybridSolver::precond(const double *r, double *z, int dot_mode, const float *r32)
 {
     const int *done = &d_state_.data()->done;
     const bool stiff = p_.do_hybrid && stiff_.ndof > 0 && !lanczos_mode_;
@@ -533,26 +544,58 @@ void HybridSolver::precond(const double *r, double *z, int dot_mode)
     // The symmetric product is SPD when I - w M A contracts in the A-norm;
     // additive MAS has lambda_max(M A) of a few units, so w = omega_factor /
     // lambda_max(M A) is estimated at factorize time (estimate_omega).
+    if (!p_.mixed) {
+        mas_apply(r, z, false, nullptr, 0, omega_);
+        launch_stiff_gather(A_, stiff_, r, z, true, done, stream_);
+        launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_);
+        launch_residual_spmv(A_, r, z, d_w_.data(), false, done, stream_);
+        mas_apply(d_w_.data(), z, true, r, dot_mode, omega_);
+        return;
+    }
     // mixed precision: z also goes out rounded to FP32 (the stiff correction
-    // keeps that copy current), so the FP32 residual SpMV converts nothing
-    float *z32 = p_.mixed ? d_z32_.data() : nullptr;
+    // keeps that copy current) and r - A z runs entirely in FP32 into the
+    // second, FP32 MAS apply; no FP64 instruction is spent on conversions
+    // inside the SpMV (r32 comes from the PCG update, or is converted here).
+    if (!r32) {
+        launch_stiff_to_fp32(n_vec(), r, d_r32_.data(), stream_);
+        r32 = d_r32_.data();
+    }
+    float *z32 = d_z32_.data();
     mas_apply(r, z, false, nullptr, 0, omega_, z32);
     launch_stiff_gather(A_, stiff_, r, z, true, done, stream_);
     launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_, z32);
-    if (z32) launch_residual_spmv_x32(A_, r, z32, d_w_.data(), done, stream_);
-    else launch_residual_spmv(A_, r, z, d_w_.data(), false, done, stream_);
-    mas_apply(d_w_.data(), z, true, r, dot_mode, omega_);
+    launch_residual32(A_, r32, z32, d_w32_.data(), done, stream_);
+    mas_apply(nullptr, z, true, r, dot_mode, omega_, nullptr, d_w32_.data());
 }
 
 // ------------------------------------------------------------------ PCG
 
+void HybridSolver::outer_spmv_alpha()
+{
+    if (df32())
+        launch_pcg_spmv_alpha_df(A_, d_p_df_.data(), d_ap_df_.data(), d_state_.data(), gr_, stream_);
+    else
+        launch_pcg_spmv_alpha(A_, d_p_.data(), d_ap_.data(), d_state_.data(), gr_, stream_);
+}
+
+void HybridSolver::split_p()
+{
+    if (df32()) launch_split(n_vec(), d_p_.data(), d_p_df_.data(), stream_);
+}
+
 void HybridSolver::iteration()
 {
-    launch_pcg_spmv_alpha(A_, d_p_.data(), d_ap_.data(), d_state_.data(), gr_, stream_);
-    launch_pcg_update_xr(n_vec(), d_x_.data(), d_r_.data(), d_p_.data(), d_ap_.data(), d_state_.data(), gr_,
-                         stream_);
-    precond(d_r_.data(), d_z_.data(), 2);
-    launch_pcg_update_p(n_vec(), d_p_.data(), d_z_.data(), d_state_.data(), stream_);
+    outer_spmv_alpha();
+    float *r32 = p_.mixed ? d_r32_.data() : nullptr;
+    if (df32())
+        launch_pcg_update_xr_df(n_vec(), d_x_.data(), d_r_.data(), d_p_.data(), d_ap_df_.data(), d_state_.data(),
+                                gr_, stream_, r32);
+    else
+        launch_pcg_update_xr(n_vec(), d_x_.data(), d_r_.data(), d_p_.data(), d_ap_.data(), d_state_.data(), gr_,
+                             stream_, r32);
+    precond(d_r_.data(), d_z_.data(), 2, r32);
+    launch_pcg_update_p(n_vec(), d_p_.data(), d_z_.data(), d_state_.data(), stream_,
+                        df32() ? d_p_df_.data() : nullptr);
 }
 
 void HybridSolver::launch_chunk(int iters)
@@ -622,6 +665,7 @@ void HybridSolver::run_pcg()
         if (p_.max_iter > 0) {
             precond(d_r_.data(), d_z_.data(), 1);
             launch_copy(n, d_z_.data(), d_p_.data(), nullptr, stream_);
+            split_p();
         }
         while (launched < p_.max_iter) {
             const int chunk = std::min(p_.check_every, p_.max_iter - launched);
@@ -670,7 +714,10 @@ void HybridSolver::autotune_spmv()
     for (int64_t i = 0; i < n; ++i) h[i] = 1.0 + 1e-3 * (double)(i % 89);
     LSS_CUDA(cudaMemcpyAsync(d_p_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
     LSS_CUDA(cudaMemcpyAsync(d_r_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
-    if (A_.vals32) launch_stiff_to_fp32(n, d_p_.data(), d_z32_.data(), stream_);
+    if (p_.mixed) {
+        launch_stiff_to_fp32(n, d_p_.data(), d_z32_.data(), stream_);
+        launch_stiff_to_fp32(n, d_r_.data(), d_r32_.data(), stream_);
+    }
     cudaEvent_t e0, e1;
     LSS_CUDA(cudaEventCreate(&e0));
     LSS_CUDA(cudaEventCreate(&e1));
@@ -685,18 +732,32 @@ void HybridSolver::autotune_spmv()
         return ms;
     };
     std::string log;
-    for (int pass = 0; pass < (A_.vals32 ? 2 : 1); ++pass) {
+    if (df32()) {
+        split_p();
+        PcgState hs{};
+        hs.gamma = 1.0;
+        hs.max_iter = 1 << 30;
+        *h_state_ = hs;
+        LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
+    }
+    for (int pass = 0; pass < (p_.mixed ? 2 : 1); ++pass) {
         float best = 1e30f;
         int best_l = 4;
         for (int l : {1, 2, 4, 8, 16}) {
             BsrDev T = A_;
             T.lanes = T.lanes32 = l;
-            const float ms = pass == 0 ? time_it([&]() { launch_spmv(T, d_p_.data(), d_ap_.data(), nullptr, stream_); })
+            const float ms = pass == 0 ? time_it([&]() {
+                                             if (df32())
+                                                 launch_pcg_spmv_alpha_df(T, d_p_df_.data(), d_ap_df_.data(),
+                                                                          d_state_.data(), gr_, stream_);
+                                             else
+                                                 launch_spmv(T, d_p_.data(), d_ap_.data(), nullptr, stream_);
+                                         })
                                        : time_it([&]() {
-                                             launch_residual_spmv_x32(T, d_r_.data(), d_z32_.data(), d_ap_.data(),
-                                                                      nullptr, stream_);
+                                             launch_residual32(T, d_r32_.data(), d_z32_.data(), d_w32_.data(),
+                                                               nullptr, stream_);
                                          });
-            log += (pass ? " f32:" : " f64:") + std::to_string(l) + "=" + std::to_string(ms / 5);
+            log += (pass ? " f32:" : (df32() ? " df32:" : " f64:")) + std::to_string(l) + "=" + std::to_string(ms / 5);
             if (ms < best) { best = ms; best_l = l; }
         }
         if (pass == 0) A_.lanes = best_l;
@@ -766,6 +827,7 @@ void HybridSolver::estimate_omega()
     try {
         precond(d_r_.data(), d_z_.data(), 1);
         launch_copy(n, d_z_.data(), d_p_.data(), nullptr, stream_);
+        split_p();
         for (int j = 0; j < k; ++j) iteration();
     } catch (...) {
         lanczos_mode_ = false;
@@ -878,6 +940,25 @@ void HybridSolver::op_spmv(const double *x, double *y)
     LSS_CUDA(cudaStreamSynchronize(stream_));
 }
 
+void HybridSolver::op_spmv_outer(const double *x, double *y)
+{
+    if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "no factorized operator");
+    const int64_t n = n_vec();
+    PcgState hs{};
+    hs.gamma = 1.0;
+    hs.max_iter = 1 << 30;
+    *h_state_ = hs;
+    LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
+    LSS_CUDA(cudaMemcpyAsync(d_tmp_.data(), x, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_p_.data(), true, stream_);
+    split_p();
+    outer_spmv_alpha();
+    if (df32()) launch_df_to_double(n, d_ap_df_.data(), d_ap_.data(), stream_);
+    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_ap_.data(), d_tmp_.data(), false, stream_);
+    LSS_CUDA(cudaMemcpyAsync(y, d_tmp_.data(), n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+}
+
 void HybridSolver::op_mas(const double *r, double *z)
 {
     if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "no factorized operator");
@@ -928,7 +1009,11 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
     LSS_CUDA(cudaMemcpyAsync(d_r_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
     LSS_CUDA(cudaMemcpyAsync(d_x_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
     LSS_CUDA(cudaMemcpyAsync(d_z_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
-    if (p_.mixed) launch_stiff_to_fp32(n, d_p_.data(), d_z32_.data(), stream_);
+    if (p_.mixed) {
+        launch_stiff_to_fp32(n, d_p_.data(), d_z32_.data(), stream_);
+        launch_stiff_to_fp32(n, d_r_.data(), d_r32_.data(), stream_);
+    }
+    split_p();
     auto body = [&]() {
         switch (kind) {
         case 0: launch_spmv(A_, d_p_.data(), d_ap_.data(), nullptr, stream_); break;
@@ -937,9 +1022,10 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
         case 4: launch_mas_level0(mas_, d_inv0_.data(), d_u_.data(), mas_fp32_, d_r_.data(), d_z_.data(), stream_);
             break;
         case 5:
-            if (p_.mixed) launch_residual_spmv_x32(A_, d_r_.data(), d_z32_.data(), d_ap_.data(), nullptr, stream_);
+            if (p_.mixed) launch_residual32(A_, d_r32_.data(), d_z32_.data(), d_w32_.data(), nullptr, stream_);
             else launch_residual_spmv(A_, d_r_.data(), d_p_.data(), d_ap_.data(), false, nullptr, stream_);
             break;
+        case 6: outer_spmv_alpha(); break;
         default: iteration(); break;
         }
     };
@@ -961,14 +1047,15 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
     const double mas_bytes = (double)(mas_.nparts + mas_.ncoarse) * mas_.tile_elems * esz + 2.0 * n * 8 +
                              (double)pat_.nb * (1 + 4);
     const double vb = p_.mixed ? 4.0 : 8.0;  // operator value bytes of the residual SpMV
-    // r and y in FP64; x in FP32 in mixed precision (the shadow of z), FP64 otherwise
-    const double res_bytes = (double)nnzb * (bd * bd * vb + 4) + (pat_.nb + 1) * 4.0 + (p_.mixed ? 20.0 : 24.0) * n;
+    // r, x, y in FP32 in mixed precision, FP64 otherwise
+    const double res_bytes = (double)nnzb * (bd * bd * vb + 4) + (pat_.nb + 1) * 4.0 + (p_.mixed ? 12.0 : 24.0) * n;
     const double mas0_bytes = (double)mas_.nparts * mas_.tile_elems * esz + 2.0 * n * 8 + (double)pat_.nb * 5;
     switch (kind) {
     case 0: *bytes = spmv_bytes; break;
     case 1: *bytes = mas_bytes; break;
     case 4: *bytes = mas0_bytes; break;
     case 5: *bytes = res_bytes; break;
+    case 6: *bytes = spmv_bytes + 8.0 * n; break;  // + p for p.Ap
     default: *bytes = 0; break;
     }
 }

@@ -38,6 +38,7 @@ public:
 
     // operator-level access (original ordering, host pointers)
     void op_spmv(const double *x, double *y);
+    void op_spmv_outer(const double *x, double *y);
     void op_mas(const double *r, double *z);
     void op_precond(const double *r, double *z);
     void op_time(int kind, int reps, double *ms, double *bytes);
@@ -72,9 +73,10 @@ private:
     void setup_mas();
     void ensure_vectors();
     void run_pcg();
-    void precond(const double *r, double *z, int dot_mode);
+    // r32 (optional): r already rounded to FP32 (mixed precision); converted here otherwise
+    void precond(const double *r, double *z, int dot_mode, const float *r32 = nullptr);
     void mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale,
-                   float *z32 = nullptr);
+                   float *z32 = nullptr, const float *xin32 = nullptr);
     void estimate_omega();
     void autotune_spmv();
     void iteration();
@@ -101,6 +103,7 @@ private:
     DBuf<int32_t> d_rows_, d_cols_, d_perm_, d_outer_, d_inner_, d_row_of_;
     DBuf<double> d_vals_, d_csc_;
     DBuf<float> d_vals32_;
+    DBuf<float2> d_vals_df_;  // df32 outer SpMV: operator values as (hi, lo) FP32 pairs
     DBuf<int64_t> d_src_;
     // MAS
     MasDev mas_;
@@ -119,6 +122,11 @@ private:
     // PCG
     DBuf<double> d_x_, d_b_, d_r_, d_p_, d_z_, d_ap_, d_w_, d_tmp_;
     DBuf<float> d_z32_;  // mixed precision: FP32 shadow of z, input of the FP32 residual SpMV
+    DBuf<float2> d_p_df_, d_ap_df_;  // df32 outer SpMV: p and A p as (hi, lo) FP32 pairs
+    DBuf<float> d_r32_, d_w32_;      // mixed precision: r and the preconditioner's residual in FP32
+    bool df32() const { return p_.outer_spmv == 2 || (p_.outer_spmv == 0 && p_.mixed); }
+    void outer_spmv_alpha();  // Ap, p.Ap, alpha with the configured outer SpMV
+    void split_p();           // refresh the df32 split of p (after p = z)
     DBuf<PcgState> d_state_;
     PcgState *h_state_ = nullptr;
     DBuf<double> d_partials_, d_scalar_;

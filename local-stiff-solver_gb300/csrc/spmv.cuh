@@ -37,6 +37,7 @@ __device__ __forceinline__ void bsr_block_row(const int32_t *__restrict__ rows, 
     const VT *__restrict__ v = vals + (int64_t)b * (BD * BD);
 #pragma unroll
     for (int r = 0; r < BD; ++r) y[r] = ACC(0);
+#pragma unroll 2
     for (int32_t l = lane; l < len; l += LANES) {
         const int32_t c = __ldcs(cols + b + l);
         ACC xv[BD];
@@ -66,6 +67,70 @@ __device__ __forceinline__ double bsr_scalar_row(const int32_t *__restrict__ row
         for (int k = 0; k < BD; ++k) acc += (double)v[(int64_t)(comp * BD + k) * len + l] * (double)x[(int64_t)c * BD + k];
     }
     return group_sum<32>(acc);
+}
+
+// ---- double-float (an FP32 pair hi + lo) arithmetic on the FP32 pipe.  The
+// intrinsics keep the compiler from contracting the error-free transforms.
+
+// (sh, sl) += (ah + al) * (xh + xl): TwoProd of the high words (exact product
+// and its rounding error by FMA), TwoSum into sh, the error terms and the two
+// cross products into sl; al * xl (2^-48 relative) is dropped.
+__device__ __forceinline__ void df_fma(float &sh, float &sl, float ah, float al, float xh, float xl)
+{
+    const float p = __fmul_rn(ah, xh);
+    const float e = __fmaf_rn(ah, xh, -p);
+    const float t = __fadd_rn(sh, p);
+    const float z = __fsub_rn(t, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z));
+    sh = t;
+    sl = __fadd_rn(sl, __fadd_rn(err, __fadd_rn(e, __fmaf_rn(ah, xl, __fmul_rn(al, xh)))));
+}
+
+// (ah, al) += (bh, bl)
+__device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl)
+{
+    const float t = __fadd_rn(ah, bh);
+    const float z = __fsub_rn(t, ah);
+    const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(t, z)), __fsub_rn(bh, z));
+    ah = t;
+    al = __fadd_rn(__fadd_rn(al, bl), err);
+}
+
+// Block row i of A x in double-float: values and x as (hi, lo) pairs, one
+// 8-byte load each.  The group reduction runs on the pairs with FP32
+// shuffles; the sums are valid in every lane of the group.
+template <int BD, int LANES>
+__device__ __forceinline__ void bsr_block_row_df(const int32_t *__restrict__ rows, const int32_t *__restrict__ cols,
+                                                 const float2 *__restrict__ vals, int32_t i, bool valid,
+                                                 const float2 *__restrict__ x, int lane, float (&sh)[BD],
+                                                 float (&sl)[BD])
+{
+    const int32_t b = valid ? rows[i] : 0, e = valid ? rows[i + 1] : 0, len = e - b;
+    const float2 *__restrict__ v = vals + (int64_t)b * (BD * BD);
+#pragma unroll
+    for (int r = 0; r < BD; ++r) sh[r] = sl[r] = 0.f;
+#pragma unroll 2
+    for (int32_t l = lane; l < len; l += LANES) {
+        const int32_t c = __ldcs(cols + b + l);
+        float2 xv[BD];
+#pragma unroll
+        for (int k = 0; k < BD; ++k) xv[k] = x[(int64_t)c * BD + k];
+#pragma unroll
+        for (int r = 0; r < BD; ++r)
+#pragma unroll
+            for (int k = 0; k < BD; ++k) {
+                const float2 a = __ldcs(v + (int64_t)(r * BD + k) * len + l);
+                df_fma(sh[r], sl[r], a.x, a.y, xv[k].x, xv[k].y);
+            }
+    }
+#pragma unroll
+    for (int r = 0; r < BD; ++r)
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1) {
+            const float bh = __shfl_xor_sync(0xffffffffu, sh[r], o, LANES);
+            const float bl = __shfl_xor_sync(0xffffffffu, sl[r], o, LANES);
+            df_add(sh[r], sl[r], bh, bl);
+        }
 }
 
 }  // namespace lss

@@ -315,6 +315,7 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
 
 void launch_stiff_to_fp32(int64_t count, const double *src, float *dst, cudaStream_t s)
 {
+    if (count > 0 && (!src || !dst)) fail(LSS_ERR_INTERNAL, "FP32 conversion launched without its arrays");
     if (count == 0) return;
     to_fp32_kernel<<<grid_for(count, 256, 152 * 8), 256, 0, s>>>(count, src, dst);
     LSS_LAUNCH_CHECK();

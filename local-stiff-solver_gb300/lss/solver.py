@@ -36,7 +36,7 @@ EXPORTS = [
     "lss_set_problematic_dofs",
     "lss_solve", "lss_solve_device", "lss_solve_transpose", "lss_grad_A_pattern",
     "lss_grad_A_pattern_device", "lss_grad_params_device", "lss_selected_dofs", "lss_gmm_selection", "lss_subdomains",
-    "lss_partition", "lss_op_row_l1_norms", "lss_op_spmv", "lss_op_mas_apply", "lss_op_precond",
+    "lss_partition", "lss_op_row_l1_norms", "lss_op_spmv", "lss_op_spmv_outer", "lss_op_mas_apply", "lss_op_precond",
     "lss_op_time", "lss_set_memory_cap", "lss_gmm_select_device_noalloc",
 ]
 
@@ -86,6 +86,7 @@ def load(path: str | None = None):
     L.lss_partition.argtypes = [vp, _i32p, C.c_int32, _i32p, C.c_int32, _i32p]
     L.lss_op_row_l1_norms.argtypes = [C.c_int32, C.c_int64, _i32p, _f64p, _f64p]
     L.lss_op_spmv.argtypes = [vp, _f64p, _f64p]
+    L.lss_op_spmv_outer.argtypes = [vp, _f64p, _f64p]
     L.lss_op_mas_apply.argtypes = [vp, _f64p, _f64p]
     L.lss_op_precond.argtypes = [vp, _f64p, _f64p]
     L.lss_op_time.argtypes = [vp, C.c_int32, C.c_int32, _f64p, _f64p]
@@ -285,6 +286,13 @@ class Solver:
         x = np.ascontiguousarray(x, np.float64)
         y = np.empty_like(x)
         self._check(self._L.lss_op_spmv(self._h, _p(x, _f64p), _p(y, _f64p)))
+        return y
+
+    def spmv_outer(self, x):
+        """A x with the PCG's own product (FP64 or double-float, gb300.outer_spmv)."""
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.empty_like(x)
+        self._check(self._L.lss_op_spmv_outer(self._h, _p(x, _f64p), _p(y, _f64p)))
         return y
 
     def mas_apply(self, r):

@@ -118,6 +118,25 @@ def test_spmv_matches_scipy(bs, lanes, elast20, lap):
     assert np.all(np.abs(y - ref) <= 1e-13 * bound + 1e-300)
 
 
+@pytest.mark.parametrize("lanes", [1, 2, 4, 16])
+@pytest.mark.parametrize("outer", ["fp64", "df32"])
+@pytest.mark.parametrize("bs", [1, 3])
+def test_outer_spmv_matches_scipy(bs, outer, lanes, elast20, lap):
+    """The PCG's own A p: FP64, or double-float on the FP32 pipe (values and
+    p split into FP32 high and low words, error-free products and sums).  Both
+    within 1e-13 of |A||x| per entry; the double-float form carries about
+    2^-47 relative error per term, FP64 about 2^-53."""
+    A = elast20[0] if bs == 3 else lap[0]
+    s = _solver({"block_size": bs, "do_hybrid_precond": False}, {"outer_spmv": outer, "spmv_lanes": lanes})
+    s.factorize(A)
+    assert s.get_info()["outer_spmv"] == outer
+    x = np.random.default_rng(3).standard_normal(A.shape[0]) * np.exp(np.random.default_rng(4).standard_normal(A.shape[0]))
+    y = s.spmv_outer(x)
+    ref = A.tocsr() @ x
+    bound = abs(A.tocsr()) @ abs(x)
+    assert np.all(np.abs(y - ref) <= 1e-13 * bound + 1e-300)
+
+
 def _oracle_with_product_partition(A, s, params, **kw):
     from oracle import oracle as O
     perm, offs = s.partition()
@@ -236,17 +255,20 @@ def _check_solution(A, b, x, rtol=1e-8, etol=1e-6):
     return rel, err
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_solve_elasticity_inclusion(precision, elast20):
+@pytest.mark.parametrize("precision,outer", [("fp64", "auto"), ("mixed", "auto"), ("fp64", "df32"),
+                                             ("mixed", "fp64")])
+def test_solve_elasticity_inclusion(precision, outer, elast20):
     A, b = elast20
     s = _solver({"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0,
-                 "min_subdomain_size": 4}, {"precision": precision})
+                 "min_subdomain_size": 4}, {"precision": precision, "outer_spmv": outer})
     s.factorize(A)
     x = s.solve(b)
     _check_solution(A, b, x)
     info = s.get_info()
     assert info["status"] == "converged_rel" and info["num_iterations"] > 0
     assert info["num_stiff_dofs"] > 0 and info["precision"] == precision
+    expect = {"auto": "df32" if precision == "mixed" else "fp64"}.get(outer, outer)
+    assert info["outer_spmv"] == expect
 
 
 def test_solve_reference_matrices(built):

@@ -42,6 +42,8 @@ def test_invalid_parameters_are_rejected_before_device_use(built):
     assert st == 1
     st = L.lss_create(b'{"gb300": {"spmv_lanes": 3}}', C.byref(h))
     assert st == 1 and b"spmv_lanes" in L.lss_last_error(None)
+    st = L.lss_create(b'{"gb300": {"outer_spmv": "fp32"}}', C.byref(h))
+    assert st == 1 and b"outer_spmv" in L.lss_last_error(None)
 
 
 def test_no_device_is_an_error_not_a_fallback(built):
