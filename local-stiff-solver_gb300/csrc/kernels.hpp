@@ -108,6 +108,9 @@ void launch_pcg_update_xr(int64_t n, double *x, double *r, const double *p, cons
 void launch_pcg_update_xr_df(int64_t n, double *x, double *r, const double *p, const float2 *Ap_df, PcgState *st,
                              GridReduce gr, cudaStream_t s, float *r32 = nullptr);
 void launch_df_to_double(int64_t n, const float2 *src, double *dst, cudaStream_t s);
+// the damping estimate's probe, v_i = ((i * 2654435761) mod 2^32) / 2^32 - 0.5 over
+// original indices i, written in the permuted order
+void launch_probe(int64_t nb, int bd, const int32_t *perm, double *dst, cudaStream_t s);
 // p = z + beta p
 // p_df (optional): the df32 split of the new p, the x operand of the df32 SpMV
 void launch_pcg_update_p(int64_t n, double *p, const double *z, const PcgState *st, cudaStream_t s,

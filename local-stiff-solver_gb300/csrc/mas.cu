@@ -99,6 +99,24 @@ __global__ void __launch_bounds__(256) assemble0_kernel(BsrDev A, const int32_t 
 }
 
 template <int BD>
+__device__ __forceinline__ void add_coarse_block(double *base, int32_t ci, int32_t cj, const double (&acc)[BD * BD])
+{
+    constexpr int N = 32 * BD;
+#pragma unroll
+    for (int bi = 0; bi < BD; ++bi)
+#pragma unroll
+        for (int bj = 0; bj < BD; ++bj) {
+            const int row = bi * 32 + (ci & 31), col = bj * 32 + (cj & 31);
+            if (row > col) continue;  // upper triangle only
+            atomicAdd(base + (int64_t)row * N + col, acc[bi * BD + bj]);
+        }
+}
+
+// Galerkin blocks of every coarse level, one thread per block row.  The
+// row's blocks arrive in column order, so neighbours that fall into the same
+// coarse item come in runs: a run is summed in registers and leaves as one
+// set of atomics (at the coarser levels nearly the whole row is one run).
+template <int BD>
 __global__ void __launch_bounds__(256) assemble_coarse_kernel(BsrDev A, MasDev m, const int32_t *__restrict__ cmap,
                                                               double *__restrict__ stage)
 {
@@ -112,50 +130,74 @@ __global__ void __launch_bounds__(256) assemble_coarse_kernel(BsrDev A, MasDev m
         const int32_t ci = map[i];
         const int32_t g = m.boff[l] + (ci >> 5);
         double *base = stage + (int64_t)g * N * N;
+        int32_t cur = -1;
+        double acc[BD * BD];
+#pragma unroll
+        for (int k = 0; k < BD * BD; ++k) acc[k] = 0.0;
         for (int32_t q = 0; q < len; ++q) {
             const int32_t cj = map[A.cols[b + q]];
             if ((cj >> 5) != (ci >> 5)) continue;
+            if (cj != cur) {
+                if (cur >= 0) add_coarse_block<BD>(base, ci, cur, acc);
+                cur = cj;
 #pragma unroll
-            for (int bi = 0; bi < BD; ++bi)
+                for (int k = 0; k < BD * BD; ++k) acc[k] = 0.0;
+            }
 #pragma unroll
-                for (int bj = 0; bj < BD; ++bj) {
-                    const int row = bi * 32 + (ci & 31), col = bj * 32 + (cj & 31);
-                    if (row > col) continue;  // upper triangle only
-                    atomicAdd(base + (int64_t)row * N + col, v[(int64_t)(bi * BD + bj) * len + q]);
-                }
+            for (int k = 0; k < BD * BD; ++k) acc[k] += v[(int64_t)k * len + q];
         }
+        if (cur >= 0) add_coarse_block<BD>(base, ci, cur, acc);
     }
 }
 
 // Symmetric sweep inversion of S (N x N, leading dimension ld, in shared
 // memory): the Gauss-Jordan variant of MASPreconditioner.cu:799-900, which
-// leaves -A^-1 in S.  Flags zero / non-finite pivots.
-__device__ void sweep_invert(double *S, int ld, int N, double *col, double *scol, int *bad)
+// leaves -A^-1 in S.  Only the upper triangle (t <= c) is read and kept:
+// the sweep preserves symmetry, so half the FP64 updates suffice.  The
+// triangle's entries are dealt to the CTA's threads in linear order, so
+// every update instruction runs on full warps (a partly predicated FP64
+// instruction costs the pipe a whole warp).  Flags zero / non-finite pivots.
+// Needs blockDim.x == 256.
+template <int N>
+__device__ void sweep_invert(double *S, int ld, double *col, double *scol, int *bad)
 {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+    constexpr int NE = N * (N + 1) / 2;
+    constexpr int PER = (NE + 255) / 256;
+    const int tid = threadIdx.x;
+    uint32_t tc[PER];  // (t << 16) | c of this thread's entries; ~0u past the end
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int e = tid + k * 256;
+        tc[k] = ~0u;
+        if (e < NE) {
+            int t = 0, off = 0;
+            while (off + (N - t) <= e) {
+                off += N - t;
+                ++t;
+            }
+            tc[k] = ((uint32_t)t << 16) | (uint32_t)(t + (e - off));
+        }
+    }
     for (int p = 0; p < N; ++p) {
         const double piv = S[p * ld + p];
-        for (int t = tid; t < N; t += nt) {
-            const double cv = (t == p) ? 0.0 : S[t * ld + p];
+        for (int t = tid; t < N; t += 256) {
+            const double cv = (t == p) ? 0.0 : (t < p ? S[t * ld + p] : S[p * ld + t]);
             col[t] = cv;
             scol[t] = cv / piv;
         }
         if (tid == 0 && (!isfinite(piv) || piv == 0.0)) atomicOr(bad, 1);
         __syncthreads();
-        for (int t = wid; t < N; t += nw) {
-            if (t == p) continue;
-            const double st = scol[t];
-            for (int c = lane; c < N; c += 32)
-                if (c != p) S[t * ld + c] -= st * col[c];
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            if (tc[k] == ~0u) continue;
+            const int t = (int)(tc[k] >> 16), c = (int)(tc[k] & 0xffffu);
+            if (t != p && c != p) S[t * ld + c] -= scol[t] * col[c];
         }
         __syncthreads();
-        for (int t = tid; t < N; t += nt) {
+        for (int t = tid; t < N; t += 256) {
             if (t == p) S[p * ld + p] = -1.0 / piv;
-            else {
-                S[t * ld + p] = scol[t];
-                S[p * ld + t] = scol[t];
-            }
+            else if (t < p) S[t * ld + p] = scol[t];
+            else S[p * ld + t] = scol[t];
         }
         __syncthreads();
     }
@@ -172,13 +214,13 @@ __global__ void __launch_bounds__(256) mas_invert_kernel(const double *__restric
     const double *src = stage + bank * N * N;
     for (int idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
         const int r = idx / N, c = idx % N;
-        S[r * LD + c] = (r <= c) ? src[(int64_t)r * N + c] : src[(int64_t)c * N + r];
+        if (r <= c) S[r * LD + c] = src[(int64_t)r * N + c];  // the upper triangle is all the sweep uses
     }
     __syncthreads();
     for (int d = threadIdx.x; d < N; d += blockDim.x)
         if (S[d * LD + d] == 0.0) S[d * LD + d] = 1.0;  // padding (MASPreconditioner.cu:779-796)
     __syncthreads();
-    sweep_invert(S, LD, N, col, scol, bad);
+    sweep_invert<N>(S, LD, col, scol, bad);
     // tiles
     T *dst = out + bank * tile_elems<BD>();
     int64_t off = 0;
@@ -187,7 +229,8 @@ __global__ void __launch_bounds__(256) mas_invert_kernel(const double *__restric
             const int nd = (c == c2) ? 17 : 32;
             for (int e = threadIdx.x; e < nd * 32; e += blockDim.x) {
                 const int d = e >> 5, r = e & 31;
-                const double val = -S[(c * 32 + r) * LD + c2 * 32 + ((r + d) & 31)];
+                const int gi = c * 32 + r, gj = c2 * 32 + ((r + d) & 31);
+                const double val = -S[min(gi, gj) * LD + max(gi, gj)];
                 if (!isfinite(val)) atomicOr(bad, 2);
                 dst[off + e] = (T)val;
             }

@@ -501,6 +501,24 @@ void launch_pcg_spmv_alpha_df(const BsrDev &A, const float2 *p_df, float2 *Ap_df
     LSS_LAUNCH_CHECK();
 }
 
+// dst[perm-ordered] = v_i = ((i * 2654435761) mod 2^32) / 2^32 - 0.5 of the
+// original index i (the damping estimate's probe vector)
+__global__ void probe_kernel(int64_t nb, int bd, const int32_t *__restrict__ perm, double *__restrict__ dst)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb * bd;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t h = (uint32_t)((uint64_t)(uint32_t)i * 2654435761u);
+        dst[(int64_t)perm[i / bd] * bd + i % bd] = (double)h / 4294967296.0 - 0.5;
+    }
+}
+
+void launch_probe(int64_t nb, int bd, const int32_t *perm, double *dst, cudaStream_t s)
+{
+    if (nb == 0) return;
+    probe_kernel<<<grid_for(nb * bd, 1024, 152 * 16), 256, 0, s>>>(nb, bd, perm, dst);
+    LSS_LAUNCH_CHECK();
+}
+
 __global__ void df_to_double_kernel(int64_t n, const float2 *__restrict__ src, double *__restrict__ dst)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)

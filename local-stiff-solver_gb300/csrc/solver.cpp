@@ -813,10 +813,7 @@ void HybridSolver::estimate_omega()
     const int64_t n = n_vec();
     const int k = p_.omega_iters;
     // probe vector v_i = ((i * 2654435761) mod 2^32) / 2^32 - 0.5, original ordering
-    std::vector<double> h(n);
-    for (int64_t i = 0; i < n; ++i) h[i] = (double)(uint32_t)((uint64_t)(uint32_t)i * 2654435761u) / 4294967296.0 - 0.5;
-    LSS_CUDA(cudaMemcpyAsync(d_tmp_.data(), h.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_));
-    launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_r_.data(), true, stream_);
+    launch_probe(pat_.nb, pat_.bd, d_perm_.data(), d_r_.data(), stream_);
     PcgState hs{};
     hs.bb = 1.0;
     hs.max_iter = k;
