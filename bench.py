@@ -42,6 +42,14 @@ import numpy as np  # noqa: E402
 
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch over the
+# kernel's algorithmic bytes, from ncu captures of the 60^3-node elasticity case
+# (profiles/spmv_df32_elasticity_650k.md, symv0_mas_level0_elasticity_650k.md,
+# residual32_elasticity_650k.md).  The elasticity workloads' kernels scale in
+# proportion, so traffic = ratio x algorithmic bytes of the timed launch.
+NCU_TRAFFIC_RATIO = {"spmv_outer": 246.24 / 252.39, "mas_level0_symv": 145.10 / 146.79,
+                     "residual_spmv_prec": 133.98 / 132.83}
+
 
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -335,9 +343,13 @@ def main():
              "residual_spmv_prec": kern["residual_spmv_prec"]["ms"]}
     dom = max(share, key=share.get)
     ach = kern[dom]["gbs"]
+    traffic, traffic_src = None, None
+    if args.workload.startswith("elasticity") and dom in NCU_TRAFFIC_RATIO:
+        traffic = kern[dom]["bytes"] * NCU_TRAFFIC_RATIO[dom]
+        traffic_src = "ncu DRAM bytes of the 60^3-node case scaled by algorithmic bytes"
     roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
-            "frac": ach / hbm if ach else None, "traffic": None, "peak_source": pk_src,
-            "per_kernel": kern}
+            "frac": ach / hbm if ach else None, "traffic": traffic, "traffic_source": traffic_src,
+            "peak_source": pk_src, "per_kernel": kern}
 
     # CPU baseline: the oracle's method on the host cores, same partition, bounded sample
     cpu = None

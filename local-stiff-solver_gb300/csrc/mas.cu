@@ -180,10 +180,11 @@ __device__ void sweep_invert(double *S, int ld, double *col, double *scol, int *
     }
     for (int p = 0; p < N; ++p) {
         const double piv = S[p * ld + p];
+        const double rpiv = 1.0 / piv;  // one division per pivot; the column is scaled by multiplication
         for (int t = tid; t < N; t += 256) {
             const double cv = (t == p) ? 0.0 : (t < p ? S[t * ld + p] : S[p * ld + t]);
             col[t] = cv;
-            scol[t] = cv / piv;
+            scol[t] = cv * rpiv;
         }
         if (tid == 0 && (!isfinite(piv) || piv == 0.0)) atomicOr(bad, 1);
         __syncthreads();
@@ -195,7 +196,7 @@ __device__ void sweep_invert(double *S, int ld, double *col, double *scol, int *
         }
         __syncthreads();
         for (int t = tid; t < N; t += 256) {
-            if (t == p) S[p * ld + p] = -1.0 / piv;
+            if (t == p) S[p * ld + p] = -rpiv;
             else if (t < p) S[t * ld + p] = scol[t];
             else S[p * ld + t] = scol[t];
         }
@@ -204,7 +205,7 @@ __device__ void sweep_invert(double *S, int ld, double *col, double *scol, int *
 }
 
 template <int BD, typename T>
-__global__ void __launch_bounds__(256) mas_invert_kernel(const double *__restrict__ stage, T *__restrict__ out,
+__global__ void __launch_bounds__(256, 2) mas_invert_kernel(const double *__restrict__ stage, T *__restrict__ out,
                                                          int *bad)
 {
     constexpr int N = 32 * BD, LD = N + 1;
