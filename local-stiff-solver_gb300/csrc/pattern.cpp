@@ -137,7 +137,7 @@ Pattern analyze_pattern(int32_t n, int64_t nnz, const int32_t *outer, const int3
     }
     const int64_t nnzb = P.rows[nb];
     const int bd2 = bd * bd;
-    if (nnzb * bd2 > (int64_t)0x7fffffff * 4) fail(LSS_ERR_UNSUPPORTED, "matrix too large for this build");
+    if (nnzb * bd2 > (int64_t)0x7fffffff * 4) fail(LSS_ERR_UNSUPPORTED, "matrix too large: more than 2^33 block values");
     P.cols.assign(nnzb, 0);
     P.src.assign(nnzb * bd2, -1);
     std::vector<int> dup(threads, 0);

@@ -1,7 +1,8 @@
 /*
  * lss_oracle.c -- CPU restatement of the reference's GPU hybrid solve path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker, never the product).  Parity status:
+ * TEST INFRASTRUCTURE ONLY (the reference for parity tests, never the
+ * product).  Parity status:
  * UNPINNED -- the reference has no golden vectors for this path and cannot be
  * compiled here; see lss_oracle.h.
  *

@@ -1,9 +1,10 @@
 /*
  * lss_oracle.h -- CPU restatement of the reference's GPU hybrid solve path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: tests, the smoke
- * entry point and the CPU-baseline leg of the benchmark may call it; the
- * product (the CUDA library) never links or calls it.
+ * TEST INFRASTRUCTURE ONLY.  This library is what the GPU path is compared
+ * against: tests, the smoke entry point and the CPU-baseline leg of the
+ * benchmark may call it; the product (the CUDA library) never links or calls
+ * it.
  *
  * Parity status: UNPINNED.  The reference (geometryprocessing/local-stiff-solver)
  * ships no golden vectors or known-answer tests for this path, and its code
