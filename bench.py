@@ -224,7 +224,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="elasticity_3m",
-                    choices=["elasticity_3m", "delaunay_1m", "elasticity_24k", "elasticity_650k"])
+                    choices=["elasticity_3m", "delaunay_1m", "elasticity_24k", "elasticity_650k", "batched"])
+    ap.add_argument("--batch-count", type=int, default=64, help="systems of the batched workload")
+    ap.add_argument("--batch-rhs", type=int, default=16, help="right-hand sides per batched system")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--ref-iters", type=int, default=25, help="PCG iterations per reference-arm step")
     ap.add_argument("--cpu-iters", type=int, default=10, help="PCG iterations of the CPU-baseline sample")
@@ -237,6 +239,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
 
     ws, rank, local = dist_env()
     import torch
@@ -391,6 +395,125 @@ def main():
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
+
+
+BATCH_PARAMS = {"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4,
+                "max_iter": 20000}
+
+
+def run_batched(args):
+    """Many systems of uneven size with several right-hand sides each: all
+    systems factorized and solved at once (lss_factorize_batched_device +
+    lss_solve_batched_device, mixed precision, one host thread and one stream
+    per system) against the same solves one after another in plain FP64.
+    One step = factorize every system (values in HBM) + solve every
+    right-hand side to a true relative residual of 1e-8 (b in HBM)."""
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    import __graft_entry__ as g
+    g.build()
+    import lss
+    from lss import gen
+    dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
+    systems = gen.workload_batched(seed=args.seed + rank, count=args.batch_count, nrhs=args.batch_rhs)
+    gen_s = time.perf_counter() - t0
+    nrhs = args.batch_rhs
+    mats, vals, bs = [], [], []
+    for A, B, info in systems:
+        A = A.tocsc()
+        A.sum_duplicates()
+        mats.append(A)
+        vals.append(torch.tensor(A.data, dtype=torch.float64, device=dev))
+        bs.append(torch.tensor(np.ascontiguousarray(B.T), dtype=torch.float64, device=dev))
+
+    def make(precision):
+        out = []
+        for A in mats:
+            s = lss.Solver.create({"solver": "GPUHybrid", "GPUHybrid": dict(BATCH_PARAMS),
+                                   "gb300": {"precision": precision, "device": local}})
+            s.analyze_pattern(A)
+            s.factorize(A)
+            out.append(s)
+        return out
+
+    s_mixed, s_plain = make("mixed"), make("fp64")
+    xs = [torch.zeros_like(b) for b in bs]
+    vptr = [v.data_ptr() for v in vals]
+    bptr = [b.data_ptr() for b in bs]
+    xptr = [x.data_ptr() for x in xs]
+
+    def batched_step():
+        for x in xs:
+            x.zero_()
+        lss.factorize_batched_device(s_mixed, vptr)
+        return lss.solve_batched_device(s_mixed, bptr, xptr, nrhs)
+
+    def sequential_plain():
+        its = []
+        for si, s in enumerate(s_plain):
+            s.factorize_device(vptr[si])
+            n = mats[si].shape[0]
+            for k in range(nrhs):
+                x = torch.zeros(n, dtype=torch.float64, device=dev)
+                s.solve_device(bs[si][k].data_ptr(), x.data_ptr())
+                its.append(s.get_info()["num_iterations"])
+        return np.array(its)
+
+    for _ in range(args.warmup):
+        batched_step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    l0 = s_mixed[0].get_info()["kernel_launches"]
+    with clocks:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        t1 = time.perf_counter()
+        for _ in range(args.steps):
+            its_m = batched_step()
+        torch.cuda.synchronize()
+        e1.record()
+        e1.synchronize()
+        wall_m = (time.perf_counter() - t1) / args.steps
+    launches = (s_mixed[0].get_info()["kernel_launches"] - l0) / args.steps
+    # accuracy of the batched solves (true residual per system and right-hand side)
+    import scipy.sparse as sp
+    worst = 0.0
+    for si, A in enumerate(mats):
+        X = xs[si].cpu().numpy()
+        B = bs[si].cpu().numpy()
+        R = (A.tocsr() @ X.T) - B.T
+        worst = max(worst, float((np.linalg.norm(R, axis=0) / np.linalg.norm(B.T, axis=0)).max()))
+    sequential_plain()  # warm-up of the plain solvers' graphs
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    its_p = sequential_plain()
+    torch.cuda.synchronize()
+    wall_p = time.perf_counter() - t2
+    nsolve = len(mats) * nrhs
+    dofs = [A.shape[0] for A in mats]
+    line = {
+        "metric": "batched_throughput_solves_per_s", "value": nsolve / wall_m, "unit": "solves/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall_m,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 outer PCG (df32 A p) / f32 MAS", "data": "synthetic (seeded, generated on the host)",
+        "config": {
+            "workload": f"batched_{len(mats)}_elasticity_inclusions_x{nrhs}_rhs",
+            "systems": len(mats), "rhs_per_system": nrhs, "dofs_min": min(dofs), "dofs_max": max(dofs),
+            "dofs_total": int(sum(dofs)), "generate_s": gen_s,
+            "step": "factorize every system (values in HBM) + solve every right-hand side to true rel. residual 1e-8",
+            "sequential_plain_fp64_ms": 1e3 * wall_p, "batched_speedup_vs_sequential_plain": wall_p / wall_m,
+            "iterations_mixed_mean": float(its_m.mean()), "iterations_mixed_max": int(its_m.max()),
+            "iterations_plain_mean": float(its_p.mean()), "iterations_plain_max": int(its_p.max()),
+            "worst_rel_residual_batched": worst,
+            "l2": "inputs larger than L2 (64 systems' matrices and MAS inverses), no flush",
+        },
+        "gpu_launches": int(launches) if launches > 0 else None,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def run_profile(args):

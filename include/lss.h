@@ -190,6 +190,28 @@ lss_status lss_op_time(lss_solver *s, int32_t kind, int32_t reps, double *ms_per
  * exercises the out-of-memory path without exhausting the GPU. */
 lss_status lss_set_memory_cap(size_t bytes);
 
+/* ---- batched solves -------------------------------------------------------- */
+
+/* Solve many independent systems, each with nrhs right-hand sides, at once
+ * (no single counterpart in the reference, which solves one system per call:
+ * this is its GPUHybrid::solve, GPUHybrid.cu:342-399, for every system and
+ * right-hand side).  solvers[s] is a factorized solver of system s (distinct
+ * objects); d_b[s] and d_x[s] are device arrays of n_s x nrhs (column-major,
+ * leading dimension n_s); x is the initial guess on entry, as in lss_solve.
+ * Host threads (threads <= 0: one per system) each drive one system's PCG on
+ * that solver's own stream, so the GPU overlaps the systems; every system and
+ * right-hand side converges on its own scalars and stop flag.
+ * iterations (optional, count x nrhs): iterations per solve.  Returns the
+ * first failing system's status (lss_last_error(NULL) names it); the other
+ * systems still run. */
+lss_status lss_solve_batched_device(lss_solver *const *solvers, int32_t count, const double *const *d_b,
+                                    double *const *d_x, int32_t nrhs, int32_t threads, int32_t *iterations);
+
+/* lss_factorize_device for every system s (values d_values[s], the layout of
+ * that solver's analysed pattern), from the same host-thread pool. */
+lss_status lss_factorize_batched_device(lss_solver *const *solvers, int32_t count, const double *const *d_values,
+                                        int32_t threads);
+
 /* ---- allocation-free entry point ----------------------------------------- */
 
 /* Largest n accepted by lss_gmm_select_device_noalloc. */

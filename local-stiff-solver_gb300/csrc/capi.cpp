@@ -1,8 +1,12 @@
 // extern "C" entry points (include/lss.h).  Every call converts exceptions
 // into status codes and records the message; nothing here exits the process.
+#include <atomic>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "noalloc.hpp"
 #include "solver.hpp"
@@ -18,9 +22,9 @@ size_t &alloc_cap_base()
     static size_t base = 0;
     return base;
 }
-unsigned long long &launch_count()
+std::atomic<unsigned long long> &launch_count()
 {
-    static unsigned long long c = 0;
+    static std::atomic<unsigned long long> c{0};
     return c;
 }
 size_t &alloc_live_bytes()
@@ -346,5 +350,94 @@ lss_status lss_gmm_select_device_noalloc(int32_t n, int64_t nnz, const int32_t *
     return guarded(nullptr, [&]() {
         lss::noalloc_gmm_select(n, nnz, d_outer, d_values, gmm_jump_threshold, gmm_tol, max_gmm_iterations,
                                 d_selected, d_count, (cudaStream_t)stream);
+    });
+}
+
+namespace {
+// Runs work(s) for every system from a pool of host threads (threads <= 0:
+// one per system); returns the first failing system's status.
+template <typename F>
+lss_status for_each_system(lss_solver *const *solvers, int32_t count, int32_t threads, F work)
+{
+    for (int32_t s = 0; s < count; ++s)
+        if (!valid(solvers[s])) {
+            g_create_error = "invalid solver of system " + std::to_string(s);
+            return LSS_ERR_INVALID_ARGUMENT;
+        }
+    // one host thread drives each solver: the systems must be distinct objects
+    for (int32_t s = 0; s < count; ++s)
+        for (int32_t t = s + 1; t < count; ++t)
+            if (solvers[s] == solvers[t]) {
+                g_create_error = "batched systems must be distinct solver objects";
+                return LSS_ERR_INVALID_ARGUMENT;
+            }
+    if (count == 0) return LSS_OK;
+    const int nthreads = threads > 0 ? std::min<int>(threads, count) : count;
+    std::atomic<int32_t> next{0};
+    std::mutex mu;
+    lss_status first = LSS_OK;
+    std::string first_msg;
+    auto worker = [&]() {
+        for (;;) {
+            const int32_t s = next.fetch_add(1);
+            if (s >= count) return;
+            lss_solver *sv = solvers[s];
+            const lss_status st = guarded(sv, [&]() {
+                LSS_CUDA(cudaSetDevice(sv->impl->device()));
+                work(s, sv);
+            });
+            if (st != LSS_OK) {
+                std::lock_guard<std::mutex> lock(mu);
+                if (first == LSS_OK) {
+                    first = st;
+                    first_msg = "system " + std::to_string(s) + ": " + sv->impl->last_error;
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthreads; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &th : pool) th.join();
+    if (first != LSS_OK) g_create_error = first_msg;
+    return first;
+}
+}  // namespace
+
+lss_status lss_factorize_batched_device(lss_solver *const *solvers, int32_t count, const double *const *d_values,
+                                        int32_t threads)
+{
+    if (count < 0 || (count > 0 && (!solvers || !d_values))) {
+        g_create_error = "invalid batched-factorize arguments";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    for (int32_t s = 0; s < count; ++s)
+        if (!d_values[s]) {
+            g_create_error = "null values of system " + std::to_string(s);
+            return LSS_ERR_INVALID_ARGUMENT;
+        }
+    return for_each_system(solvers, count, threads,
+                           [&](int32_t s, lss_solver *sv) { sv->impl->factorize_device(d_values[s], nullptr); });
+}
+
+lss_status lss_solve_batched_device(lss_solver *const *solvers, int32_t count, const double *const *d_b,
+                                    double *const *d_x, int32_t nrhs, int32_t threads, int32_t *iterations)
+{
+    if (count < 0 || nrhs < 0 || (count > 0 && (!solvers || !d_b || !d_x))) {
+        g_create_error = "invalid batched-solve arguments";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    for (int32_t s = 0; s < count && nrhs > 0; ++s)
+        if (!d_b[s] || !d_x[s]) {
+            g_create_error = "null vector of system " + std::to_string(s);
+            return LSS_ERR_INVALID_ARGUMENT;
+        }
+    if (nrhs == 0) return for_each_system(solvers, count, threads, [](int32_t, lss_solver *) {});
+    return for_each_system(solvers, count, threads, [&](int32_t s, lss_solver *sv) {
+        const int64_t n = sv->impl->n();
+        for (int32_t k = 0; k < nrhs; ++k) {
+            sv->impl->solve_device(d_b[s] + k * n, d_x[s] + k * n, nullptr);
+            if (iterations) iterations[(int64_t)s * nrhs + k] = sv->impl->iterations();
+        }
     });
 }

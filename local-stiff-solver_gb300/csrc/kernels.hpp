@@ -71,10 +71,12 @@ void launch_spmv(const BsrDev &A, const double *x, double *y, const int *done, c
 // y = r - A x, FP64 (fp32 == false) or with the FP32 operator copy (fp32 == true)
 void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, double *y, bool fp32,
                           const int *done, cudaStream_t s);
-// y32 = r32 - A x32 entirely in FP32 with the FP32 operator copy (no FP64
-// instruction; the mixed preconditioner's residual)
+// y32 = r32 - A x32 in FP32 with the FP32 operator copy (the mixed
+// preconditioner's residual); block rows flagged in `precise` (optional) are
+// evaluated in double-float from r64, the df32 values and x32 + x_lo.
 void launch_residual32(const BsrDev &A, const float *r32, const float *x32, float *y32, const int *done,
-                       cudaStream_t s);
+                       cudaStream_t s, const uint8_t *precise = nullptr, const double *r64 = nullptr,
+                       const float *x_lo = nullptr);
 
 // ---------------------------------------------------------------- PCG
 enum StopReason : int {
@@ -169,12 +171,13 @@ void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, b
 // z = MAS^-1 xin (acc: z += MAS^-1 xin).  dot_mode 1: st->gamma = rdot.z;
 // dot_mode 2: st->beta = rdot.z / st->gamma, st->gamma = rdot.z.
 // z = scale * MAS^-1 xin, or z += scale * MAS^-1 xin with acc.
-// z32 (optional): also store z rounded to FP32 (the input of the FP32 residual).
+// z32 (optional): also store z rounded to FP32 (the input of the FP32 residual)
+// and, with z_lo, the remainder z - z32 rounded to FP32.
 // xin32 (optional, FP32 MAS only): an FP32 input used in place of xin.
 void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
                       const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
                       int dot_mode, GridReduce gr, const int *done, cudaStream_t s, float *z32 = nullptr,
-                      const float *xin32 = nullptr);
+                      const float *xin32 = nullptr, float *z_lo = nullptr);
 
 // level-0 bank SYMV alone (z = Inv_0 xin + coarse correction already in u), for timing
 void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp32, const double *xin, double *z,
@@ -200,8 +203,9 @@ void launch_stiff_to_fp32(int64_t count, const double *src, float *dst, cudaStre
 void launch_stiff_gather(const BsrDev &A, const StiffDev &S, const double *r, const double *z, bool residual,
                          const int *done, cudaStream_t s);
 // z_S += Inv t
-// z32 (optional): FP32 shadow of z, updated at the DOFs the correction changes
+// z32, z_lo (optional): FP32 shadow of z and its remainder, updated at the
+// DOFs the correction changes
 void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done, cudaStream_t s,
-                        float *z32 = nullptr);
+                        float *z32 = nullptr, float *z_lo = nullptr);
 
 }  // namespace lss

@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -38,8 +40,9 @@ inline void cuda_check(cudaError_t e, const char *what, const char *file, int li
     throw Error(LSS_ERR_CUDA, msg);
 }
 // Kernel launch bookkeeping: launches issued by launcher functions plus the
-// kernel nodes of replayed CUDA graphs (reported by get_info).
-unsigned long long &launch_count();
+// kernel nodes of replayed CUDA graphs (reported by get_info); atomic because
+// batched solves drive several solvers from host threads at once.
+std::atomic<unsigned long long> &launch_count();
 #define LSS_CUDA(call) ::lss::cuda_check((call), #call, __FILE__, __LINE__)
 #define LSS_LAUNCH_CHECK() \
     (::lss::launch_count()++, ::lss::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__))
@@ -164,6 +167,7 @@ struct Params {
     // "gb300" extension
     bool mixed = false;             // FP32 MAS (+ FP32 operator inside the preconditioner)
     int outer_spmv = 0;             // PCG's A p: 0 auto (df32 iff mixed), 1 FP64, 2 df32 (FP32-pipe double-float)
+    int precond_residual = 0;       // mixed r - A z: 0 auto (df32 on stiff rows), 1 FP32, 2 df32 everywhere
     bool multiplicative = true;     // GPUHybrid composition; false = MASSolver additive form
     int max_coarse_levels = 4;      // MAS_MAX_COARSE_LEVEL (MASPreconditioner.hpp:11); <= 6
     double mas_damping = 0.0;       // omega of MAS in the multiplicative form; <= 0: automatic

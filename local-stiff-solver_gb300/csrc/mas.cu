@@ -373,7 +373,8 @@ template <int BD, typename T, bool ACC, int DOT, typename XT>
 __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restrict__ inv0, const T *__restrict__ u,
                                                     const XT *__restrict__ xin, double *__restrict__ z,
                                                     double scale, const double *__restrict__ rdot, PcgState *st,
-                                                    GridReduce gr, const int *done, float *__restrict__ z32)
+                                                    GridReduce gr, const int *done, float *__restrict__ z32,
+                                                    float *__restrict__ z_lo)
 {
     if (done && *done) return;
     const int lane = threadIdx.x & 31;
@@ -399,7 +400,11 @@ __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restric
                 const int64_t e = (int64_t)node * BD + c;
                 if (ACC) val += z[e];
                 z[e] = val;
-                if (z32) z32[e] = (float)val;
+                if (z32) {
+                    const float h = (float)val;
+                    z32[e] = h;
+                    if (z_lo) z_lo[e] = (float)(val - (double)h);
+                }
                 if (DOT) dot[0] += rdot[e] * val;
             }
         }
@@ -421,7 +426,7 @@ __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restric
 template <int BD, typename T, typename XT>
 void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, const XT *xin, double *z,
                      bool acc, double scale, const double *rdot, PcgState *st, int dot_mode, GridReduce gr,
-                     const int *done, cudaStream_t s, float *z32)
+                     const int *done, cudaStream_t s, float *z32, float *z_lo)
 {
     if (m.L > 1) {
         restrict0_kernel<BD, T, XT><<<grid_for((int64_t)m.nparts * 32, 256, 152 * 16), 256, 0, s>>>(m, xin, v, done);
@@ -434,7 +439,7 @@ void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, 
     }
     const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
 #define LSS_S0(A_, D_) \
-    symv0_kernel<BD, T, A_, D_, XT><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32)
+    symv0_kernel<BD, T, A_, D_, XT><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32, z_lo)
     if (dot_mode == 0) {
         if (acc) LSS_S0(true, 0);
         else LSS_S0(false, 0);
@@ -512,7 +517,7 @@ void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp
     GridReduce gr{};
 #define LSS_L0(BD_, T_)                                                                                        \
     symv0_kernel<BD_, T_, false, 0, double><<<grid, 256, 0, s>>>(m, (const T_ *)inv0, (const T_ *)u, xin, z, 1.0,   \
-                                                                 nullptr, nullptr, gr, nullptr, nullptr)
+                                                                 nullptr, nullptr, gr, nullptr, nullptr, nullptr)
     if (fp32) {
         if (m.bd == 1) LSS_L0(1, float);
         else if (m.bd == 2) LSS_L0(2, float);
@@ -528,14 +533,15 @@ void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp
 
 void launch_mas_apply(const MasDev &m, const void *inv0, const void *invc, void *v, void *u, bool fp32,
                       const double *xin, double *z, bool acc, double scale, const double *rdot, PcgState *st,
-                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s, float *z32, const float *xin32)
+                      int dot_mode, GridReduce gr, const int *done, cudaStream_t s, float *z32, const float *xin32,
+                      float *z_lo)
 {
 #define LSS_MAS(BD_, T_)                                                                                          \
     mas_apply_dot_t<BD_, T_, double>(m, (const T_ *)inv0, (const T_ *)invc, (T_ *)v, (T_ *)u, xin, z, acc, scale, \
-                                     rdot, st, dot_mode, gr, done, s, z32)
+                                     rdot, st, dot_mode, gr, done, s, z32, z_lo)
 #define LSS_MAS32(BD_)                                                                                            \
     mas_apply_dot_t<BD_, float, float>(m, (const float *)inv0, (const float *)invc, (float *)v, (float *)u, xin32, \
-                                       z, acc, scale, rdot, st, dot_mode, gr, done, s, z32)
+                                       z, acc, scale, rdot, st, dot_mode, gr, done, s, z32, z_lo)
     if (xin32) {
         if (!fp32) fail(LSS_ERR_INTERNAL, "an FP32 input needs the FP32 MAS");
         if (m.bd == 1) LSS_MAS32(1);

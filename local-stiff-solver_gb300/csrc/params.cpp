@@ -194,6 +194,11 @@ Params parse_params(const char *json, const Params &base)
                 if (v.kind != JValue::Str || (v.str != "fp64" && v.str != "mixed"))
                     fail(LSS_ERR_INVALID_ARGUMENT, "gb300.precision must be \"fp64\" or \"mixed\"");
                 p.mixed = v.str == "mixed";
+            } else if (k == "precond_residual") {
+                if (v.kind != JValue::Str || (v.str != "auto" && v.str != "fp32" && v.str != "df32"))
+                    fail(LSS_ERR_INVALID_ARGUMENT,
+                         "gb300.precond_residual must be \"auto\", \"fp32\" or \"df32\"");
+                p.precond_residual = v.str == "auto" ? 0 : (v.str == "fp32" ? 1 : 2);
             } else if (k == "outer_spmv") {
                 if (v.kind != JValue::Str || (v.str != "auto" && v.str != "fp64" && v.str != "df32"))
                     fail(LSS_ERR_INVALID_ARGUMENT, "gb300.outer_spmv must be \"auto\", \"fp64\" or \"df32\"");

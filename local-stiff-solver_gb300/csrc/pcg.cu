@@ -85,12 +85,20 @@ __global__ void __launch_bounds__(256) residual_kernel(BsrDev A, const VT *__res
     }
 }
 
-// y32 = r32 - A32 x32 entirely in FP32 (the mixed preconditioner's residual:
-// its result feeds the FP32 MAS, and no FP64 instruction is issued)
+// y32 = r - A x for the mixed preconditioner, rounded to FP32 (its result
+// feeds the FP32 MAS).  Rows flagged in `precise` (the stiff rows: there r - A
+// z cancels terms many orders larger than the result -- entries of 1e7 times a
+// nearly rigid z -- which FP32 would turn into noise of the result's size) are
+// evaluated in double-float (values as (hi, lo) pairs, x = x32 + x_lo, r in
+// FP64); all other rows entirely in FP32.  A warp takes the double-float branch
+// for all of its rows when any of them is flagged, so the group shuffles stay
+// warp-uniform.
 template <int BD, int LANES>
 __global__ void __launch_bounds__(256) residual32_kernel(BsrDev A, const float *__restrict__ r32,
                                                          const float *__restrict__ x32, float *__restrict__ y32,
-                                                         const int *done)
+                                                         const uint8_t *__restrict__ precise,
+                                                         const double *__restrict__ r64,
+                                                         const float *__restrict__ x_lo, const int *done)
 {
     if (done && *done) return;
     const int lane = threadIdx.x % LANES;
@@ -100,12 +108,25 @@ __global__ void __launch_bounds__(256) residual32_kernel(BsrDev A, const float *
     for (int64_t wr = w0 * RPW; wr < A.nb; wr += nw * RPW) {
         const int64_t i = wr + (threadIdx.x & 31) / LANES;
         const bool valid = i < A.nb;
-        float acc[BD];
-        bsr_block_row<BD, LANES, float, float, float>(A.rows, A.cols, A.vals32, (int32_t)i, valid, x32, lane, acc);
-        if (valid) {
+        const bool mine = precise && valid && precise[i];
+        if (__any_sync(0xffffffffu, mine)) {
+            float sh[BD], sl[BD];
+            bsr_block_row_df_split<BD, LANES>(A.rows, A.cols, A.vals_df, (int32_t)i, valid, x32, x_lo, lane, sh, sl);
+            if (valid) {
 #pragma unroll
-            for (int k = 0; k < BD; ++k)
-                if (k % LANES == lane) y32[i * BD + k] = r32[i * BD + k] - acc[k];
+                for (int k = 0; k < BD; ++k)
+                    if (k % LANES == lane)
+                        y32[i * BD + k] = (float)(r64[i * BD + k] - ((double)sh[k] + (double)sl[k]));
+            }
+        } else {
+            float acc[BD];
+            bsr_block_row<BD, LANES, float, float, float>(A.rows, A.cols, A.vals32, (int32_t)i, valid, x32, lane,
+                                                          acc);
+            if (valid) {
+#pragma unroll
+                for (int k = 0; k < BD; ++k)
+                    if (k % LANES == lane) y32[i * BD + k] = r32[i * BD + k] - acc[k];
+            }
         }
     }
 }
@@ -436,28 +457,32 @@ void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, dou
 }
 
 template <int BD>
-void residual32_dispatch(const BsrDev &A, const float *r32, const float *x32, float *y32, const int *done,
-                         cudaStream_t s)
+void residual32_dispatch(const BsrDev &A, const float *r32, const float *x32, float *y32, const uint8_t *precise,
+                         const double *r64, const float *x_lo, const int *done, cudaStream_t s)
 {
     const int grid = grid_for((int64_t)A.nb * A.lanes32, 256, 152 * 16);
+#define LSS_R32(L_) residual32_kernel<BD, L_><<<grid, 256, 0, s>>>(A, r32, x32, y32, precise, r64, x_lo, done)
     switch (A.lanes32) {
-    case 1: residual32_kernel<BD, 1><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
-    case 2: residual32_kernel<BD, 2><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
-    case 4: residual32_kernel<BD, 4><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
-    case 8: residual32_kernel<BD, 8><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
-    case 16: residual32_kernel<BD, 16><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
-    default: residual32_kernel<BD, 32><<<grid, 256, 0, s>>>(A, r32, x32, y32, done); break;
+    case 1: LSS_R32(1); break;
+    case 2: LSS_R32(2); break;
+    case 4: LSS_R32(4); break;
+    case 8: LSS_R32(8); break;
+    case 16: LSS_R32(16); break;
+    default: LSS_R32(32); break;
     }
+#undef LSS_R32
 }
 
 void launch_residual32(const BsrDev &A, const float *r32, const float *x32, float *y32, const int *done,
-                       cudaStream_t s)
+                       cudaStream_t s, const uint8_t *precise, const double *r64, const float *x_lo)
 {
     if (A.nb > 0 && (!A.vals32 || !r32 || !x32 || !y32))
         fail(LSS_ERR_INTERNAL, "FP32 residual SpMV launched without its operand arrays");
-    if (A.bd == 1) residual32_dispatch<1>(A, r32, x32, y32, done, s);
-    else if (A.bd == 2) residual32_dispatch<2>(A, r32, x32, y32, done, s);
-    else residual32_dispatch<3>(A, r32, x32, y32, done, s);
+    if (precise && (!A.vals_df || !r64 || !x_lo))
+        fail(LSS_ERR_INTERNAL, "double-float rows of the FP32 residual need their operand arrays");
+    if (A.bd == 1) residual32_dispatch<1>(A, r32, x32, y32, precise, r64, x_lo, done, s);
+    else if (A.bd == 2) residual32_dispatch<2>(A, r32, x32, y32, precise, r64, x_lo, done, s);
+    else residual32_dispatch<3>(A, r32, x32, y32, precise, r64, x_lo, done, s);
     LSS_LAUNCH_CHECK();
 }
 

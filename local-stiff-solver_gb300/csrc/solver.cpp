@@ -86,7 +86,8 @@ void HybridSolver::set_parameters(const char *json)
                                  np.cond_threshold != p_.cond_threshold || np.decompose != p_.decompose ||
                                  np.min_sub != p_.min_sub || np.max_sub != p_.max_sub || np.expand != p_.expand ||
                                  np.float_subdomains != p_.float_subdomains ||
-                                 np.multiplicative != p_.multiplicative || np.outer_spmv != p_.outer_spmv;
+                                 np.multiplicative != p_.multiplicative || np.outer_spmv != p_.outer_spmv ||
+                                 np.precond_residual != p_.precond_residual;
     p_ = np;
     if (pattern_affecting) have_pattern_ = false;
     if (value_affecting) factorized_ = false;
@@ -120,7 +121,7 @@ std::string HybridSolver::info_json() const
     o << ", \"outer_spmv\": \"" << (df32() ? "df32" : "fp64") << "\"";
     o << ", \"composition\": \"" << (p_.multiplicative ? "multiplicative" : "additive") << "\"";
     o << ", \"mas_omega\": " << omega_;
-    o << ", \"kernel_launches\": " << launch_count();
+    o << ", \"kernel_launches\": " << launch_count().load();
     int64_t nstiff = 0;
     for (const auto &s : subs_) nstiff += (int64_t)s.size();
     o << ", \"num_stiff_dofs\": " << nstiff << ", \"num_subdomains\": " << subs_.size();
@@ -277,7 +278,7 @@ void HybridSolver::factorize_common()
     d_bad_.zero(stream_);
     launch_check_finite(nnz, d_csc_.data(), d_bad_.data(), stream_);
     mas_fp32_ = p_.mixed;
-    const bool df = df32();
+    const bool df = need_vals_df();
     if (p_.mixed) d_vals32_.resize(pat_.src.size());
     else d_vals32_.release();
     if (df) d_vals_df_.resize(pat_.src.size());
@@ -303,6 +304,7 @@ void HybridSolver::factorize_common()
     setup_mas();
     LSS_CUDA(cudaStreamSynchronize(stream_));
     stats_["time_mas_setup"] = secs(t4);
+    setup_precise_rows();
     ensure_vectors();
     d_csc_.release();
     factorized_ = true;
@@ -460,6 +462,41 @@ void HybridSolver::setup_stiff()
     stats_["max_subdomain_dofs"] = (double)maxm;
 }
 
+// Mixed precision: the block rows whose preconditioner residual runs in
+// double-float -- every block row holding a DOF of the GMM selection or of a
+// stiff subdomain ("auto"), all rows ("df32") or none ("fp32").
+void HybridSolver::setup_precise_rows()
+{
+    precise_rows_ = false;
+    if (!p_.mixed || p_.precond_residual == 1) {
+        d_precise_.release();
+        return;
+    }
+    const int32_t nb = pat_.nb, bd = pat_.bd;
+    std::vector<uint8_t> flag(nb, p_.precond_residual == 2 ? 1 : 0);
+    int64_t count = p_.precond_residual == 2 ? nb : 0;
+    auto mark = [&](int32_t dof) {
+        if (dof < 0 || dof >= pat_.n) return;
+        uint8_t &f = flag[pat_.part.perm[dof / bd]];
+        if (!f) {
+            f = 1;
+            ++count;
+        }
+    };
+    if (p_.precond_residual == 0) {
+        for (int32_t d : gmm_sel_) mark(d);
+        for (const auto &s : subs_)
+            for (int32_t d : s) mark(d);
+    }
+    stats_["precise_residual_block_rows"] = (double)count;
+    if (count == 0) {
+        d_precise_.release();
+        return;
+    }
+    d_precise_.upload(flag, stream_);
+    precise_rows_ = true;
+}
+
 void HybridSolver::setup_mas()
 {
     const int bd = pat_.bd, N = 32 * bd;
@@ -499,9 +536,13 @@ void HybridSolver::ensure_vectors()
 {
     const int64_t n = n_vec();
     for (DBuf<double> *b : {&d_x_, &d_b_, &d_r_, &d_p_, &d_z_, &d_ap_, &d_w_, &d_tmp_}) b->resize(n);
-    for (DBuf<float> *b : {&d_z32_, &d_r32_, &d_w32_}) {
-        if (p_.mixed) b->resize(n);
-        else b->release();
+    for (DBuf<float> *b : {&d_z32_, &d_r32_, &d_w32_, &d_z_lo_}) {
+        if (p_.mixed) {
+            b->resize(n);
+            b->zero(stream_);
+        } else {
+            b->release();
+        }
     }
     for (DBuf<float2> *b : {&d_p_df_, &d_ap_df_}) {
         if (df32()) b->resize(n);
@@ -512,10 +553,10 @@ void HybridSolver::ensure_vectors()
 // ------------------------------------------------------------------ preconditioner
 
 void HybridSolver::mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale,
-                             float *z32, const float *xin32)
+                             float *z32, const float *xin32, float *z_lo)
 {
     launch_mas_apply(mas_, d_inv0_.data(), d_invc_.data(), d_v_.data(), d_u_.data(), mas_fp32_, xin, z, acc, scale,
-                     rdot, d_state_.data(), dot_mode, gr_, &d_state_.data()->done, stream_, z32, xin32);
+                     rdot, d_state_.data(), dot_mode, gr_, &d_state_.data()->done, stream_, z32, xin32, z_lo);
 }
 
 void HybridSolver::rz_dot(const double *r, const double *z, int dot_mode)
@@ -561,10 +602,12 @@ void HybridSolver::precond(const double *r, double *z, int dot_mode, const float
         r32 = d_r32_.data();
     }
     float *z32 = d_z32_.data();
-    mas_apply(r, z, false, nullptr, 0, omega_, z32);
+    float *z_lo = precise_rows_ ? d_z_lo_.data() : nullptr;
+    mas_apply(r, z, false, nullptr, 0, omega_, z32, nullptr, z_lo);
     launch_stiff_gather(A_, stiff_, r, z, true, done, stream_);
-    launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_, z32);
-    launch_residual32(A_, r32, z32, d_w32_.data(), done, stream_);
+    launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_, z32, z_lo);
+    launch_residual32(A_, r32, z32, d_w32_.data(), done, stream_, precise_rows_ ? d_precise_.data() : nullptr, r,
+                      z_lo);
     mas_apply(nullptr, z, true, r, dot_mode, omega_, nullptr, d_w32_.data());
 }
 
@@ -620,7 +663,7 @@ void HybridSolver::launch_chunk(int iters)
         if (cudaGraphGetNodes(g, nullptr, &nodes) == cudaSuccess) stats_["kernels_per_iteration"] = (double)nodes / iters;
         graph_nodes_ = nodes;
         // the capture ran the launchers once without executing anything
-        launch_count() -= (unsigned long long)std::min<size_t>(launch_count(), nodes);
+        launch_count() -= std::min<unsigned long long>(launch_count().load(), nodes);
         LSS_CUDA(cudaGraphInstantiate(&graph_exec_, g, 0));
         cudaGraphDestroy(g);
         graph_iters_ = iters;
@@ -755,7 +798,9 @@ void HybridSolver::autotune_spmv()
                                          })
                                        : time_it([&]() {
                                              launch_residual32(T, d_r32_.data(), d_z32_.data(), d_w32_.data(),
-                                                               nullptr, stream_);
+                                                               nullptr, stream_,
+                                                               precise_rows_ ? d_precise_.data() : nullptr,
+                                                               d_r_.data(), d_z_lo_.data());
                                          });
             log += (pass ? " f32:" : (df32() ? " df32:" : " f64:")) + std::to_string(l) + "=" + std::to_string(ms / 5);
             if (ms < best) { best = ms; best_l = l; }
@@ -1019,7 +1064,9 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
         case 4: launch_mas_level0(mas_, d_inv0_.data(), d_u_.data(), mas_fp32_, d_r_.data(), d_z_.data(), stream_);
             break;
         case 5:
-            if (p_.mixed) launch_residual32(A_, d_r32_.data(), d_z32_.data(), d_w32_.data(), nullptr, stream_);
+            if (p_.mixed)
+                launch_residual32(A_, d_r32_.data(), d_z32_.data(), d_w32_.data(), nullptr, stream_,
+                                  precise_rows_ ? d_precise_.data() : nullptr, d_r_.data(), d_z_lo_.data());
             else launch_residual_spmv(A_, d_r_.data(), d_p_.data(), d_ap_.data(), false, nullptr, stream_);
             break;
         case 6: outer_spmv_alpha(); break;

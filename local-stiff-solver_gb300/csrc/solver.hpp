@@ -49,6 +49,8 @@ public:
     const Pattern &pattern() const { return pat_; }
     bool factorized() const { return factorized_; }
     int32_t n() const { return pat_.n; }
+    int device() const { return p_.device; }
+    int iterations() const { return num_iterations_; }
 
     std::string last_error;
 
@@ -76,7 +78,7 @@ private:
     // r32 (optional): r already rounded to FP32 (mixed precision); converted here otherwise
     void precond(const double *r, double *z, int dot_mode, const float *r32 = nullptr);
     void mas_apply(const double *xin, double *z, bool acc, const double *rdot, int dot_mode, double scale,
-                   float *z32 = nullptr, const float *xin32 = nullptr);
+                   float *z32 = nullptr, const float *xin32 = nullptr, float *z_lo = nullptr);
     void estimate_omega();
     void autotune_spmv();
     void iteration();
@@ -124,6 +126,11 @@ private:
     DBuf<float> d_z32_;  // mixed precision: FP32 shadow of z, input of the FP32 residual SpMV
     DBuf<float2> d_p_df_, d_ap_df_;  // df32 outer SpMV: p and A p as (hi, lo) FP32 pairs
     DBuf<float> d_r32_, d_w32_;      // mixed precision: r and the preconditioner's residual in FP32
+    DBuf<float> d_z_lo_;             // mixed precision: z - z32 rounded to FP32 (double-float residual rows)
+    DBuf<uint8_t> d_precise_;        // mixed precision: block rows whose residual runs in double-float
+    bool precise_rows_ = false;
+    bool need_vals_df() const { return df32() || (p_.mixed && p_.precond_residual != 1); }
+    void setup_precise_rows();
     bool df32() const { return p_.outer_spmv == 2 || (p_.outer_spmv == 0 && p_.mixed); }
     void outer_spmv_alpha();  // Ap, p.Ap, alpha with the configured outer SpMV
     void split_p();           // refresh the df32 split of p (after p = z)

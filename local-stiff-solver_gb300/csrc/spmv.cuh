@@ -133,4 +133,42 @@ __device__ __forceinline__ void bsr_block_row_df(const int32_t *__restrict__ row
         }
 }
 
+// bsr_block_row_df with x given as separate high and low FP32 arrays
+template <int BD, int LANES>
+__device__ __forceinline__ void bsr_block_row_df_split(const int32_t *__restrict__ rows,
+                                                       const int32_t *__restrict__ cols,
+                                                       const float2 *__restrict__ vals, int32_t i, bool valid,
+                                                       const float *__restrict__ xh, const float *__restrict__ xl,
+                                                       int lane, float (&sh)[BD], float (&sl)[BD])
+{
+    const int32_t b = valid ? rows[i] : 0, e = valid ? rows[i + 1] : 0, len = e - b;
+    const float2 *__restrict__ v = vals + (int64_t)b * (BD * BD);
+#pragma unroll
+    for (int r = 0; r < BD; ++r) sh[r] = sl[r] = 0.f;
+    for (int32_t l = lane; l < len; l += LANES) {
+        const int32_t c = __ldcs(cols + b + l);
+        float x1[BD], x2[BD];
+#pragma unroll
+        for (int k = 0; k < BD; ++k) {
+            x1[k] = xh[(int64_t)c * BD + k];
+            x2[k] = xl[(int64_t)c * BD + k];
+        }
+#pragma unroll
+        for (int r = 0; r < BD; ++r)
+#pragma unroll
+            for (int k = 0; k < BD; ++k) {
+                const float2 a = __ldcs(v + (int64_t)(r * BD + k) * len + l);
+                df_fma(sh[r], sl[r], a.x, a.y, x1[k], x2[k]);
+            }
+    }
+#pragma unroll
+    for (int r = 0; r < BD; ++r)
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1) {
+            const float bh = __shfl_xor_sync(0xffffffffu, sh[r], o, LANES);
+            const float bl = __shfl_xor_sync(0xffffffffu, sl[r], o, LANES);
+            df_add(sh[r], sl[r], bh, bl);
+        }
+}
+
 }  // namespace lss

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) gather_kernel(BsrDev A, StiffDev S, const
 
 template <typename VT>
 __global__ void __launch_bounds__(256) apply_kernel(StiffDev S, const VT *__restrict__ inv, double *__restrict__ z,
-                                                    float *__restrict__ z32, const int *done)
+                                                    float *__restrict__ z32, float *__restrict__ z_lo, const int *done)
 {
     if (done && *done) return;
     const int lane = threadIdx.x & 31;
@@ -237,7 +237,11 @@ __global__ void __launch_bounds__(256) apply_kernel(StiffDev S, const VT *__rest
         const int32_t d = S.dofs[j];
         const double nz = z[d] + acc;
         z[d] = nz;
-        if (z32) z32[d] = (float)nz;
+        if (z32) {
+            const float h = (float)nz;
+            z32[d] = h;
+            if (z_lo) z_lo[d] = (float)(nz - (double)h);
+        }
     }
 }
 
@@ -334,12 +338,13 @@ void launch_stiff_gather(const BsrDev &A, const StiffDev &S, const double *r, co
     LSS_LAUNCH_CHECK();
 }
 
-void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done, cudaStream_t s, float *z32)
+void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done, cudaStream_t s, float *z32,
+                        float *z_lo)
 {
     if (S.ndof == 0) return;
     const int grid = (int)(((int64_t)S.ndof * 32 + 255) / 256);
-    if (fp32) apply_kernel<float><<<grid, 256, 0, s>>>(S, S.inv32, z, z32, done);
-    else apply_kernel<double><<<grid, 256, 0, s>>>(S, S.inv, z, z32, done);
+    if (fp32) apply_kernel<float><<<grid, 256, 0, s>>>(S, S.inv32, z, z32, z_lo, done);
+    else apply_kernel<double><<<grid, 256, 0, s>>>(S, S.inv, z, z32, z_lo, done);
     LSS_LAUNCH_CHECK();
 }
 

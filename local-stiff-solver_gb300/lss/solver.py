@@ -37,7 +37,8 @@ EXPORTS = [
     "lss_solve", "lss_solve_device", "lss_solve_transpose", "lss_grad_A_pattern",
     "lss_grad_A_pattern_device", "lss_grad_params_device", "lss_selected_dofs", "lss_gmm_selection", "lss_subdomains",
     "lss_partition", "lss_op_row_l1_norms", "lss_op_spmv", "lss_op_spmv_outer", "lss_op_mas_apply", "lss_op_precond",
-    "lss_op_time", "lss_set_memory_cap", "lss_gmm_select_device_noalloc",
+    "lss_op_time", "lss_set_memory_cap", "lss_gmm_select_device_noalloc", "lss_solve_batched_device",
+    "lss_factorize_batched_device",
 ]
 
 
@@ -91,6 +92,9 @@ def load(path: str | None = None):
     L.lss_op_precond.argtypes = [vp, _f64p, _f64p]
     L.lss_op_time.argtypes = [vp, C.c_int32, C.c_int32, _f64p, _f64p]
     L.lss_set_memory_cap.argtypes = [C.c_size_t]
+    L.lss_solve_batched_device.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(vp), C.POINTER(vp), C.c_int32,
+                                           C.c_int32, _i32p]
+    L.lss_factorize_batched_device.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(vp), C.c_int32]
     L.lss_gmm_select_device_noalloc.argtypes = [C.c_int32, C.c_int64, vp, vp, C.c_double, C.c_double, C.c_int32,
                                                 vp, vp, vp]
     for name in EXPORTS:
@@ -131,6 +135,40 @@ def row_l1_norms(A):
     if st:
         raise LssError(st, L.lss_last_error(None).decode())
     return out
+
+
+def solve_batched_device(solvers, d_b, d_x, nrhs: int, threads: int = 0) -> np.ndarray:
+    """Solve every system s (a factorized Solver) for nrhs right-hand sides at
+    once: d_b[s], d_x[s] are device pointers (ints) to n_s x nrhs column-major
+    arrays; x is the initial guess on entry.  One host thread per system
+    (threads <= 0) drives that solver's PCG on its own stream, so the GPU
+    overlaps the systems.  Returns the iteration counts, shape (count, nrhs)."""
+    L = load()
+    count = len(solvers)
+    if len(d_b) != count or len(d_x) != count:
+        raise ValueError("one b and one x pointer per system")
+    S = (C.c_void_p * max(count, 1))(*[s._h.value for s in solvers])
+    B = (C.c_void_p * max(count, 1))(*[int(p) for p in d_b])
+    X = (C.c_void_p * max(count, 1))(*[int(p) for p in d_x])
+    its = np.zeros(max(count * nrhs, 1), np.int32)
+    st = L.lss_solve_batched_device(S, count, B, X, nrhs, threads, _p(its, _i32p))
+    if st:
+        raise LssError(st, L.lss_last_error(None).decode())
+    return its[:count * nrhs].reshape(count, nrhs)
+
+
+def factorize_batched_device(solvers, d_values, threads: int = 0) -> None:
+    """factorize_device of every system at once (d_values[s]: device pointer to
+    system s's values in its analysed pattern's CSC order)."""
+    L = load()
+    count = len(solvers)
+    if len(d_values) != count:
+        raise ValueError("one values pointer per system")
+    S = (C.c_void_p * max(count, 1))(*[s._h.value for s in solvers])
+    V = (C.c_void_p * max(count, 1))(*[int(p) for p in d_values])
+    st = L.lss_factorize_batched_device(S, count, V, threads)
+    if st:
+        raise LssError(st, L.lss_last_error(None).decode())
 
 
 class Solver:
