@@ -732,9 +732,17 @@ void HybridSolver::run_pcg()
         const bool improving = res2 < 0.25 * prev_res2;
         prev_res2 = res2;
         if (converged && !true_ok && improving && attempt < p_.max_refinements && launched < p_.max_iter) {
-            // the recurrence residual drifted from the true one: restart from x
+            // the recurrence residual drifted from the true one: restart from x,
+            // aiming the recurrence below the tolerance by the drift seen so far
+            // (at least 2x), so that the restarted solve's own drift still lands
+            // the true residual under it
             ++refinements_;
             h_state_->done = STOP_RUNNING;
+            if (hs.rel_eps > 0 && !(res2 / bb <= hs.rel_eps)) {
+                const double true_rel = std::sqrt(res2 / bb);
+                const double target = p_.rel_tol * std::min(1.0, 0.5 * p_.rel_tol / true_rel);
+                h_state_->rel_eps = target * target;
+            }
             LSS_CUDA(cudaMemcpyAsync(d_state_.data(), h_state_, sizeof(PcgState), cudaMemcpyHostToDevice, stream_));
             continue;
         }
