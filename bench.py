@@ -224,7 +224,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="elasticity_3m",
-                    choices=["elasticity_3m", "delaunay_1m", "elasticity_24k", "elasticity_650k", "batched"])
+                    choices=["elasticity_3m", "delaunay_1m", "elasticity_24k", "elasticity_650k", "batched",
+                             "adjoint_500k"])
     ap.add_argument("--batch-count", type=int, default=64, help="systems of the batched workload")
     ap.add_argument("--batch-rhs", type=int, default=16, help="right-hand sides per batched system")
     ap.add_argument("--seed", type=int, default=0)
@@ -241,6 +242,8 @@ def main():
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "adjoint_500k":
+        return run_adjoint(args)
 
     ws, rank, local = dist_env()
     import torch
@@ -510,6 +513,132 @@ def run_batched(args):
             "l2": "inputs larger than L2 (64 systems' matrices and MAS inverses), no flush",
         },
         "gpu_launches": int(launches) if launches > 0 else None,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_adjoint(args):
+    """Differentiation workload: x = A(theta)^-1 b on the 55^3-node Kuhn-tet cube
+    (499,125 DOFs), theta_e = exp(z_e), z ~ N(0, 1), a seeded sphere of tets
+    x1e5; L = 1/2 ||x - x*||^2.  One step = forward (assemble the values on the
+    GPU, factorize, solve to 1e-8) + backward (adjoint solve with the same
+    factorization, fused parameter-gradient kernel), through the
+    torch.autograd.Function.  The gradient is checked against finite
+    differences of the solver's own loss (tolerance 1e-12) on 20 random
+    relative directions with the five-point stencil."""
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    import __graft_entry__ as g
+    g.build()
+    from lss import gen
+    from lss import autograd as AG
+    dev = torch.device("cuda", local)
+    nodes = 55
+    t0 = time.perf_counter()
+    pattern, M, c = gen.elasticity_parametric(nodes)
+    gen_s = time.perf_counter() - t0
+    rng = np.random.Generator(np.random.PCG64(args.seed + rank))
+    ntet = M.shape[1]
+    theta = np.exp(rng.standard_normal(ntet))
+    cen = gen.tet_centroids(nodes, nodes, nodes)
+    centre = rng.uniform(0.3, 0.7, 3)
+    inside = ((cen - centre) ** 2).sum(1) < 0.2 ** 2
+    theta[inside] *= 1e5
+    n = pattern.shape[0]
+    b = rng.standard_normal(n)
+    xstar = rng.standard_normal(n)
+    base = {"block_size": 3, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4}
+
+    def log(msg):
+        print(f"[adjoint {time.perf_counter() - t0:7.1f}s] {msg}", file=sys.stderr, flush=True)
+
+    log(f"generated {n} DOFs, {ntet} parameters in {gen_s:.1f}s")
+
+    def system(tol, precision, max_iter):
+        p = {"solver": "GPUHybrid", "GPUHybrid": dict(base, relative_tolerance=tol, max_iter=max_iter),
+             "gb300": {"precision": precision, "device": local, "max_refinements": 2}}
+        return AG.LinearSystem(pattern, M, c, p, device=dev)
+
+    sysm = system(1e-8, "mixed", 20000)
+    bt = torch.tensor(b, dtype=torch.float64, device=dev)
+    xs = torch.tensor(xstar, dtype=torch.float64, device=dev)
+
+    def step(sys_):
+        th = torch.tensor(theta, dtype=torch.float64, device=dev, requires_grad=True)
+        x = AG.solve(th, bt, sys_)
+        L = 0.5 * ((x - xs) ** 2).sum()
+        L.backward()
+        return th.grad
+
+    for _ in range(args.warmup):
+        step(sysm)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    with clocks:
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        fwd = []
+        e0.record()
+        for _ in range(args.steps):
+            step(sysm)
+        e1.record()
+        e1.synchronize()
+        step_ms = e0.elapsed_time(e1) / args.steps
+        for _ in range(args.steps):
+            th = torch.tensor(theta, dtype=torch.float64, device=dev)
+            e0.record()
+            with torch.no_grad():
+                AG.solve(th, bt, sysm)
+            e2.record()
+            e2.synchronize()
+            fwd.append(e0.elapsed_time(e2))
+    info = sysm.solver.get_info()
+    fwd_ms = statistics.mean(fwd)
+    log(f"step {step_ms:.1f} ms, forward {fwd_ms:.1f} ms, {info['num_iterations']} iterations")
+    # finite-difference check of the gradient (tight tolerance: the loss carries
+    # solve noise of about cond(A) * tol relative), within a wall-clock budget
+    syst = system(1e-11, "mixed", 4000)
+    gt = step(syst).cpu().numpy()
+    log(f"tight gradient: {syst.solver.get_info()['num_iterations']} iterations, "
+        f"status {syst.solver.get_info()['status']}, rel. residual {syst.solver.get_info()['relative_residual']:.2e}")
+
+    def loss(t):
+        with torch.no_grad():
+            xx = AG.solve(torch.tensor(t, dtype=torch.float64, device=dev), bt, syst)
+            return 0.5 * float(((xx - xs) ** 2).sum())
+
+    drng = np.random.Generator(np.random.PCG64(7))
+    h = 1e-2
+    errs = []
+    t_fd = time.perf_counter()
+    for _ in range(20):
+        if time.perf_counter() - t_fd > 240.0:
+            break
+        d = drng.standard_normal(ntet) * theta
+        fd = (-loss(theta + 2 * h * d) + 8 * loss(theta + h * d) - 8 * loss(theta - h * d)
+              + loss(theta - 2 * h * d)) / (12 * h)
+        an = float(gt @ d)
+        errs.append(abs(fd - an) / max(abs(an), 1e-300))
+        log(f"direction {len(errs)}: rel. err {errs[-1]:.2e}")
+    # the production (mixed, 1e-8) gradient against the tight one
+    gm = step(sysm).cpu().numpy()
+    line = {
+        "metric": "adjoint_step_ms", "value": step_ms, "unit": "ms", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 outer PCG (df32 A p) / f32 MAS", "data": "synthetic (seeded)",
+        "config": {
+            "workload": "elasticity_55^3_nodes_lognormal_theta_inclusion_1e5", "n": int(n),
+            "nnz": int(pattern.nnz), "parameters": int(ntet), "generate_s": gen_s,
+            "step": "forward (GPU assembly + factorize + solve to 1e-8) + backward (adjoint solve + dL/dtheta)",
+            "forward_ms": fwd_ms, "backward_ms": step_ms - fwd_ms,
+            "iterations_forward": info["num_iterations"],
+            "fd_check": {"directions": len(errs), "stencil": "5-point, relative step 1e-2",
+                         "solver": "mixed, relative tolerance 1e-11",
+                         "worst_rel_err": max(errs), "median_rel_err": float(np.median(errs))},
+            "mixed_1e-8_gradient_rel_err_vs_tight": float(np.linalg.norm(gm - gt) / np.linalg.norm(gt)),
+        },
         "clocks": clocks.summary(),
     }
     if rank == 0:
