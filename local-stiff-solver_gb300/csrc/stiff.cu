@@ -107,26 +107,40 @@ __global__ void __launch_bounds__(256) invert_small_kernel(const int32_t *__rest
 //   P = S[:,K] D^-1 (D = S[K,K]);  S[I,J] -= P[I] S[K,J]  (I, J outside K);
 //   S[I,K] = P[I];  S[K,J] = P[J]^T;  S[K,K] = -D^-1.
 // After every block has been swept S holds -A^-1.  Four launches per block of
-// SW_T pivots; the trailing update is a tiled FP64 rank-SW_T product.
+// SW_T pivots; the trailing update is a tiled rank-SW_T product.
 constexpr int SW_T = 32;
 
-__global__ void symmetrize_kernel(double *__restrict__ S, int m)
+// ---- large subdomains in double-float: the working matrix W holds (hi, lo)
+// FP32 pairs in place of the FP64 entries (same 8 bytes), only its upper
+// triangle is kept (the sweep preserves symmetry), and the m^3 / 2 trailing
+// updates run error-free products and compensated sums on the FP32 pipe (GB300
+// issues 2 DFMA/clk/SM against 128 FP32 FMA).  The pivot blocks (32 x 32) and
+// the panels (32 m^2 in total) stay in FP64.
+
+__device__ __forceinline__ float2 df_split(double v)
 {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)m * m) return;
-    const int r = (int)(idx / m), c = (int)(idx % m);
-    if (r > c) S[idx] = S[(int64_t)c * m + r];
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double df_value(float2 w) { return (double)w.x + (double)w.y; }
+
+// in place, elementwise: the FP64 entry becomes its (hi, lo) pair
+__global__ void to_df_kernel(double *__restrict__ S, int64_t count)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        reinterpret_cast<float2 *>(S)[i] = df_split(S[i]);
 }
 
-// D^-1 of the pivot block by the scalar sweep in shared memory (one CTA)
-__global__ void __launch_bounds__(256) blk_diag_kernel(const double *__restrict__ S, int m, int k0, int t,
-                                                       double *__restrict__ Dinv, int *bad)
+// D^-1 of the pivot block (upper triangle of W[K][K]) by the FP64 scalar sweep
+__global__ void __launch_bounds__(256) blk_diag_df_kernel(const float2 *__restrict__ W, int m, int k0, int t,
+                                                          double *__restrict__ Dinv, int *bad)
 {
     __shared__ double D[SW_T * (SW_T + 1)], col[SW_T], scol[SW_T];
     const int ld = SW_T + 1;
     for (int e = threadIdx.x; e < t * t; e += blockDim.x) {
         const int r = e / t, c = e % t;
-        D[r * ld + c] = S[(int64_t)(k0 + r) * m + k0 + c];
+        const int a = min(r, c), b = max(r, c);
+        D[r * ld + c] = df_value(W[(int64_t)(k0 + a) * m + k0 + b]);
     }
     __syncthreads();
     sweep_invert_small(D, ld, t, col, scol, bad);
@@ -136,70 +150,115 @@ __global__ void __launch_bounds__(256) blk_diag_kernel(const double *__restrict_
     }
 }
 
-// P[i][c] = sum_s S[i][k0+s] Dinv[s][c] for every row i (rows inside K unused)
-__global__ void __launch_bounds__(256) blk_panel_kernel(const double *__restrict__ S, int m, int k0, int t,
-                                                        const double *__restrict__ Dinv, double *__restrict__ P)
+// P[i][:] = S[i][K] Dinv for every row i (one thread per row, FP64), stored as pairs
+__global__ void __launch_bounds__(128) blk_panel_df_kernel(const float2 *__restrict__ W, int m, int k0, int t,
+                                                           const double *__restrict__ Dinv, float2 *__restrict__ P)
 {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)m * SW_T) return;
-    const int i = (int)(idx / SW_T), c = (int)(idx % SW_T);
-    if (c >= t) return;
-    const double *row = S + (int64_t)i * m + k0;
-    double acc = 0.0;
-    for (int q = 0; q < t; ++q) acc += row[q] * Dinv[q * SW_T + c];
-    P[(int64_t)i * SW_T + c] = acc;
+    __shared__ double Ds[SW_T * SW_T];
+    for (int e = threadIdx.x; e < SW_T * SW_T; e += blockDim.x) Ds[e] = Dinv[e];
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || (i >= k0 && i < k0 + t)) return;
+    double acc[SW_T];
+#pragma unroll
+    for (int c = 0; c < SW_T; ++c) acc[c] = 0.0;
+    for (int q = 0; q < t; ++q) {
+        const int kq = k0 + q;
+        const double s = df_value(i < kq ? W[(int64_t)i * m + kq] : W[(int64_t)kq * m + i]);
+#pragma unroll
+        for (int c = 0; c < SW_T; ++c) acc[c] += s * Ds[q * SW_T + c];
+    }
+#pragma unroll
+    for (int c = 0; c < SW_T; ++c) P[(int64_t)i * SW_T + c] = df_split(c < t ? acc[c] : 0.0);
 }
 
-// S[i][j] -= sum_s P[i][s] S[k0+s][j] for i, j outside K; 32x32 output tiles
-__global__ void __launch_bounds__(256) blk_update_kernel(double *__restrict__ S, int m, int k0, int t,
-                                                         const double *__restrict__ P)
+// W[i][j] -= sum_q P[i][q] S[k0+q][j] for the upper-triangle tiles outside K,
+// in double-float; 32 x 32 output tiles, four rows per thread
+__global__ void __launch_bounds__(256) blk_update_df_kernel(float2 *__restrict__ W, int m, int k0, int t,
+                                                            const float2 *__restrict__ P)
 {
-    __shared__ double Pt[32][SW_T + 1], Kt[SW_T][33];
-    const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+    const int bi = blockIdx.y, bj = blockIdx.x, bk = k0 / 32;
+    if (bj < bi || bi == bk || bj == bk) return;
+    __shared__ float2 Pt[32][SW_T + 1], Kt[SW_T][33];
+    const int i0 = bi * 32, j0 = bj * 32;
     for (int e = threadIdx.x; e < 32 * SW_T; e += blockDim.x) {
         const int r = e / SW_T, q = e % SW_T;
         const int i = i0 + r;
-        Pt[r][q] = (i < m && q < t) ? P[(int64_t)i * SW_T + q] : 0.0;
-        const int qq = e / 32, cc = e % 32;
-        const int j = j0 + cc;
-        Kt[qq][cc] = (j < m && qq < t) ? S[(int64_t)(k0 + qq) * m + j] : 0.0;
+        Pt[r][q] = (i < m && q < t) ? P[(int64_t)i * SW_T + q] : make_float2(0.f, 0.f);
+    }
+    if (j0 < k0) {  // S[k0+q][j] = W[j][k0+q] (upper storage): read rows j, contiguous in q
+        for (int e = threadIdx.x; e < 32 * SW_T; e += blockDim.x) {
+            const int cc = e / SW_T, q = e % SW_T;
+            const int j = j0 + cc;
+            Kt[q][cc] = (j < m && q < t) ? W[(int64_t)j * m + k0 + q] : make_float2(0.f, 0.f);
+        }
+    } else {        // S[k0+q][j] = W[k0+q][j]: contiguous in j
+        for (int e = threadIdx.x; e < 32 * SW_T; e += blockDim.x) {
+            const int q = e / 32, cc = e % 32;
+            const int j = j0 + cc;
+            Kt[q][cc] = (j < m && q < t) ? W[(int64_t)(k0 + q) * m + j] : make_float2(0.f, 0.f);
+        }
     }
     __syncthreads();
-    const int cc = threadIdx.x & 31;
+    const int cc = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int j = j0 + cc;
-    for (int r = threadIdx.x >> 5; r < 32; r += blockDim.x >> 5) {
-        const int i = i0 + r;
-        if (i >= m || j >= m) continue;
-        if ((i >= k0 && i < k0 + t) || (j >= k0 && j < k0 + t)) continue;
-        double acc = 0.0;
-#pragma unroll 8
-        for (int q = 0; q < SW_T; ++q) acc += Pt[r][q] * Kt[q][cc];
-        S[(int64_t)i * m + j] -= acc;
+    float sh[4], sl[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) sh[s] = sl[s] = 0.f;
+#pragma unroll 4
+    for (int q = 0; q < SW_T; ++q) {
+        const float2 k = Kt[q][cc];
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const float2 a = Pt[wid + 8 * s][q];
+            df_fma(sh[s], sl[s], a.x, a.y, k.x, k.y);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int i = i0 + wid + 8 * s;
+        if (i >= m || j >= m || j < i) continue;
+        float2 w = W[(int64_t)i * m + j];
+        df_add(w.x, w.y, -sh[s], -sl[s]);
+        const float hsum = __fadd_rn(w.x, w.y);  // renormalise the pair
+        w.y = __fsub_rn(w.y, __fsub_rn(hsum, w.x));
+        w.x = hsum;
+        W[(int64_t)i * m + j] = w;
     }
 }
 
-// write the swept pivot rows/columns: S[i][K] = P[i], S[K][i] = P[i]^T, S[K][K] = -Dinv
-__global__ void __launch_bounds__(256) blk_write_kernel(double *__restrict__ S, int m, int k0, int t,
-                                                        const double *__restrict__ P,
-                                                        const double *__restrict__ Dinv)
+// the swept pivot rows (upper storage): S[i][K] = P[i] for i < k0, S[K][i] = P[i]
+// for i past K, S[K][K] = -Dinv
+__global__ void __launch_bounds__(256) blk_write_df_kernel(float2 *__restrict__ W, int m, int k0, int t,
+                                                           const float2 *__restrict__ P,
+                                                           const double *__restrict__ Dinv)
 {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)m * SW_T) return;
     const int i = (int)(idx / SW_T), c = (int)(idx % SW_T);
     if (c >= t) return;
-    if (i >= k0 && i < k0 + t) {
-        S[(int64_t)i * m + k0 + c] = -Dinv[(i - k0) * SW_T + c];
-    } else {
-        const double v = P[(int64_t)i * SW_T + c];
-        S[(int64_t)i * m + k0 + c] = v;
-        S[(int64_t)(k0 + c) * m + i] = v;
+    if (i >= k0 && i < k0 + t) W[(int64_t)i * m + k0 + c] = df_split(-Dinv[(i - k0) * SW_T + c]);
+    else if (i < k0) W[(int64_t)i * m + k0 + c] = P[(int64_t)i * SW_T + c];
+    else W[(int64_t)(k0 + c) * m + i] = P[(int64_t)i * SW_T + c];
+}
+
+// lower triangle := upper triangle (pairs)
+__global__ void mirror_df_kernel(float2 *__restrict__ W, int m)
+{
+    const int64_t mm = (int64_t)m * m;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < mm;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(idx / m), c = (int)(idx % m);
+        if (r > c) W[idx] = W[(int64_t)c * m + r];
     }
 }
 
-__global__ void negate_check_kernel(double *__restrict__ S, int64_t count, int *bad)
+// in place, elementwise: the pair becomes the FP64 entry of A^-1 (the sweep leaves -A^-1)
+__global__ void finish_df_kernel(double *__restrict__ S, int64_t count, int *bad)
 {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
-        const double v = -S[i];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = -df_value(reinterpret_cast<const float2 *>(S)[i]);
         if (!isfinite(v)) atomicOr(bad, 8);
         S[i] = v;
     }
@@ -294,23 +353,27 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
     int maxm = 0;
     for (int32_t q = 0; q < nsub; ++q) maxm = std::max(maxm, h_off[q + 1] - h_off[q]);
     if (maxm > SMALL) {
-        DBuf<double> Dinv((size_t)SW_T * SW_T), P((size_t)maxm * SW_T);
+        DBuf<double> Dinv((size_t)SW_T * SW_T);
+        DBuf<float2> P((size_t)maxm * SW_T);
         for (int32_t q = 0; q < nsub; ++q) {
             const int m = h_off[q + 1] - h_off[q];
             if (m <= SMALL) continue;
             double *Sq = inv + hoff[q];
+            float2 *Wq = reinterpret_cast<float2 *>(Sq);
             const int64_t mm = (int64_t)m * m;
-            symmetrize_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, s>>>(Sq, m);
+            to_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, s>>>(Sq, mm);
             const unsigned gp = (unsigned)(((int64_t)m * SW_T + 255) / 256);
+            const unsigned gr = (unsigned)((m + 127) / 128);
             const dim3 gu((m + 31) / 32, (m + 31) / 32);
             for (int k0 = 0; k0 < m; k0 += SW_T) {
                 const int t = std::min(SW_T, m - k0);
-                blk_diag_kernel<<<1, 256, 0, s>>>(Sq, m, k0, t, Dinv.data(), bad);
-                blk_panel_kernel<<<gp, 256, 0, s>>>(Sq, m, k0, t, Dinv.data(), P.data());
-                blk_update_kernel<<<gu, 256, 0, s>>>(Sq, m, k0, t, P.data());
-                blk_write_kernel<<<gp, 256, 0, s>>>(Sq, m, k0, t, P.data(), Dinv.data());
+                blk_diag_df_kernel<<<1, 256, 0, s>>>(Wq, m, k0, t, Dinv.data(), bad);
+                blk_panel_df_kernel<<<gr, 128, 0, s>>>(Wq, m, k0, t, Dinv.data(), P.data());
+                blk_update_df_kernel<<<gu, 256, 0, s>>>(Wq, m, k0, t, P.data());
+                blk_write_df_kernel<<<gp, 256, 0, s>>>(Wq, m, k0, t, P.data(), Dinv.data());
             }
-            negate_check_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, s>>>(Sq, mm, bad);
+            mirror_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, s>>>(Wq, m);
+            finish_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, s>>>(Sq, mm, bad);
             LSS_LAUNCH_CHECK();
         }
         LSS_CUDA(cudaStreamSynchronize(s));  // Dinv and P are freed at scope exit

@@ -238,6 +238,31 @@ def test_mixed_matches_fp64_on_penalty_springs(built):
         _check_solution(A, b, x)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_large_stiff_subdomain(precision, built):
+    """A 0.3-radius x1e6 inclusion on a 16^3-node cube makes one stiff
+    subdomain of about 2,000 DOFs: the blocked, double-float sweep inverse
+    (blocks above 128 DOFs).  The preconditioner matches the oracle's (exact
+    Cholesky of the same block, same partition and damping) to 1e-7 in FP64,
+    and the solve reaches the parity bar."""
+    from lss import gen
+    A, b, _ = gen.workload_elasticity_inclusion(seed=2, nodes=16, radius=0.3)
+    A = A.tocsc()
+    params = {"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4}
+    s = _solver(params, {"precision": precision})
+    s.factorize(A)
+    info = s.get_info()
+    assert info["max_subdomain_dofs"] > 1000, info["max_subdomain_dofs"]
+    if precision == "fp64":
+        o = _oracle_with_product_partition(A, s, params, mas_omega=info["mas_omega"])
+        r = np.random.default_rng(5).standard_normal(A.shape[0])
+        z, zo = s.precond(r), o.precond(r)
+        assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < 1e-7
+    x = s.solve(b)
+    _check_solution(A, b, x)
+    assert s.get_info()["status"] == "converged_rel"
+
+
 def _outer_as_row(A):
     """The operator the solver applies: outer index = row (GPUHybrid.cu:203-209)."""
     A = A.tocsc()
