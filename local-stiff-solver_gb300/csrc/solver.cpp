@@ -726,7 +726,9 @@ void HybridSolver::run_pcg()
         LSS_CUDA(cudaStreamSynchronize(stream_));
         const int reason = h_state_->done;
         const bool converged = reason == STOP_CONVERGED_REL || reason == STOP_CONVERGED_ABS;
-        const bool true_ok = !(hs.rel_eps > 0) || res2 / bb <= hs.rel_eps;
+        // 10% margin: a second FP64 evaluation of b - A x (another summation
+        // order) must not find the returned x above the tolerance
+        const bool true_ok = !(hs.rel_eps > 0) || res2 / bb <= 0.81 * hs.rel_eps;
         // restart only while restarting still pays: the true residual has a rounding
         // floor of about eps * || |A| |x| || that no restart can go below
         const bool improving = res2 < 0.25 * prev_res2;
@@ -738,7 +740,7 @@ void HybridSolver::run_pcg()
             // the true residual under it
             ++refinements_;
             h_state_->done = STOP_RUNNING;
-            if (hs.rel_eps > 0 && !(res2 / bb <= hs.rel_eps)) {
+            if (hs.rel_eps > 0 && !true_ok) {
                 const double true_rel = std::sqrt(res2 / bb);
                 const double target = p_.rel_tol * std::min(1.0, 0.5 * p_.rel_tol / true_rel);
                 h_state_->rel_eps = target * target;

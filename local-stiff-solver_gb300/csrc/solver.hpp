@@ -131,7 +131,9 @@ private:
     bool precise_rows_ = false;
     bool need_vals_df() const { return df32() || (p_.mixed && p_.precond_residual != 1); }
     void setup_precise_rows();
-    bool df32() const { return p_.outer_spmv == 2 || (p_.outer_spmv == 0 && p_.mixed); }
+    // auto: double-float for block rows (a 3x3 block needs 9 DFMA per 76 bytes,
+    // FP64-pipe-bound on this GPU); FP64 for scalar CSR rows, which it does not bind
+    bool df32() const { return p_.outer_spmv == 2 || (p_.outer_spmv == 0 && p_.mixed && p_.block_size > 1); }
     void outer_spmv_alpha();  // Ap, p.Ap, alpha with the configured outer SpMV
     void split_p();           // refresh the df32 split of p (after p = z)
     DBuf<PcgState> d_state_;

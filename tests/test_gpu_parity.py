@@ -292,7 +292,7 @@ def test_solve_elasticity_inclusion(precision, outer, elast20):
     info = s.get_info()
     assert info["status"] == "converged_rel" and info["num_iterations"] > 0
     assert info["num_stiff_dofs"] > 0 and info["precision"] == precision
-    expect = {"auto": "df32" if precision == "mixed" else "fp64"}.get(outer, outer)
+    expect = {"auto": "df32" if precision == "mixed" else "fp64"}.get(outer, outer)  # block_size 3
     assert info["outer_spmv"] == expect
 
 
