@@ -615,7 +615,7 @@ void HybridSolver::precond(const double *r, double *z, int dot_mode, const float
 
 void HybridSolver::outer_spmv_alpha()
 {
-    if (df32())
+    if (outer_df())
         launch_pcg_spmv_alpha_df(A_, d_p_df_.data(), d_ap_df_.data(), d_state_.data(), gr_, stream_);
     else
         launch_pcg_spmv_alpha(A_, d_p_.data(), d_ap_.data(), d_state_.data(), gr_, stream_);
@@ -623,14 +623,14 @@ void HybridSolver::outer_spmv_alpha()
 
 void HybridSolver::split_p()
 {
-    if (df32()) launch_split(n_vec(), d_p_.data(), d_p_df_.data(), stream_);
+    if (outer_df()) launch_split(n_vec(), d_p_.data(), d_p_df_.data(), stream_);
 }
 
 void HybridSolver::iteration()
 {
     outer_spmv_alpha();
     float *r32 = p_.mixed ? d_r32_.data() : nullptr;
-    if (df32())
+    if (outer_df())
         launch_pcg_update_xr_df(n_vec(), d_x_.data(), d_r_.data(), d_p_.data(), d_ap_df_.data(), d_state_.data(),
                                 gr_, stream_, r32);
     else
@@ -638,7 +638,7 @@ void HybridSolver::iteration()
                              stream_, r32);
     precond(d_r_.data(), d_z_.data(), 2, r32);
     launch_pcg_update_p(n_vec(), d_p_.data(), d_z_.data(), d_state_.data(), stream_,
-                        df32() ? d_p_df_.data() : nullptr);
+                        outer_df() ? d_p_df_.data() : nullptr);
 }
 
 void HybridSolver::launch_chunk(int iters)
@@ -674,6 +674,18 @@ void HybridSolver::launch_chunk(int iters)
 
 void HybridSolver::run_pcg()
 {
+    // the refinement restarts switch the outer product to FP64; every solve
+    // starts with the configured one
+    struct RefineReset {
+        HybridSolver *s;
+        ~RefineReset()
+        {
+            if (s->refine_fp64_) {
+                s->refine_fp64_ = false;
+                s->invalidate_graph();
+            }
+        }
+    } refine_reset{this};
     const int64_t n = n_vec();
     double *bb_d = d_scalar_.data();
     launch_dot(n, d_b_.data(), d_b_.data(), bb_d, gr_, stream_);
@@ -740,6 +752,13 @@ void HybridSolver::run_pcg()
             // the true residual under it
             ++refinements_;
             h_state_->done = STOP_RUNNING;
+            // the restarts use the FP64 product: the double-float one's 2^-48 per
+            // term sets a floor of 2^-48 || |A| |x| || that can exceed the
+            // tolerance on high-contrast systems (1e7 moduli times a near-rigid x)
+            if (outer_df()) {
+                refine_fp64_ = true;
+                invalidate_graph();
+            }
             if (hs.rel_eps > 0 && !true_ok) {
                 const double true_rel = std::sqrt(res2 / bb);
                 const double target = p_.rel_tol * std::min(1.0, 0.5 * p_.rel_tol / true_rel);
@@ -1005,7 +1024,7 @@ void HybridSolver::op_spmv_outer(const double *x, double *y)
     launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_tmp_.data(), d_p_.data(), true, stream_);
     split_p();
     outer_spmv_alpha();
-    if (df32()) launch_df_to_double(n, d_ap_df_.data(), d_ap_.data(), stream_);
+    if (outer_df()) launch_df_to_double(n, d_ap_df_.data(), d_ap_.data(), stream_);
     launch_permute(pat_.nb, pat_.bd, d_perm_.data(), d_ap_.data(), d_tmp_.data(), false, stream_);
     LSS_CUDA(cudaMemcpyAsync(y, d_tmp_.data(), n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
     LSS_CUDA(cudaStreamSynchronize(stream_));

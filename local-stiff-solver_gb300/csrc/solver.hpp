@@ -134,6 +134,8 @@ private:
     // auto: double-float for block rows (a 3x3 block needs 9 DFMA per 76 bytes,
     // FP64-pipe-bound on this GPU); FP64 for scalar CSR rows, which it does not bind
     bool df32() const { return p_.outer_spmv == 2 || (p_.outer_spmv == 0 && p_.mixed && p_.block_size > 1); }
+    bool refine_fp64_ = false;  // refinement restarts of the current solve use the FP64 product
+    bool outer_df() const { return df32() && !refine_fp64_; }
     void outer_spmv_alpha();  // Ap, p.Ap, alpha with the configured outer SpMV
     void split_p();           // refresh the df32 split of p (after p = z)
     DBuf<PcgState> d_state_;

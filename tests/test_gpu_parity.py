@@ -238,6 +238,24 @@ def test_mixed_matches_fp64_on_penalty_springs(built):
         _check_solution(A, b, x)
 
 
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_mixed_high_contrast_reaches_tolerance(seed, built):
+    """E ratio 1e7: the double-float outer product's 2^-48 per term can set a
+    residual floor above 1e-8 here; the refinement restarts then run with the
+    FP64 product, so the returned x meets the tolerance (checked with scipy's
+    own FP64 residual)."""
+    from lss import gen
+    A, b, _ = gen.workload_elasticity_inclusion(seed=seed, nodes=20, E_ratio=1e7)
+    A = A.tocsc()
+    s = _solver({"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0,
+                 "min_subdomain_size": 4}, {"precision": "mixed"})
+    s.factorize(A)
+    x = s.solve(b)
+    Ar = _outer_as_row(A)
+    rel = np.linalg.norm(b - Ar @ x) / np.linalg.norm(b)
+    assert rel <= 1e-8, (rel, s.get_info()["refinements"])
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_large_stiff_subdomain(precision, built):
     """A 0.3-radius x1e6 inclusion on a 16^3-node cube makes one stiff
