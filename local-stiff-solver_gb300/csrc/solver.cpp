@@ -738,9 +738,9 @@ void HybridSolver::run_pcg()
         LSS_CUDA(cudaStreamSynchronize(stream_));
         const int reason = h_state_->done;
         const bool converged = reason == STOP_CONVERGED_REL || reason == STOP_CONVERGED_ABS;
-        // 10% margin: a second FP64 evaluation of b - A x (another summation
+        // 2% margin: a second FP64 evaluation of b - A x (another summation
         // order) must not find the returned x above the tolerance
-        const bool true_ok = !(hs.rel_eps > 0) || res2 / bb <= 0.81 * hs.rel_eps;
+        const bool true_ok = !(hs.rel_eps > 0) || res2 / bb <= 0.9604 * hs.rel_eps;
         // restart only while restarting still pays: the true residual has a rounding
         // floor of about eps * || |A| |x| || that no restart can go below
         const bool improving = res2 < 0.25 * prev_res2;
