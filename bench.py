@@ -229,6 +229,8 @@ def main():
     ap.add_argument("--batch-count", type=int, default=64, help="systems of the batched workload")
     ap.add_argument("--batch-rhs", type=int, default=16, help="right-hand sides per batched system")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--mas-offdiag", default="fp32", choices=["fp32", "bf16"],
+                    help="storage of the mixed solver's level-0 off-diagonal MAS inverse tiles")
     ap.add_argument("--ref-iters", type=int, default=25, help="PCG iterations per reference-arm step")
     ap.add_argument("--cpu-iters", type=int, default=10, help="PCG iterations of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -262,8 +264,10 @@ def main():
     gb300_common = {"device": local}
 
     def make(precision):
-        p = {"solver": "GPUHybrid", "GPUHybrid": dict(params),
-             "gb300": dict(gb300_common, precision=precision)}
+        gb = dict(gb300_common, precision=precision)
+        if precision == "mixed" and args.mas_offdiag != "fp32":
+            gb["mas_offdiag"] = args.mas_offdiag
+        p = {"solver": "GPUHybrid", "GPUHybrid": dict(params), "gb300": gb}
         return lss.Solver.create(p)
 
     t0 = time.perf_counter()

@@ -155,6 +155,7 @@ struct MasDev {
     const uint8_t *ccnt[MAS_MAXL] = {};
     int32_t ncoarse = 0;                // total coarse banks
     int64_t tile_elems = 0;             // inverse elements per bank
+    int64_t bank_bytes0 = 0;            // > 0: level-0 banks hold FP32 diagonal and BF16 off-diagonal tiles, this stride
     int64_t level_elems = 0;            // elements of the level-vector buffers
 };
 
@@ -167,7 +168,9 @@ void launch_mas_assemble_coarse(const BsrDev &A, const MasDev &m, const int32_t 
                                 double *stage, cudaStream_t s);
 // pad zero diagonals, invert (symmetric sweep), write bank tiles (FP32 or FP64)
 void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, bool fp32, int *bad,
-                       cudaStream_t s);
+                       cudaStream_t s, bool bf16_offdiag = false);
+// bytes of one bank with FP32 diagonal and BF16 off-diagonal tiles
+int64_t mas_bank_bytes_bf16(int bd);
 // z = MAS^-1 xin (acc: z += MAS^-1 xin).  dot_mode 1: st->gamma = rdot.z;
 // dot_mode 2: st->beta = rdot.z / st->gamma, st->gamma = rdot.z.
 // z = scale * MAS^-1 xin, or z += scale * MAS^-1 xin with acc.

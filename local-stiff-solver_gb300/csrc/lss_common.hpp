@@ -168,6 +168,7 @@ struct Params {
     bool mixed = false;             // FP32 MAS (+ FP32 operator inside the preconditioner)
     int outer_spmv = 0;             // PCG's A p: 0 auto (df32 iff mixed), 1 FP64, 2 df32 (FP32-pipe double-float)
     int precond_residual = 0;       // mixed r - A z: 0 auto (df32 on stiff rows), 1 FP32, 2 df32 everywhere
+    bool mas_bf16_offdiag = false;  // mixed: BF16 storage of the level-0 off-diagonal inverse tiles
     bool multiplicative = true;     // GPUHybrid composition; false = MASSolver additive form
     int max_coarse_levels = 4;      // MAS_MAX_COARSE_LEVEL (MASPreconditioner.hpp:11); <= 6
     double mas_damping = 0.0;       // omega of MAS in the multiplicative form; <= 0: automatic

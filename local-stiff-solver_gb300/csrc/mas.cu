@@ -16,12 +16,17 @@
 // and the symmetric partner term travels by warp shuffle instead of being
 // stored twice.  The inverse streams from HBM once per apply with evict-first
 // loads; residual and coarse vectors stay in L2.
+#include <cuda_bf16.h>
+
+#include <type_traits>
+
 #include "device_common.cuh"
 #include "kernels.hpp"
 
 namespace lss {
 
 int64_t mas_tile_elems(int bd) { return (int64_t)bd * 17 * 32 + (int64_t)bd * (bd - 1) / 2 * 1024; }
+int64_t mas_bank_bytes_bf16(int bd) { return (int64_t)bd * 17 * 32 * 4 + (int64_t)bd * (bd - 1) / 2 * 1024 * 2; }
 
 namespace {
 
@@ -68,6 +73,52 @@ __device__ __forceinline__ void tile_symv(const T *__restrict__ tile, const T (&
                 y[c2] += __shfl_sync(FULL, tr, (lane - d) & 31);
             }
             t += 32 * 32;
+        }
+    }
+}
+
+// tile_symv for a bank whose diagonal tiles are FP32 and whose off-diagonal
+// tiles (c < c2) are BF16 (the same order: for each c, tile (c, c) then the
+// tiles (c, c2 > c)); a BF16 value widens to FP32 exactly by a 16-bit shift.
+__device__ __forceinline__ float bf16_bits_to_float(unsigned short u) { return __uint_as_float((uint32_t)u << 16); }
+
+template <int BD>
+__device__ __forceinline__ void tile_symv_bf(const unsigned char *__restrict__ bank, const float (&x)[BD],
+                                             float (&y)[BD], int lane)
+{
+#pragma unroll
+    for (int c = 0; c < BD; ++c) y[c] = 0.f;
+    const unsigned char *t = bank;
+#pragma unroll
+    for (int c = 0; c < BD; ++c) {
+        {
+            const float *__restrict__ dt = reinterpret_cast<const float *>(t);
+            float a = ld_stream(dt + lane);
+            y[c] += a * x[c];
+#pragma unroll
+            for (int d = 1; d < 16; ++d) {
+                a = ld_stream(dt + d * 32 + lane);
+                const float xs = __shfl_sync(FULL, x[c], (lane + d) & 31);
+                y[c] += a * xs;
+                const float tr = a * x[c];
+                y[c] += __shfl_sync(FULL, tr, (lane - d) & 31);
+            }
+            a = ld_stream(dt + 16 * 32 + lane);
+            y[c] += a * __shfl_xor_sync(FULL, x[c], 16);
+            t += 17 * 32 * sizeof(float);
+        }
+#pragma unroll
+        for (int c2 = c + 1; c2 < BD; ++c2) {
+            const unsigned short *__restrict__ ot = reinterpret_cast<const unsigned short *>(t);
+#pragma unroll 8
+            for (int d = 0; d < 32; ++d) {
+                const float a = bf16_bits_to_float(__ldcs(ot + d * 32 + lane));
+                const float xs = __shfl_sync(FULL, x[c2], (lane + d) & 31);
+                y[c] += a * xs;
+                const float tr = a * x[c];
+                y[c2] += __shfl_sync(FULL, tr, (lane - d) & 31);
+            }
+            t += 32 * 32 * sizeof(unsigned short);
         }
     }
 }
@@ -204,7 +255,7 @@ __device__ void sweep_invert(double *S, int ld, double *col, double *scol, int *
     }
 }
 
-template <int BD, typename T>
+template <int BD, typename T, bool BF>
 __global__ void __launch_bounds__(256, 2) mas_invert_kernel(const double *__restrict__ stage, T *__restrict__ out,
                                                          int *bad)
 {
@@ -223,6 +274,23 @@ __global__ void __launch_bounds__(256, 2) mas_invert_kernel(const double *__rest
     __syncthreads();
     sweep_invert<N>(S, LD, col, scol, bad);
     // tiles
+    if (BF) {  // FP32 diagonal tiles, BF16 off-diagonal tiles (round to nearest even)
+        unsigned char *dst = reinterpret_cast<unsigned char *>(out) + bank * (int64_t)(BD * 17 * 32 * 4 + BD * (BD - 1) / 2 * 2048);
+        for (int c = 0; c < BD; ++c)
+            for (int c2 = c; c2 < BD; ++c2) {
+                const int nd = (c == c2) ? 17 : 32;
+                for (int e = threadIdx.x; e < nd * 32; e += blockDim.x) {
+                    const int d = e >> 5, r = e & 31;
+                    const int gi = c * 32 + r, gj = c2 * 32 + ((r + d) & 31);
+                    const double val = -S[min(gi, gj) * LD + max(gi, gj)];
+                    if (!isfinite(val)) atomicOr(bad, 2);
+                    if (c == c2) reinterpret_cast<float *>(dst)[e] = (float)val;
+                    else reinterpret_cast<__nv_bfloat16 *>(dst)[e] = __float2bfloat16_rn((float)val);
+                }
+                dst += (c == c2) ? 17 * 32 * 4 : 32 * 32 * 2;
+            }
+        return;
+    }
     T *dst = out + bank * tile_elems<BD>();
     int64_t off = 0;
     for (int c = 0; c < BD; ++c)
@@ -369,7 +437,7 @@ __global__ void __launch_bounds__(256) prolong_all_kernel(MasDev m, T *__restric
 
 // level 0: z = Inv_0 x (+ coarse correction u_1), optional accumulate and r.z;
 // x in FP64, or in FP32 (XT = float) when it comes from the FP32 residual
-template <int BD, typename T, bool ACC, int DOT, typename XT>
+template <int BD, typename T, bool ACC, int DOT, typename XT, bool BF = false>
 __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restrict__ inv0, const T *__restrict__ u,
                                                     const XT *__restrict__ xin, double *__restrict__ z,
                                                     double scale, const double *__restrict__ rdot, PcgState *st,
@@ -388,7 +456,10 @@ __global__ void __launch_bounds__(256) symv0_kernel(MasDev m, const T *__restric
         T x[BD], y[BD];
 #pragma unroll
         for (int c = 0; c < BD; ++c) x[c] = valid ? (T)xin[(int64_t)node * BD + c] : T(0);
-        tile_symv<BD, T>(inv0 + p * m.tile_elems, x, y, lane);
+        if constexpr (BF && std::is_same<T, float>::value)
+            tile_symv_bf<BD>(reinterpret_cast<const unsigned char *>(inv0) + p * m.bank_bytes0, x, y, lane);
+        else
+            tile_symv<BD, T>(inv0 + p * m.tile_elems, x, y, lane);
         if (valid) {
             int64_t cidx = -1;
             if (m.L > 1) cidx = (int64_t)(m.cbase0[p] + m.key0[node]) * BD;
@@ -438,8 +509,15 @@ void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, 
             prolong_all_kernel<BD, T><<<grid_for(m.nitems[1], 256, 1 << 30), 256, 0, s>>>(m, u, done);
     }
     const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
-#define LSS_S0(A_, D_) \
-    symv0_kernel<BD, T, A_, D_, XT><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr, done, z32, z_lo)
+#define LSS_S0(A_, D_)                                                                                          \
+    do {                                                                                                        \
+        if (std::is_same<T, float>::value && m.bank_bytes0 > 0)                                                 \
+            symv0_kernel<BD, T, A_, D_, XT, true><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr,   \
+                                                                       done, z32, z_lo);                        \
+        else                                                                                                    \
+            symv0_kernel<BD, T, A_, D_, XT, false><<<grid, 256, 0, s>>>(m, inv0, u, xin, z, scale, rdot, st, gr,  \
+                                                                        done, z32, z_lo);                       \
+    } while (0)
     if (dot_mode == 0) {
         if (acc) LSS_S0(true, 0);
         else LSS_S0(false, 0);
@@ -482,23 +560,33 @@ void launch_mas_assemble_coarse(const BsrDev &A, const MasDev &m, const int32_t 
     LSS_LAUNCH_CHECK();
 }
 
-template <int BD, typename T>
+template <int BD, typename T, bool BF = false>
 static void invert_t(int64_t nbanks, const double *stage, T *out, int *bad, cudaStream_t s)
 {
     constexpr int N = 32 * BD;
     const size_t smem = (size_t)(N * (N + 1) + 2 * N) * sizeof(double);
-    LSS_CUDA(cudaFuncSetAttribute(mas_invert_kernel<BD, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    LSS_CUDA(cudaFuncSetAttribute(mas_invert_kernel<BD, T, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
     for (int64_t b0 = 0; b0 < nbanks; b0 += 1 << 30) {
         const int64_t cnt = std::min<int64_t>(nbanks - b0, 1 << 30);
-        mas_invert_kernel<BD, T><<<(unsigned)cnt, 256, smem, s>>>(stage + b0 * N * N, out + b0 * mas_tile_elems(BD),
-                                                                  bad);
+        T *o = BF ? reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(out) + b0 * mas_bank_bytes_bf16(BD))
+                  : out + b0 * mas_tile_elems(BD);
+        mas_invert_kernel<BD, T, BF><<<(unsigned)cnt, 256, smem, s>>>(stage + b0 * N * N, o, bad);
     }
     LSS_LAUNCH_CHECK();
 }
 
-void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, bool fp32, int *bad, cudaStream_t s)
+void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, bool fp32, int *bad, cudaStream_t s,
+                       bool bf16_offdiag)
 {
     if (nbanks == 0) return;
+    if (bf16_offdiag) {
+        if (!fp32) fail(LSS_ERR_INTERNAL, "BF16 off-diagonal tiles need the FP32 MAS");
+        if (bd == 1) invert_t<1, float, true>(nbanks, stage, (float *)out, bad, s);
+        else if (bd == 2) invert_t<2, float, true>(nbanks, stage, (float *)out, bad, s);
+        else invert_t<3, float, true>(nbanks, stage, (float *)out, bad, s);
+        return;
+    }
     if (fp32) {
         if (bd == 1) invert_t<1, float>(nbanks, stage, (float *)out, bad, s);
         else if (bd == 2) invert_t<2, float>(nbanks, stage, (float *)out, bad, s);
@@ -518,7 +606,13 @@ void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp
 #define LSS_L0(BD_, T_)                                                                                        \
     symv0_kernel<BD_, T_, false, 0, double><<<grid, 256, 0, s>>>(m, (const T_ *)inv0, (const T_ *)u, xin, z, 1.0,   \
                                                                  nullptr, nullptr, gr, nullptr, nullptr, nullptr)
-    if (fp32) {
+#define LSS_L0BF(BD_)                                                                                          \
+    symv0_kernel<BD_, float, false, 0, double, true><<<grid, 256, 0, s>>>(                                     \
+        m, (const float *)inv0, (const float *)u, xin, z, 1.0, nullptr, nullptr, gr, nullptr, nullptr, nullptr)
+    if (fp32 && m.bank_bytes0 > 0) {
+        if (m.bd == 2) LSS_L0BF(2);
+        else LSS_L0BF(3);
+    } else if (fp32) {
         if (m.bd == 1) LSS_L0(1, float);
         else if (m.bd == 2) LSS_L0(2, float);
         else LSS_L0(3, float);
@@ -528,6 +622,7 @@ void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp
         else LSS_L0(3, double);
     }
 #undef LSS_L0
+#undef LSS_L0BF
     LSS_LAUNCH_CHECK();
 }
 

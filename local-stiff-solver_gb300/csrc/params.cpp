@@ -199,6 +199,10 @@ Params parse_params(const char *json, const Params &base)
                     fail(LSS_ERR_INVALID_ARGUMENT,
                          "gb300.precond_residual must be \"auto\", \"fp32\" or \"df32\"");
                 p.precond_residual = v.str == "auto" ? 0 : (v.str == "fp32" ? 1 : 2);
+            } else if (k == "mas_offdiag") {
+                if (v.kind != JValue::Str || (v.str != "fp32" && v.str != "bf16"))
+                    fail(LSS_ERR_INVALID_ARGUMENT, "gb300.mas_offdiag must be \"fp32\" or \"bf16\"");
+                p.mas_bf16_offdiag = v.str == "bf16";
             } else if (k == "outer_spmv") {
                 if (v.kind != JValue::Str || (v.str != "auto" && v.str != "fp64" && v.str != "df32"))
                     fail(LSS_ERR_INVALID_ARGUMENT, "gb300.outer_spmv must be \"auto\", \"fp64\" or \"df32\"");

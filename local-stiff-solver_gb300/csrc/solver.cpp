@@ -87,7 +87,8 @@ void HybridSolver::set_parameters(const char *json)
                                  np.min_sub != p_.min_sub || np.max_sub != p_.max_sub || np.expand != p_.expand ||
                                  np.float_subdomains != p_.float_subdomains ||
                                  np.multiplicative != p_.multiplicative || np.outer_spmv != p_.outer_spmv ||
-                                 np.precond_residual != p_.precond_residual;
+                                 np.precond_residual != p_.precond_residual ||
+                                 np.mas_bf16_offdiag != p_.mas_bf16_offdiag;
     p_ = np;
     if (pattern_affecting) have_pattern_ = false;
     if (value_affecting) factorized_ = false;
@@ -503,7 +504,10 @@ void HybridSolver::setup_mas()
     const int64_t nparts = mas_.nparts, ncoarse = mas_.ncoarse;
     const int64_t te = mas_.tile_elems;
     const size_t esz = mas_fp32_ ? sizeof(float) : sizeof(double);
-    d_inv0_.resize(nparts * te * esz);
+    // mixed precision may store the level-0 off-diagonal tiles in BF16
+    const bool bf = mas_fp32_ && p_.mas_bf16_offdiag && bd > 1;
+    mas_.bank_bytes0 = bf ? mas_bank_bytes_bf16(bd) : 0;
+    d_inv0_.resize(bf ? (size_t)(nparts * mas_.bank_bytes0) : (size_t)(nparts * te * esz));
     d_invc_.resize(std::max<int64_t>(ncoarse, 1) * te * esz);
     d_bad_.zero(stream_);
     {
@@ -511,7 +515,7 @@ void HybridSolver::setup_mas()
         DBuf<double> stage((size_t)nparts * N * N);
         stage.zero(stream_);
         launch_mas_assemble0(A_, d_part_of_.data(), d_part_off_.data(), stage.data(), stream_);
-        launch_mas_invert(bd, nparts, stage.data(), d_inv0_.data(), mas_fp32_, d_bad_.data(), stream_);
+        launch_mas_invert(bd, nparts, stage.data(), d_inv0_.data(), mas_fp32_, d_bad_.data(), stream_, bf);
         LSS_CUDA(cudaStreamSynchronize(stream_));
     }
     if (ncoarse > 0) {
@@ -529,7 +533,7 @@ void HybridSolver::setup_mas()
     d_u_.resize(std::max<int64_t>(mas_.level_elems, 1) * esz);
     d_v_.zero(stream_);
     d_u_.zero(stream_);
-    stats_["mas_inverse_bytes"] = (double)(nparts + ncoarse) * te * esz;
+    stats_["mas_inverse_bytes"] = (double)(bf ? nparts * mas_.bank_bytes0 : nparts * te * esz) + (double)ncoarse * te * esz;
 }
 
 void HybridSolver::ensure_vectors()
@@ -1117,12 +1121,14 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
     *ms = t / reps;
     const double spmv_bytes = (double)nnzb * (bd * bd * 8 + 4) + (pat_.nb + 1) * 4.0 + 2.0 * n * 8;
     const double esz = mas_fp32_ ? 4.0 : 8.0;
-    const double mas_bytes = (double)(mas_.nparts + mas_.ncoarse) * mas_.tile_elems * esz + 2.0 * n * 8 +
+    const double inv0_bytes = mas_.bank_bytes0 > 0 ? (double)mas_.nparts * mas_.bank_bytes0
+                                                   : (double)mas_.nparts * mas_.tile_elems * esz;
+    const double mas_bytes = inv0_bytes + (double)mas_.ncoarse * mas_.tile_elems * esz + 2.0 * n * 8 +
                              (double)pat_.nb * (1 + 4);
     const double vb = p_.mixed ? 4.0 : 8.0;  // operator value bytes of the residual SpMV
     // r, x, y in FP32 in mixed precision, FP64 otherwise
     const double res_bytes = (double)nnzb * (bd * bd * vb + 4) + (pat_.nb + 1) * 4.0 + (p_.mixed ? 12.0 : 24.0) * n;
-    const double mas0_bytes = (double)mas_.nparts * mas_.tile_elems * esz + 2.0 * n * 8 + (double)pat_.nb * 5;
+    const double mas0_bytes = inv0_bytes + 2.0 * n * 8 + (double)pat_.nb * 5;
     switch (kind) {
     case 0: *bytes = spmv_bytes; break;
     case 1: *bytes = mas_bytes; break;

@@ -214,6 +214,27 @@ def test_mixed_precond_every_residual_shape(lanes, springs16):
     assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < 2e-3
 
 
+def test_mas_bf16_offdiagonal_tiles(springs16):
+    """Mixed precision with the level-0 off-diagonal inverse tiles in BF16:
+    the MAS apply stays within 2e-2 of the FP32-tile one (BF16 keeps 8 bits),
+    the solve converges to the parity bar, and the level-0 inverse bytes drop
+    by a third."""
+    A, b = springs16
+    params = {"block_size": 3, "relative_tolerance": 1e-8, "decompose_subdomains": False}
+    s32 = _solver(params, {"precision": "mixed"})
+    s16 = _solver(params, {"precision": "mixed", "mas_offdiag": "bf16"})
+    s32.factorize(A)
+    s16.factorize(A)
+    r = np.random.default_rng(9).standard_normal(A.shape[0])
+    z32, z16 = s32.mas_apply(r), s16.mas_apply(r)
+    assert np.linalg.norm(z16 - z32) / np.linalg.norm(z32) < 2e-2
+    i32, i16 = s32.get_info(), s16.get_info()
+    assert i16["mas_inverse_bytes"] < 0.8 * i32["mas_inverse_bytes"]
+    x = s16.solve(b)
+    _check_solution(A, b, x)
+    assert s16.get_info()["status"] == "converged_rel"
+
+
 def test_mixed_matches_fp64_on_penalty_springs(built):
     """Lognormal moduli and 1e8 diagonal penalty springs: the mixed mode
     converges like the FP64 mode (same damping estimate within 1e-4, at most
