@@ -79,9 +79,9 @@ __device__ __forceinline__ void tile_symv(const T *__restrict__ tile, const T (&
 
 // tile_symv for a bank whose diagonal tiles are FP32 and whose off-diagonal
 // tiles (c < c2) are BF16 (the same order: for each c, tile (c, c) then the
-// tiles (c, c2 > c)); a BF16 value widens to FP32 exactly by a 16-bit shift.
-__device__ __forceinline__ float bf16_bits_to_float(unsigned short u) { return __uint_as_float((uint32_t)u << 16); }
-
+// tiles (c, c2 > c)).  In a BF16 tile, 32-bit word k * 32 + r holds the
+// entries [2k][r] (low half) and [2k + 1][r] (high half), so every warp load
+// is still one 128-byte line; a BF16 value widens to FP32 exactly by a shift.
 template <int BD>
 __device__ __forceinline__ void tile_symv_bf(const unsigned char *__restrict__ bank, const float (&x)[BD],
                                              float (&y)[BD], int lane)
@@ -109,14 +109,19 @@ __device__ __forceinline__ void tile_symv_bf(const unsigned char *__restrict__ b
         }
 #pragma unroll
         for (int c2 = c + 1; c2 < BD; ++c2) {
-            const unsigned short *__restrict__ ot = reinterpret_cast<const unsigned short *>(t);
-#pragma unroll 8
-            for (int d = 0; d < 32; ++d) {
-                const float a = bf16_bits_to_float(__ldcs(ot + d * 32 + lane));
-                const float xs = __shfl_sync(FULL, x[c2], (lane + d) & 31);
-                y[c] += a * xs;
-                const float tr = a * x[c];
-                y[c2] += __shfl_sync(FULL, tr, (lane - d) & 31);
+            const unsigned int *__restrict__ ot = reinterpret_cast<const unsigned int *>(t);
+#pragma unroll 4
+            for (int k = 0; k < 16; ++k) {
+                const unsigned int w = __ldcs(ot + k * 32 + lane);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int d = 2 * k + h;
+                    const float a = __uint_as_float(h ? (w & 0xffff0000u) : (w << 16));
+                    const float xs = __shfl_sync(FULL, x[c2], (lane + d) & 31);
+                    y[c] += a * xs;
+                    const float tr = a * x[c];
+                    y[c2] += __shfl_sync(FULL, tr, (lane - d) & 31);
+                }
             }
             t += 32 * 32 * sizeof(unsigned short);
         }
@@ -285,7 +290,8 @@ __global__ void __launch_bounds__(256, 2) mas_invert_kernel(const double *__rest
                     const double val = -S[min(gi, gj) * LD + max(gi, gj)];
                     if (!isfinite(val)) atomicOr(bad, 2);
                     if (c == c2) reinterpret_cast<float *>(dst)[e] = (float)val;
-                    else reinterpret_cast<__nv_bfloat16 *>(dst)[e] = __float2bfloat16_rn((float)val);
+                    else reinterpret_cast<__nv_bfloat16 *>(dst)[(d >> 1) * 64 + 2 * r + (d & 1)] =
+                        __float2bfloat16_rn((float)val);
                 }
                 dst += (c == c2) ? 17 * 32 * 4 : 32 * 32 * 2;
             }
