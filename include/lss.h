@@ -163,6 +163,24 @@ lss_status lss_op_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer,
 /* y = A x with the factorized FP64 operator (original ordering). */
 lss_status lss_op_spmv(lss_solver *s, const double *x, double *y);
 
+/* Per scalar row of the permuted operator (partition order): |diagonal|,
+ * max |off-diagonal| and the l1 norm -- the scores of MASSolver's bad-DOF
+ * selections (BadDOFPreconditioner.cu:110-145, BadDofKMeanPreconditioner.cu:
+ * 187-226, BadDofGMMPreconditioner.cu:285-310).  Arrays of n. */
+lss_status lss_op_row_scores(lss_solver *s, double *diag_abs, double *offdiag_max, double *l1);
+
+/* MASSolver's bad-DOF selection on host scores (the solver applies it with
+ * "gb300": {"bad_dof_strategy": ...}): strategy 1 elbow on |diagonal|
+ * (BadDOFPreconditioner.cu:61-100); 2 k-means with p1 = search fraction,
+ * p2 = jump threshold, i1 = max iterations, i2 = expand neighbours
+ * (BadDofKMeanPreconditioner.cu:63-172); 3 GMM with p1 = jump threshold,
+ * p2 = tol, i1 = max iterations, i2 = expand neighbours
+ * (BadDofGMMPreconditioner.cu:73-255).  Writes the selected positions in the
+ * reference's output order to out (capacity n; may be NULL) and their number
+ * to count. */
+lss_status lss_op_select_bad_dofs(int32_t strategy, int32_t n, const double *score, double p1, double p2,
+                                  int32_t i1, int32_t i2, int32_t *out, int32_t *count);
+
 /* y = A x with the PCG's own operator product (the A p of pcg_solve,
  * GPUHybrid.cu:1458): FP64, or double-float on the FP32 pipe when
  * gb300.outer_spmv resolves to "df32". */

@@ -8,6 +8,7 @@
 #include <thread>
 #include <vector>
 
+#include "baddof.hpp"
 #include "noalloc.hpp"
 #include "solver.hpp"
 
@@ -441,3 +442,28 @@ lss_status lss_solve_batched_device(lss_solver *const *solvers, int32_t count, c
         }
     });
 }
+
+lss_status lss_op_row_scores(lss_solver *s, double *diag_abs, double *offdiag_max, double *l1)
+{
+    if (!valid(s) || !diag_abs || !offdiag_max || !l1) return LSS_ERR_INVALID_ARGUMENT;
+    return guarded(s, [&]() { s->impl->op_row_scores(diag_abs, offdiag_max, l1); });
+}
+
+lss_status lss_op_select_bad_dofs(int32_t strategy, int32_t n, const double *score, double p1, double p2, int32_t i1,
+                                  int32_t i2, int32_t *out, int32_t *count)
+{
+    if (n < 0 || (n > 0 && !score) || !count || strategy < 1 || strategy > 3) {
+        g_create_error = "invalid bad-DOF selection arguments";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    return guarded(nullptr, [&]() {
+        const std::vector<double> v(score, score + n);
+        std::vector<int32_t> sel;
+        if (strategy == lss::BADDOF_ELBOW) sel = lss::mas_select_elbow(v);
+        else if (strategy == lss::BADDOF_KMEAN) sel = lss::mas_select_kmean(v, p1, p2, i1, i2);
+        else sel = lss::mas_select_gmm(v, p1, p2, i1, i2);
+        *count = (int32_t)sel.size();
+        if (out) std::copy(sel.begin(), sel.end(), out);
+    });
+}
+

@@ -63,6 +63,9 @@ struct BsrDev {
     const float2 *vals_df = nullptr; // df32 pairs (hi, lo): vals = hi + lo to 2^-48 relative
 };
 
+// per scalar row of the permuted operator: |diagonal|, max |off-diagonal|, l1 norm
+void launch_row_scores(const BsrDev &A, double *diag, double *offmax, double *l1, cudaStream_t s);
+
 // vals[j] = src >= 0 ? csc[src] : 0  (BSR slot gather)
 void launch_gather_values(int64_t count, const int64_t *src, const double *csc, double *vals, float *vals32,
                           cudaStream_t s, float2 *vals_df = nullptr);

@@ -169,6 +169,14 @@ struct Params {
     int outer_spmv = 0;             // PCG's A p: 0 auto (df32 iff mixed), 1 FP64, 2 df32 (FP32-pipe double-float)
     int precond_residual = 0;       // mixed r - A z: 0 auto (df32 on stiff rows), 1 FP32, 2 df32 everywhere
     bool mas_bf16_offdiag = false;  // mixed: BF16 storage of the level-0 off-diagonal inverse tiles
+    // MASSolver's bad-DOF selections (linear-solver-spec.json "/MAS/bad_dof_*"
+    // keys and defaults) in place of GPUHybrid's GMM + post-processing
+    int bad_dof_strategy = 0;       // BadDofStrategy: 0 GPUHybrid, 1 elbow, 2 kmean, 3 gmm
+    double kmeans_search_fraction = 0.2, kmeans_jump_threshold = 10.0;
+    int kmeans_max_iterations = 32, kmeans_expand_neighbors = 128;
+    double mas_gmm_jump_threshold = 10.0, mas_gmm_tol = 1e-3;
+    int mas_gmm_max_iterations = 20, mas_gmm_expand_neighbors = 16;
+    int bad_dof_max_block = 20000;  // components above this (dense inverse) are dropped
     bool multiplicative = true;     // GPUHybrid composition; false = MASSolver additive form
     int max_coarse_levels = 4;      // MAS_MAX_COARSE_LEVEL (MASPreconditioner.hpp:11); <= 6
     double mas_damping = 0.0;       // omega of MAS in the multiplicative form; <= 0: automatic

@@ -203,6 +203,30 @@ Params parse_params(const char *json, const Params &base)
                 if (v.kind != JValue::Str || (v.str != "fp32" && v.str != "bf16"))
                     fail(LSS_ERR_INVALID_ARGUMENT, "gb300.mas_offdiag must be \"fp32\" or \"bf16\"");
                 p.mas_bf16_offdiag = v.str == "bf16";
+            } else if (k == "bad_dof_strategy") {
+                if (v.kind != JValue::Str ||
+                    (v.str != "gpuhybrid" && v.str != "elbow" && v.str != "kmean" && v.str != "gmm"))
+                    fail(LSS_ERR_INVALID_ARGUMENT,
+                         "gb300.bad_dof_strategy must be \"gpuhybrid\", \"elbow\", \"kmean\" or \"gmm\"");
+                p.bad_dof_strategy = v.str == "gpuhybrid" ? 0 : (v.str == "elbow" ? 1 : (v.str == "kmean" ? 2 : 3));
+            } else if (k == "bad_dof_kmeans_search_fraction") {
+                p.kmeans_search_fraction = num(v, kc);
+            } else if (k == "bad_dof_kmeans_jump_threshold") {
+                p.kmeans_jump_threshold = num(v, kc);
+            } else if (k == "bad_dof_kmeans_max_iterations") {
+                p.kmeans_max_iterations = integer(v, kc);
+            } else if (k == "bad_dof_kmeans_expand_neighbors") {
+                p.kmeans_expand_neighbors = integer(v, kc);
+            } else if (k == "bad_dof_gmm_jump_threshold") {
+                p.mas_gmm_jump_threshold = num(v, kc);
+            } else if (k == "bad_dof_gmm_tol") {
+                p.mas_gmm_tol = num(v, kc);
+            } else if (k == "bad_dof_gmm_max_iterations") {
+                p.mas_gmm_max_iterations = integer(v, kc);
+            } else if (k == "bad_dof_gmm_expand_neighbors") {
+                p.mas_gmm_expand_neighbors = integer(v, kc);
+            } else if (k == "bad_dof_max_block") {
+                p.bad_dof_max_block = integer(v, kc);
             } else if (k == "outer_spmv") {
                 if (v.kind != JValue::Str || (v.str != "auto" && v.str != "fp64" && v.str != "df32"))
                     fail(LSS_ERR_INVALID_ARGUMENT, "gb300.outer_spmv must be \"auto\", \"fp64\" or \"df32\"");
@@ -231,6 +255,8 @@ Params parse_params(const char *json, const Params &base)
     if (p.max_coarse_levels < 1 || p.max_coarse_levels > 6)
         fail(LSS_ERR_INVALID_ARGUMENT, "gb300.max_coarse_levels must be in [1, 6]");
     if (p.check_every < 1) p.check_every = 1;
+    if (!(p.kmeans_search_fraction > 0.0) || p.kmeans_search_fraction > 1.0)
+        fail(LSS_ERR_INVALID_ARGUMENT, "gb300.bad_dof_kmeans_search_fraction must be in (0, 1]");
     if (p.spmv_lanes != 0 && (p.spmv_lanes < 1 || p.spmv_lanes > 32 || (p.spmv_lanes & (p.spmv_lanes - 1))))
         fail(LSS_ERR_INVALID_ARGUMENT, "gb300.spmv_lanes must be 0 (autotune) or a power of two <= 32");
     if (p.omega_iters < 1 || p.omega_iters > 64) fail(LSS_ERR_INVALID_ARGUMENT, "gb300.omega_iters must be in [1, 64]");

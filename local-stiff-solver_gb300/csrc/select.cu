@@ -296,6 +296,34 @@ __global__ void __launch_bounds__(256) gershgorin_kernel(int bd, const int32_t *
     }
 }
 
+// Per scalar row of the permuted operator (BSR block order, then column within
+// the block, as MASSolver's BSR traversal): |diagonal|, the largest |off-
+// diagonal| and the l1 norm (BadDOFPreconditioner.cu:110-145,
+// BadDofKMeanPreconditioner.cu:187-226, BadDofGMMPreconditioner.cu:285-310).
+template <int BD>
+__global__ void row_scores_kernel(BsrDev A, double *__restrict__ diag, double *__restrict__ offmax,
+                                  double *__restrict__ l1)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (int64_t)A.nb * BD) return;
+    const int32_t i = (int32_t)(s / BD), r = (int32_t)(s % BD);
+    const int32_t b = A.rows[i], len = A.rows[i + 1] - b;
+    const double *v = A.vals + (int64_t)b * BD * BD;
+    double d = 0.0, mx = 0.0, sum = 0.0;
+    for (int32_t l = 0; l < len; ++l) {
+        const int32_t j = A.cols[b + l];
+        for (int k = 0; k < BD; ++k) {
+            const double a = fabs(v[(int64_t)(r * BD + k) * len + l]);
+            sum += a;
+            if (j == i && k == r) d = a;
+            else mx = fmax(mx, a);
+        }
+    }
+    diag[s] = d;
+    offmax[s] = mx;
+    l1[s] = sum;
+}
+
 }  // namespace
 
 void launch_gershgorin(int nb, int bd, const int32_t *rows, const int32_t *cols, const double *vals,
@@ -350,6 +378,17 @@ void launch_gmm_scatter(int32_t n, const double *rn, const GmmState *st, double 
 {
     const int grid = (int)((n + 255) / 256);
     if (grid > 0) scatter_kernel<<<grid, 256, 0, s>>>(n, rn, st, threshold, block_offset, out);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_row_scores(const BsrDev &A, double *diag, double *offmax, double *l1, cudaStream_t s)
+{
+    const int64_t n = (int64_t)A.nb * A.bd;
+    if (n == 0) return;
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    if (A.bd == 1) row_scores_kernel<1><<<grid, 256, 0, s>>>(A, diag, offmax, l1);
+    else if (A.bd == 2) row_scores_kernel<2><<<grid, 256, 0, s>>>(A, diag, offmax, l1);
+    else row_scores_kernel<3><<<grid, 256, 0, s>>>(A, diag, offmax, l1);
     LSS_LAUNCH_CHECK();
 }
 

@@ -12,6 +12,8 @@
 //   device stop flag once per chunk.
 #include "solver.hpp"
 
+#include "baddof.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -329,6 +331,10 @@ void HybridSolver::select_stiff(const CscView &A)
     gmm_sel_.clear();
     subs_.clear();
     if (!p_.do_hybrid) return;
+    if (p_.bad_dof_strategy != BADDOF_GPUHYBRID) {
+        select_stiff_mas(A);
+        return;
+    }
     std::vector<int32_t> sel;
     if (p_.select_l1) {
         const int32_t n = A.n;
@@ -401,6 +407,64 @@ void HybridSolver::select_stiff(const CscView &A)
     // selected DOF; its inverse is block diagonal over the connected components,
     // so factoring the components separately applies the same operator.
     subs_ = decompose_subdomains(A, sel, p_.decompose ? (int64_t)p_.max_sub : INT64_MAX);
+}
+
+// MASSolver's bad-DOF selections (MASSolver.cu:266-290 with
+// BadDOFPreconditioner / BadDofKMeanPreconditioner / BadDofGMMPreconditioner):
+// scores per scalar row of the permuted operator on the device, selection on
+// the host in that order (the expansion window counts partition-order
+// positions), then one factorization of the selected set -- here its
+// connected components, the same operator (components above
+// bad_dof_max_block DOFs, beyond a dense inverse, are dropped).
+void HybridSolver::select_stiff_mas(const CscView &A)
+{
+    const int64_t n = n_vec();
+    const std::vector<double> score = row_scores(p_.bad_dof_strategy);
+    std::vector<int32_t> pos;
+    switch (p_.bad_dof_strategy) {
+    case BADDOF_ELBOW: pos = mas_select_elbow(score); break;
+    case BADDOF_KMEAN:
+        pos = mas_select_kmean(score, p_.kmeans_search_fraction, p_.kmeans_jump_threshold, p_.kmeans_max_iterations,
+                               p_.kmeans_expand_neighbors);
+        break;
+    default:
+        pos = mas_select_gmm(score, p_.mas_gmm_jump_threshold, p_.mas_gmm_tol, p_.mas_gmm_max_iterations,
+                             p_.mas_gmm_expand_neighbors);
+        break;
+    }
+    const int32_t bd = pat_.bd;
+    std::vector<int32_t> old_of(pat_.nb);
+    for (int32_t b = 0; b < pat_.nb; ++b) old_of[pat_.part.perm[b]] = b;
+    std::vector<int32_t> sel;
+    sel.reserve(pos.size());
+    for (int32_t p : pos)
+        if (p >= 0 && p < n) sel.push_back(old_of[p / bd] * bd + p % bd);
+    std::sort(sel.begin(), sel.end());
+    gmm_sel_ = sel;
+    stats_["bad_dof_selected"] = (double)sel.size();
+    if (sel.empty()) return;
+    subs_ = decompose_subdomains(A, sel, (int64_t)p_.bad_dof_max_block);
+}
+
+// kind 1: |diagonal|, 2: max |off-diagonal|, 3: l1 norm; per scalar row of the
+// permuted operator
+std::vector<double> HybridSolver::row_scores(int kind)
+{
+    const int64_t n = n_vec();
+    DBuf<double> diag(n), offmax(n), l1(n);
+    launch_row_scores(A_, diag.data(), offmax.data(), l1.data(), stream_);
+    std::vector<double> out = (kind == BADDOF_ELBOW ? diag : (kind == BADDOF_KMEAN ? offmax : l1)).download(stream_);
+    LSS_CUDA(cudaStreamSynchronize(stream_));
+    return out;
+}
+
+void HybridSolver::op_row_scores(double *diag, double *offmax, double *l1)
+{
+    if (!factorized_) fail(LSS_ERR_NOT_FACTORIZED, "no factorized operator");
+    const std::vector<double> a = row_scores(BADDOF_ELBOW), b = row_scores(BADDOF_KMEAN), c = row_scores(BADDOF_GMM);
+    std::copy(a.begin(), a.end(), diag);
+    std::copy(b.begin(), b.end(), offmax);
+    std::copy(c.begin(), c.end(), l1);
 }
 
 void HybridSolver::setup_stiff()

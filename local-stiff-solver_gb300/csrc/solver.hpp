@@ -39,6 +39,7 @@ public:
     // operator-level access (original ordering, host pointers)
     void op_spmv(const double *x, double *y);
     void op_spmv_outer(const double *x, double *y);
+    void op_row_scores(double *diag, double *offmax, double *l1);
     void op_mas(const double *r, double *z);
     void op_precond(const double *r, double *z);
     void op_time(int kind, int reps, double *ms, double *bytes);
@@ -71,6 +72,8 @@ private:
     };
     void factorize_common();
     void select_stiff(const CscView &A);
+    void select_stiff_mas(const CscView &A);
+    std::vector<double> row_scores(int kind);
     void setup_stiff();
     void setup_mas();
     void ensure_vectors();

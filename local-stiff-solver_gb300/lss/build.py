@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unknown-pragmas"]
 LIB_SOURCES = ["select.cu", "pcg.cu", "mas.cu", "stiff.cu", "noalloc.cu", "solver.cpp", "capi.cpp", "params.cpp",
-               "postproc.cpp", "partition.cpp", "pattern.cpp"]
+               "postproc.cpp", "partition.cpp", "pattern.cpp", "baddof.cpp"]
 
 
 def _nvcc():
@@ -56,7 +56,9 @@ def build(force: bool = False, verbose: bool = False) -> dict:
         o = os.path.join(_paths.BUILD_DIR, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            extra = ["-x", "cu"] if src.endswith(".cu") else []
+            # host code: no FMA contraction, so that x86 and aarch64 builds (and
+            # the oracle, built the same way) round every expression alike
+            extra = ["-x", "cu"] if src.endswith(".cu") else ["-Xcompiler", "-ffp-contract=off"]
             jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *extra, "-I", _paths.CSRC, "-I", _paths.INCLUDE, "-c", s,
                          "-o", o])
     if jobs:

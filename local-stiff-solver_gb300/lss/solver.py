@@ -38,7 +38,7 @@ EXPORTS = [
     "lss_grad_A_pattern_device", "lss_grad_params_device", "lss_selected_dofs", "lss_gmm_selection", "lss_subdomains",
     "lss_partition", "lss_op_row_l1_norms", "lss_op_spmv", "lss_op_spmv_outer", "lss_op_mas_apply", "lss_op_precond",
     "lss_op_time", "lss_set_memory_cap", "lss_gmm_select_device_noalloc", "lss_solve_batched_device",
-    "lss_factorize_batched_device",
+    "lss_factorize_batched_device", "lss_op_row_scores", "lss_op_select_bad_dofs",
 ]
 
 
@@ -95,6 +95,9 @@ def load(path: str | None = None):
     L.lss_solve_batched_device.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(vp), C.POINTER(vp), C.c_int32,
                                            C.c_int32, _i32p]
     L.lss_factorize_batched_device.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(vp), C.c_int32]
+    L.lss_op_row_scores.argtypes = [vp, _f64p, _f64p, _f64p]
+    L.lss_op_select_bad_dofs.argtypes = [C.c_int32, C.c_int32, _f64p, C.c_double, C.c_double, C.c_int32,
+                                         C.c_int32, _i32p, _i32p]
     L.lss_gmm_select_device_noalloc.argtypes = [C.c_int32, C.c_int64, vp, vp, C.c_double, C.c_double, C.c_int32,
                                                 vp, vp, vp]
     for name in EXPORTS:
@@ -169,6 +172,26 @@ def factorize_batched_device(solvers, d_values, threads: int = 0) -> None:
     st = L.lss_factorize_batched_device(S, count, V, threads)
     if st:
         raise LssError(st, L.lss_last_error(None).decode())
+
+
+BAD_DOF_STRATEGIES = {"elbow": 1, "kmean": 2, "gmm": 3}
+
+
+def select_bad_dofs(strategy: str, score, p1=0.0, p2=0.0, i1=0, i2=0) -> np.ndarray:
+    """MASSolver's bad-DOF selection (host code of the library) on a score
+    vector: "elbow" (|diagonal|), "kmean" (p1 search fraction, p2 jump
+    threshold, i1 iterations, i2 expand neighbours) or "gmm" (p1 jump
+    threshold, p2 tol, i1 iterations, i2 expand neighbours).  Positions in the
+    reference's output order."""
+    L = load()
+    v = np.ascontiguousarray(score, np.float64)
+    out = np.empty(max(len(v), 1), np.int32)
+    cnt = C.c_int32(0)
+    st = L.lss_op_select_bad_dofs(BAD_DOF_STRATEGIES[strategy], len(v), _p(v, _f64p), p1, p2, i1, i2,
+                                  _p(out, _i32p), C.byref(cnt))
+    if st:
+        raise LssError(st, L.lss_last_error(None).decode())
+    return out[:cnt.value].copy()
 
 
 class Solver:
@@ -325,6 +348,14 @@ class Solver:
         y = np.empty_like(x)
         self._check(self._L.lss_op_spmv(self._h, _p(x, _f64p), _p(y, _f64p)))
         return y
+
+    def row_scores(self):
+        """(|diagonal|, max |off-diagonal|, l1 norm) per scalar row of the
+        permuted operator (partition order)."""
+        n = self._n
+        d, o, l = np.empty(n), np.empty(n), np.empty(n)
+        self._check(self._L.lss_op_row_scores(self._h, _p(d, _f64p), _p(o, _f64p), _p(l, _f64p)))
+        return d, o, l
 
     def spmv_outer(self, x):
         """A x with the PCG's own product (FP64 or double-float, gb300.outer_spmv)."""

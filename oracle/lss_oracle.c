@@ -1161,3 +1161,221 @@ void lsso_solver_destroy(lsso_solver *s)
     free(s->t0); free(s->t1); free(s->t2); free(s->t3); free(s->t4);
     free(s);
 }
+
+/* ===================================================================== */
+/* MAS-side bad-DOF selections                                            */
+/* ===================================================================== */
+
+/* index sort by value with ties broken by index (qsort: single-threaded use) */
+static const double *g_key;
+static int g_desc;
+static int cmp_by_key(const void *a, const void *b)
+{
+    const int32_t i = *(const int32_t *)a, j = *(const int32_t *)b;
+    const double x = g_key[i], y = g_key[j];
+    if (x < y) return g_desc ? 1 : -1;
+    if (x > y) return g_desc ? -1 : 1;
+    return (i > j) - (i < j);
+}
+static int32_t *sorted_positions(int32_t n, const double *key, int desc)
+{
+    int32_t *order = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    for (int32_t i = 0; i < n; ++i) order[i] = i;
+    g_key = key;
+    g_desc = desc;
+    qsort(order, (size_t)n, sizeof(int32_t), cmp_by_key);
+    return order;
+}
+
+/* positions of `hit` (visited in `visit` order), each widened by +-w; first-seen order */
+static int32_t widen(int32_t n, int32_t m, const int32_t *visit, const unsigned char *hit, int32_t w, int32_t *out)
+{
+    int32_t k = 0;
+    if (w <= 0) {
+        for (int32_t t = 0; t < m; ++t)
+            if (hit[t]) out[k++] = visit[t];
+        return k;
+    }
+    unsigned char *mask = (unsigned char *)xcalloc((size_t)(n > 0 ? n : 1), 1);
+    for (int32_t t = 0; t < m; ++t) {
+        if (!hit[t]) continue;
+        const int32_t pos = visit[t];
+        const int32_t lo = pos - w < 0 ? 0 : pos - w, hi = pos + w > n - 1 ? n - 1 : pos + w;
+        for (int32_t j = lo; j <= hi; ++j)
+            if (!mask[j]) {
+                mask[j] = 1;
+                out[k++] = j;
+            }
+    }
+    free(mask);
+    return k;
+}
+
+/* BadDOFPreconditioner.cu:61-100 */
+int32_t lsso_mas_select_elbow(int32_t n, const double *diag_abs, int32_t *out)
+{
+    if (n <= 0) return 0;
+    int32_t *order = sorted_positions(n, diag_abs, 0);
+    int32_t cut = 0;
+    if (n > 1) {
+        const double lo = log(diag_abs[order[0]]), hi = log(diag_abs[order[n - 1]]);
+        double best = -1.0;
+        for (int32_t i = 0; i < n; ++i) {
+            const double chord = (hi - lo) / (n - 1.0) * i + lo;
+            const double dev = fabs(chord - log(diag_abs[order[i]]));
+            if (dev > best) {
+                best = dev;
+                cut = i;
+            }
+        }
+    }
+    int32_t k = 0;
+    for (int32_t i = cut; i < n; ++i) out[k++] = order[i];
+    free(order);
+    return k;
+}
+
+/* BadDofKMeanPreconditioner.cu:63-172 (the assignment writes a value to the
+ * cluster of the other centre, and a centre moves only with >= 1 (cluster 0)
+ * or >= 2 (cluster 1) members: both as in the reference) */
+int32_t lsso_mas_select_kmean(int32_t n, const double *v, double search_fraction, double jump_threshold,
+                              int32_t max_iterations, int32_t expand_neighbors, int32_t *out)
+{
+    if (n < 2) return 0;
+    int32_t *order = sorted_positions(n, v, 1);
+    int32_t m = (int32_t)(n * search_fraction);
+    if (m < 2) m = 2;
+    if (m > n) m = n;
+    double c0 = v[order[0]], c1 = v[order[m - 1]];
+    for (int32_t it = 0; it < max_iterations; ++it) {
+        double s0 = 0.0, s1 = 0.0;
+        int32_t k0 = 0, k1 = 0;
+        for (int32_t t = 0; t < m; ++t) {
+            const double x = v[order[t]];
+            if (fabs(x - c0) < fabs(x - c1)) {
+                ++k1;
+                s1 += x;
+            } else {
+                ++k0;
+                s0 += x;
+            }
+        }
+        const double n0 = k0 > 0 ? s0 / k0 : c0;
+        const double n1 = k1 > 1 ? s1 / k1 : c1;
+        if (n0 == c0 && n1 == c1) break;
+        c0 = n0;
+        c1 = n1;
+    }
+    if (c0 < c1) {
+        const double t = c0;
+        c0 = c1;
+        c1 = t;
+    }
+    const double ratio = c0 / c1;
+    int32_t k = 0;
+    if (!isnan(ratio) && !(ratio < jump_threshold)) {
+        const double sep = 0.5 * (c0 + c1);
+        unsigned char *hit = (unsigned char *)xmalloc((size_t)m);
+        for (int32_t t = 0; t < m; ++t) hit[t] = v[order[t]] > sep;
+        k = widen(n, m, order, hit, expand_neighbors, out);
+        free(hit);
+    }
+    free(order);
+    return k;
+}
+
+static double rel_change(double now, double before)
+{
+    const double d = fabs(before) > 1e-300 ? fabs(before) : 1e-300;
+    return fabs(now - before) / d;
+}
+static double log_normal_density(double x, double mean, double var)
+{
+    const double two_pi = 2.0 * 3.141592653589793238462643383279502884;
+    return -0.5 * log(two_pi * var) - 0.5 * (x - mean) * (x - mean) / var;
+}
+
+/* BadDofGMMPreconditioner.cu:73-255 */
+int32_t lsso_mas_select_gmm(int32_t n, const double *x, double jump_threshold, double tol, int32_t max_iterations,
+                            int32_t expand_neighbors, int32_t *out)
+{
+    if (n < 2) return 0;
+    double sum = 0.0;
+    for (int32_t i = 0; i < n; ++i) sum += x[i];
+    const double gmean = sum / n;
+    double vs = 0.0;
+    for (int32_t i = 0; i < n; ++i) {
+        const double d = x[i] - gmean;
+        vs += d * d;
+    }
+    const double gvar = vs / n;
+    double m0 = x[0], m1 = x[0];
+    for (int32_t i = 1; i < n; ++i) {
+        if (x[i] < m0) m0 = x[i];
+        if (x[i] > m1) m1 = x[i];
+    }
+    const double var_reg = 1e-6;
+    double v0 = gvar > var_reg ? gvar : var_reg, v1 = v0, w0 = 0.5, w1 = 0.5;
+    if (m0 == m1 || !isfinite(gvar)) return 0;
+    double *g0 = (double *)xcalloc((size_t)n, sizeof(double));
+    double *g1 = (double *)xcalloc((size_t)n, sizeof(double));
+    const int32_t iters = max_iterations > 1 ? max_iterations : 1;
+    for (int32_t it = 0; it < iters; ++it) {
+        const double lw0 = log(w0 > DBL_MIN ? w0 : DBL_MIN), lw1 = log(w1 > DBL_MIN ? w1 : DBL_MIN);
+        for (int32_t i = 0; i < n; ++i) {
+            const double a = lw0 + log_normal_density(x[i], m0, v0);
+            const double b = lw1 + log_normal_density(x[i], m1, v1);
+            const double mx = a > b ? a : b;
+            const double lt = mx + log(exp(a - mx) + exp(b - mx));
+            g0[i] = exp(a - lt);
+            g1[i] = exp(b - lt);
+        }
+        double s0 = 0.0, s1 = 0.0;
+        for (int32_t i = 0; i < n; ++i) {
+            s0 += g0[i];
+            s1 += g1[i];
+        }
+        if (s0 <= 0.0 || s1 <= 0.0) break;
+        w0 = s0 / n;
+        w1 = s1 / n;
+        const double pm0 = m0, pm1 = m1, pv0 = v0, pv1 = v1;
+        m0 = 0.0;
+        m1 = 0.0;
+        for (int32_t i = 0; i < n; ++i) {
+            m0 += g0[i] * x[i];
+            m1 += g1[i] * x[i];
+        }
+        m0 /= s0;
+        m1 /= s1;
+        v0 = 0.0;
+        v1 = 0.0;
+        for (int32_t i = 0; i < n; ++i) {
+            const double d0 = x[i] - m0, d1 = x[i] - m1;
+            v0 += g0[i] * d0 * d0;
+            v1 += g1[i] * d1 * d1;
+        }
+        v0 = v0 / s0 + var_reg;
+        v1 = v1 / s1 + var_reg;
+        if (rel_change(m0, pm0) < tol && rel_change(m1, pm1) < tol && rel_change(v0, pv0) < tol &&
+            rel_change(v1, pv1) < tol)
+            break;
+    }
+    const int high0 = fabs(m0) > fabs(m1);
+    const double ratio = high0 ? fabs(m0) / fabs(m1) : fabs(m1) / fabs(m0);
+    int32_t k = 0;
+    if (!isnan(ratio) && !(ratio < jump_threshold)) {
+        int32_t *visit = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)n);
+        unsigned char *hit = (unsigned char *)xmalloc((size_t)n);
+        for (int32_t i = 0; i < n; ++i) {
+            visit[i] = i;
+            hit[i] = high0 ? (g0[i] > g1[i]) : (g1[i] > g0[i]);
+        }
+        k = widen(n, n, visit, hit, expand_neighbors, out);
+        free(visit);
+        free(hit);
+    }
+    free(g0);
+    free(g1);
+    return k;
+}
+

@@ -144,6 +144,28 @@ void lsso_solver_destroy(lsso_solver *s);
 int32_t lsso_greedy_partition(int32_t nb, const int32_t *rows, const int32_t *cols,
                               int32_t max_part, int32_t *part_of);
 
+/* ---- MAS-side bad-DOF selections (MASSolver use_bad_dof_precond) ----------
+ * Scores are per scalar row in the partition order of the permuted operator;
+ * the results are positions in that order (not sorted: the reference's own
+ * output order).  Sorting ties break by position. */
+
+/* Elbow of the ascending log|diag| curve against its chord: the positions from
+ * the largest deviation on (BadDOFPreconditioner.cu:61-100). */
+int32_t lsso_mas_select_elbow(int32_t n, const double *diag_abs, int32_t *out);
+
+/* 2-means (Lloyd) on the search_fraction largest max|off-diagonal| scores, the
+ * centroid ratio test, positions above the midpoint, each widened by
+ * +-expand_neighbors positions (BadDofKMeanPreconditioner.cu:63-172). */
+int32_t lsso_mas_select_kmean(int32_t n, const double *offdiag_max, double search_fraction,
+                              double jump_threshold, int32_t max_iterations, int32_t expand_neighbors,
+                              int32_t *out);
+
+/* Two-component GMM by EM on l1 row norms, the high/low mean ratio test,
+ * positions of the high component, each widened by +-expand_neighbors
+ * (BadDofGMMPreconditioner.cu:73-255). */
+int32_t lsso_mas_select_gmm(int32_t n, const double *l1, double jump_threshold, double tol,
+                            int32_t max_iterations, int32_t expand_neighbors, int32_t *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,6 +120,14 @@ def lib():
         L.lsso_solver_destroy.argtypes = [C.c_void_p]
         L.lsso_greedy_partition.argtypes = [C.c_int32, _i32p, _i32p, C.c_int32, _i32p]
         L.lsso_greedy_partition.restype = C.c_int32
+        L.lsso_mas_select_elbow.argtypes = [C.c_int32, _f64p, _i32p]
+        L.lsso_mas_select_elbow.restype = C.c_int32
+        L.lsso_mas_select_kmean.argtypes = [C.c_int32, _f64p, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                            _i32p]
+        L.lsso_mas_select_kmean.restype = C.c_int32
+        L.lsso_mas_select_gmm.argtypes = [C.c_int32, _f64p, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                          _i32p]
+        L.lsso_mas_select_gmm.restype = C.c_int32
         _lib = L
     return _lib
 
@@ -155,6 +163,24 @@ def c_gmm_select(rn, jump_threshold=100.0, tol=1e-3, max_iterations=20):
                               _p(sel, _i32p), C.byref(st))
     stats = {f: getattr(st, f) for f, _ in GmmStats._fields_}
     return sel[:k].copy(), stats
+
+
+def c_mas_select(strategy, score, p1=0.0, p2=0.0, i1=0, i2=0):
+    """MASSolver's bad-DOF selections (lss_oracle.c): "elbow" on |diagonal|
+    (BadDOFPreconditioner.cu:61-100), "kmean" (p1 search fraction, p2 jump
+    threshold, i1 iterations, i2 expand neighbours; BadDofKMeanPreconditioner.cu:63-172),
+    "gmm" (p1 jump threshold, p2 tol, i1 iterations, i2 expand neighbours;
+    BadDofGMMPreconditioner.cu:73-255).  Positions in the reference's output order."""
+    v = np.ascontiguousarray(score, np.float64)
+    out = np.empty(max(len(v), 1), np.int32)
+    L = lib()
+    if strategy == "elbow":
+        k = L.lsso_mas_select_elbow(len(v), _p(v, _f64p), _p(out, _i32p))
+    elif strategy == "kmean":
+        k = L.lsso_mas_select_kmean(len(v), _p(v, _f64p), p1, p2, i1, i2, _p(out, _i32p))
+    else:
+        k = L.lsso_mas_select_gmm(len(v), _p(v, _f64p), p1, p2, i1, i2, _p(out, _i32p))
+    return out[:k].copy()
 
 
 def c_filter(A, sel, min_size=1, max_size=10000000, cond=100.0):

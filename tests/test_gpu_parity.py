@@ -307,6 +307,45 @@ def test_large_stiff_subdomain(precision, built):
     assert s.get_info()["status"] == "converged_rel"
 
 
+@pytest.mark.parametrize("strategy", ["elbow", "kmean", "gmm"])
+def test_mas_bad_dof_strategies(strategy, elast20):
+    """MASSolver's bad-DOF selections in place of GPUHybrid's: the device
+    scores equal numpy's on the permuted rows (|diagonal| and max
+    |off-diagonal| exactly, the l1 norm to 1e-13), the selection equals the C
+    oracle's on those scores (mapped back through the partition), and the
+    solve reaches the parity bar."""
+    from oracle import oracle as O
+    A = elast20[0]
+    b = elast20[1]
+    gb = {"bad_dof_strategy": strategy, "bad_dof_max_block": 3000}
+    params = {"block_size": 3, "relative_tolerance": 1e-8}
+    s = _solver(params, gb)
+    s.factorize(A)
+    d, o, l1 = s.row_scores()
+    perm, _ = s.partition()
+    n, bd = A.shape[0], 3
+    Ar = _outer_as_row(A)
+    absA = abs(Ar).tocsr()
+    dg = abs(Ar.diagonal())
+    off = absA - sp.diags(dg)
+    off.eliminate_zeros()
+    offmax = np.asarray(off.max(axis=1).todense()).ravel()
+    l1_ref = np.asarray(absA.sum(axis=1)).ravel()
+    pos = perm[np.arange(n) // bd] * bd + np.arange(n) % bd
+    np.testing.assert_array_equal(d[pos], dg)
+    np.testing.assert_array_equal(o[pos], offmax)
+    assert np.all(np.abs(l1[pos] - l1_ref) <= 1e-13 * l1_ref)
+    score = {"elbow": d, "kmean": o, "gmm": l1}[strategy]
+    args = {"elbow": (0.0, 0.0, 0, 0), "kmean": (0.2, 10.0, 32, 128), "gmm": (10.0, 1e-3, 20, 16)}[strategy]
+    sel_pos = O.c_mas_select(strategy, score, *args)
+    old_of = np.empty(len(perm), np.int64)
+    old_of[perm] = np.arange(len(perm))
+    expect = np.sort(old_of[sel_pos // bd] * bd + sel_pos % bd)
+    np.testing.assert_array_equal(s.gmm_selection(), expect)
+    x = s.solve(b)
+    _check_solution(A, b, x)
+
+
 def _outer_as_row(A):
     """The operator the solver applies: outer index = row (GPUHybrid.cu:203-209)."""
     A = A.tocsc()
