@@ -9,14 +9,22 @@ result feeds Solver.set_problematic_dofs.
 """
 from __future__ import annotations
 
+import warnings
+
 import numpy as np
+
+
+def _mmread(path):
+    import scipy.io
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", DeprecationWarning)  # scipy's spmatrix default change
+        return scipy.io.mmread(path)
 
 
 def read_matrix(path: str):
     """MatrixMarket matrix as a canonical scipy CSC matrix (float64)."""
-    import scipy.io
     import scipy.sparse as sp
-    A = sp.csc_matrix(scipy.io.mmread(path), dtype=np.float64)
+    A = sp.csc_matrix(_mmread(path), dtype=np.float64)
     A.sum_duplicates()
     A.sort_indices()
     return A
@@ -24,8 +32,7 @@ def read_matrix(path: str):
 
 def read_vector(path: str, n: int | None = None) -> np.ndarray:
     """MatrixMarket vector (dense array or one-column coordinate file)."""
-    import scipy.io
-    v = scipy.io.mmread(path)
+    v = _mmread(path)
     v = np.asarray(v.todense() if hasattr(v, "todense") else v, dtype=np.float64).ravel()
     if n is not None and v.size != n:
         raise ValueError(f"vector of size {v.size}, expected {n}")
