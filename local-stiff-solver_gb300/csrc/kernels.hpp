@@ -71,9 +71,9 @@ void launch_gather_values(int64_t count, const int64_t *src, const double *csc, 
                           cudaStream_t s, float2 *vals_df = nullptr);
 // y = A x  (FP64)
 void launch_spmv(const BsrDev &A, const double *x, double *y, const int *done, cudaStream_t s);
-// y = r - A x, FP64 (fp32 == false) or with the FP32 operator copy (fp32 == true)
-void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, double *y, bool fp32,
-                          const int *done, cudaStream_t s);
+// y = r - A x in FP64
+void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, double *y, const int *done,
+                          cudaStream_t s);
 // y32 = r32 - A x32 in FP32 with the FP32 operator copy (the mixed
 // preconditioner's residual); block rows flagged in `precise` (optional) are
 // evaluated in double-float from r64, the df32 values and x32 + x_lo.

@@ -441,18 +441,12 @@ void launch_spmv(const BsrDev &A, const double *x, double *y, const int *done, c
     LSS_LAUNCH_CHECK();
 }
 
-void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, double *y, bool fp32, const int *done,
+void launch_residual_spmv(const BsrDev &A, const double *r, const double *x, double *y, const int *done,
                           cudaStream_t s)
 {
-    if (fp32) {
-        if (A.bd == 1) residual_dispatch<1, float, float, double>(A, A.vals32, r, x, y, done, s);
-        else if (A.bd == 2) residual_dispatch<2, float, float, double>(A, A.vals32, r, x, y, done, s);
-        else residual_dispatch<3, float, float, double>(A, A.vals32, r, x, y, done, s);
-    } else {
-        if (A.bd == 1) residual_dispatch<1, double, double, double>(A, A.vals, r, x, y, done, s);
-        else if (A.bd == 2) residual_dispatch<2, double, double, double>(A, A.vals, r, x, y, done, s);
-        else residual_dispatch<3, double, double, double>(A, A.vals, r, x, y, done, s);
-    }
+    if (A.bd == 1) residual_dispatch<1, double, double, double>(A, A.vals, r, x, y, done, s);
+    else if (A.bd == 2) residual_dispatch<2, double, double, double>(A, A.vals, r, x, y, done, s);
+    else residual_dispatch<3, double, double, double>(A, A.vals, r, x, y, done, s);
     LSS_LAUNCH_CHECK();
 }
 

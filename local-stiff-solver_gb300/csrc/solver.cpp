@@ -657,7 +657,7 @@ void HybridSolver::precond(const double *r, double *z, int dot_mode, const float
         mas_apply(r, z, false, nullptr, 0, omega_);
         launch_stiff_gather(A_, stiff_, r, z, true, done, stream_);
         launch_stiff_apply(stiff_, p_.float_subdomains, z, done, stream_);
-        launch_residual_spmv(A_, r, z, d_w_.data(), false, done, stream_);
+        launch_residual_spmv(A_, r, z, d_w_.data(), done, stream_);
         mas_apply(d_w_.data(), z, true, r, dot_mode, omega_);
         return;
     }
@@ -784,7 +784,7 @@ void HybridSolver::run_pcg()
     double res2 = 0.0, prev_res2 = INFINITY;
     for (int attempt = 0;; ++attempt) {
         // r = b - A x; z = M r; p = z; gamma = r.z   (GPUHybrid.cu:1441-1451)
-        launch_residual_spmv(A_, d_b_.data(), d_x_.data(), d_r_.data(), false, nullptr, stream_);
+        launch_residual_spmv(A_, d_b_.data(), d_x_.data(), d_r_.data(), nullptr, stream_);
         if (p_.max_iter > 0) {
             precond(d_r_.data(), d_z_.data(), 1);
             launch_copy(n, d_z_.data(), d_p_.data(), nullptr, stream_);
@@ -799,7 +799,7 @@ void HybridSolver::run_pcg()
             if (h_state_->done) break;
         }
         // true residual (GPUHybrid.cu:383-386)
-        launch_residual_spmv(A_, d_b_.data(), d_x_.data(), d_w_.data(), false, nullptr, stream_);
+        launch_residual_spmv(A_, d_b_.data(), d_x_.data(), d_w_.data(), nullptr, stream_);
         launch_dot(n, d_w_.data(), d_w_.data(), bb_d, gr_, stream_);
         LSS_CUDA(cudaMemcpyAsync(&res2, bb_d, sizeof(double), cudaMemcpyDeviceToHost, stream_));
         LSS_CUDA(cudaMemcpyAsync(h_state_, d_state_.data(), sizeof(PcgState), cudaMemcpyDeviceToHost, stream_));
@@ -1164,7 +1164,7 @@ void HybridSolver::op_time(int kind, int reps, double *ms, double *bytes)
             if (p_.mixed)
                 launch_residual32(A_, d_r32_.data(), d_z32_.data(), d_w32_.data(), nullptr, stream_,
                                   precise_rows_ ? d_precise_.data() : nullptr, d_r_.data(), d_z_lo_.data());
-            else launch_residual_spmv(A_, d_r_.data(), d_p_.data(), d_ap_.data(), false, nullptr, stream_);
+            else launch_residual_spmv(A_, d_r_.data(), d_p_.data(), d_ap_.data(), nullptr, stream_);
             break;
         case 6: outer_spmv_alpha(); break;
         default: iteration(); break;
