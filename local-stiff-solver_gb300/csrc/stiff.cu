@@ -5,7 +5,7 @@
 // (GPUHybrid.cu:993-1411), and applies next_z = z + S^T A_SS^-1 S (r - A z)
 // (dss_precond_iter, GPUHybrid.cu:544-675).  Here every subdomain is gathered
 // into a dense FP64 block, inverted in FP64 by the symmetric sweep (one CTA in
-// shared memory up to 128 DOFs, a blocked multi-CTA sweep beyond), and
+// shared memory up to 160 DOFs, a blocked multi-CTA sweep beyond), and
 // applied as a warp-per-row GEMV fused with the scatter.  The residual rows
 // r - A z are only computed on the stiff rows (the reference forms the full
 // product and gathers it).
@@ -77,7 +77,7 @@ __device__ void sweep_invert_small(double *S, int ld, int N, double *col, double
     }
 }
 
-// one CTA per small subdomain (m <= 128), in place in global storage
+// one CTA per small subdomain (m <= 160), in place in global storage
 __global__ void __launch_bounds__(256) invert_small_kernel(const int32_t *__restrict__ sub_ids,
                                                            const int32_t *__restrict__ off,
                                                            const int64_t *__restrict__ inv_off,
@@ -264,18 +264,31 @@ __global__ void finish_df_kernel(double *__restrict__ S, int64_t count, int *bad
     }
 }
 
+// t_j = r_d (- (A z)_d) for the stiff DOFs d = dofs[j]: one thread per DOF
+// walking its row (a few to a few dozen terms), so no warp reduction -- an FP64
+// shuffle sum would cost the FP64 pipe five full warps per DOF
 template <int BD>
 __global__ void __launch_bounds__(256) gather_kernel(BsrDev A, StiffDev S, const double *__restrict__ r,
                                                      const double *__restrict__ z, bool residual, const int *done)
 {
     if (done && *done) return;
-    const int lane = threadIdx.x & 31;
-    const int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= S.ndof) return;
     const int32_t d = S.dofs[j];
     double t = r[d];
-    if (residual) t -= bsr_scalar_row<BD, double, double>(A.rows, A.cols, A.vals, d / BD, d % BD, z, lane);
-    if (lane == 0) S.t[j] = t;
+    if (residual) {
+        const int32_t i = d / BD, comp = d % BD;
+        const int32_t b = A.rows[i], len = A.rows[i + 1] - b;
+        const double *v = A.vals + (int64_t)b * BD * BD;
+        double acc = 0.0;
+        for (int32_t l = 0; l < len; ++l) {
+            const int32_t c = A.cols[b + l];
+#pragma unroll
+            for (int k = 0; k < BD; ++k) acc += v[(int64_t)(comp * BD + k) * len + l] * z[(int64_t)c * BD + k];
+        }
+        t -= acc;
+    }
+    S.t[j] = t;
 }
 
 template <typename VT>
@@ -328,7 +341,7 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
                          double *inv, int *bad, cudaStream_t s)
 {
     (void)h_inv_off;
-    constexpr int SMALL = 128;
+    constexpr int SMALL = 160;  // (160 * 161 + 320) doubles = 204 KB of shared memory
     std::vector<int32_t> small;
     for (int32_t q = 0; q < nsub; ++q)
         if (h_off[q + 1] - h_off[q] <= SMALL) small.push_back(q);
@@ -392,7 +405,7 @@ void launch_stiff_gather(const BsrDev &A, const StiffDev &S, const double *r, co
                          const int *done, cudaStream_t s)
 {
     if (S.ndof == 0) return;
-    const int grid = (int)(((int64_t)S.ndof * 32 + 255) / 256);
+    const int grid = (int)(((int64_t)S.ndof + 255) / 256);
     switch (A.bd) {
     case 1: gather_kernel<1><<<grid, 256, 0, s>>>(A, S, r, z, residual, done); break;
     case 2: gather_kernel<2><<<grid, 256, 0, s>>>(A, S, r, z, residual, done); break;

@@ -286,7 +286,7 @@ def test_mixed_high_contrast_reaches_tolerance(seed, built):
 def test_large_stiff_subdomain(precision, built):
     """A 0.3-radius x1e6 inclusion on a 16^3-node cube makes one stiff
     subdomain of about 2,000 DOFs: the blocked, double-float sweep inverse
-    (blocks above 128 DOFs).  The preconditioner matches the oracle's (exact
+    (blocks above 160 DOFs).  The preconditioner matches the oracle's (exact
     Cholesky of the same block, same partition and damping) to 1e-7 in FP64,
     and the solve reaches the parity bar."""
     from lss import gen
