@@ -366,30 +366,76 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
     int maxm = 0;
     for (int32_t q = 0; q < nsub; ++q) maxm = std::max(maxm, h_off[q + 1] - h_off[q]);
     if (maxm > SMALL) {
-        DBuf<double> Dinv((size_t)SW_T * SW_T);
-        DBuf<float2> P((size_t)maxm * SW_T);
-        for (int32_t q = 0; q < nsub; ++q) {
-            const int m = h_off[q + 1] - h_off[q];
-            if (m <= SMALL) continue;
-            double *Sq = inv + hoff[q];
-            float2 *Wq = reinterpret_cast<float2 *>(Sq);
-            const int64_t mm = (int64_t)m * m;
-            to_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, s>>>(Sq, mm);
-            const unsigned gp = (unsigned)(((int64_t)m * SW_T + 255) / 256);
-            const unsigned gr = (unsigned)((m + 127) / 128);
-            const dim3 gu((m + 31) / 32, (m + 31) / 32);
-            for (int k0 = 0; k0 < m; k0 += SW_T) {
-                const int t = std::min(SW_T, m - k0);
-                blk_diag_df_kernel<<<1, 256, 0, s>>>(Wq, m, k0, t, Dinv.data(), bad);
-                blk_panel_df_kernel<<<gr, 128, 0, s>>>(Wq, m, k0, t, Dinv.data(), P.data());
-                blk_update_df_kernel<<<gu, 256, 0, s>>>(Wq, m, k0, t, P.data());
-                blk_write_df_kernel<<<gp, 256, 0, s>>>(Wq, m, k0, t, P.data(), Dinv.data());
+        // The blocked sweeps of different subdomains are independent chains of
+        // small launches; they run on up to STREAMS_MAX side streams, each with its
+        // own pivot-block and panel scratch, joined back to s by events.  The
+        // largest subdomain goes first to the stream with the least work (m^3).
+        constexpr int STREAMS_MAX = 16;
+        std::vector<int32_t> large;
+        for (int32_t q = 0; q < nsub; ++q)
+            if (h_off[q + 1] - h_off[q] > SMALL) large.push_back(q);
+        std::stable_sort(large.begin(), large.end(), [&](int32_t a, int32_t b) {
+            return h_off[a + 1] - h_off[a] > h_off[b + 1] - h_off[b];
+        });
+        const int ns = std::min<int>(STREAMS_MAX, (int)large.size());
+        std::vector<cudaStream_t> side(ns, nullptr);
+        std::vector<cudaEvent_t> joined(ns, nullptr);
+        cudaEvent_t ready = nullptr;
+        std::vector<DBuf<double>> Dinv;
+        std::vector<DBuf<float2>> P;
+        std::vector<double> load(ns, 0.0);
+        auto release = [&]() {
+            for (cudaEvent_t e : joined)
+                if (e) cudaEventDestroy(e);
+            if (ready) cudaEventDestroy(ready);
+            for (cudaStream_t t : side)
+                if (t) cudaStreamDestroy(t);
+        };
+        try {
+            LSS_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+            LSS_CUDA(cudaEventRecord(ready, s));
+            for (int i = 0; i < ns; ++i) {
+                LSS_CUDA(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking));
+                LSS_CUDA(cudaEventCreateWithFlags(&joined[i], cudaEventDisableTiming));
+                LSS_CUDA(cudaStreamWaitEvent(side[i], ready, 0));
+                Dinv.emplace_back((size_t)SW_T * SW_T);
+                P.emplace_back((size_t)maxm * SW_T);
             }
-            mirror_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, s>>>(Wq, m);
-            finish_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, s>>>(Sq, mm, bad);
-            LSS_LAUNCH_CHECK();
+            for (int32_t q : large) {
+                const int m = h_off[q + 1] - h_off[q];
+                const int i = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+                load[i] += (double)m * m * m;
+                const cudaStream_t t = side[i];
+                double *Sq = inv + hoff[q];
+                float2 *Wq = reinterpret_cast<float2 *>(Sq);
+                const int64_t mm = (int64_t)m * m;
+                to_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, t>>>(Sq, mm);
+                const unsigned gp = (unsigned)(((int64_t)m * SW_T + 255) / 256);
+                const unsigned gr = (unsigned)((m + 127) / 128);
+                const dim3 gu((m + 31) / 32, (m + 31) / 32);
+                for (int k0 = 0; k0 < m; k0 += SW_T) {
+                    const int w = std::min(SW_T, m - k0);
+                    blk_diag_df_kernel<<<1, 256, 0, t>>>(Wq, m, k0, w, Dinv[i].data(), bad);
+                    blk_panel_df_kernel<<<gr, 128, 0, t>>>(Wq, m, k0, w, Dinv[i].data(), P[i].data());
+                    blk_update_df_kernel<<<gu, 256, 0, t>>>(Wq, m, k0, w, P[i].data());
+                    blk_write_df_kernel<<<gp, 256, 0, t>>>(Wq, m, k0, w, P[i].data(), Dinv[i].data());
+                }
+                mirror_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, t>>>(Wq, m);
+                finish_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, t>>>(Sq, mm, bad);
+                LSS_LAUNCH_CHECK();
+            }
+            for (int i = 0; i < ns; ++i) {
+                LSS_CUDA(cudaEventRecord(joined[i], side[i]));
+                LSS_CUDA(cudaStreamWaitEvent(s, joined[i], 0));
+            }
+            LSS_CUDA(cudaStreamSynchronize(s));  // scratch is freed at scope exit
+        } catch (...) {
+            for (cudaStream_t t : side)
+                if (t) cudaStreamSynchronize(t);
+            release();
+            throw;
         }
-        LSS_CUDA(cudaStreamSynchronize(s));  // Dinv and P are freed at scope exit
+        release();
     }
 }
 
