@@ -43,10 +43,9 @@ import numpy as np  # noqa: E402
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch over the
-# kernel's algorithmic bytes, from ncu captures of the 60^3-node elasticity case
-# (profiles/spmv_df32_elasticity_650k.md, symv0_mas_level0_elasticity_650k.md,
-# residual32_elasticity_650k.md).  The elasticity workloads' kernels scale in
-# proportion, so traffic = ratio x algorithmic bytes of the timed launch.
+# kernel's algorithmic bytes, from ncu captures of the same kernels on the
+# 60^3-node elasticity case (648k DOFs).  The elasticity workloads' kernels
+# scale in proportion, so traffic = ratio x algorithmic bytes of the timed launch.
 NCU_TRAFFIC_RATIO = {"spmv_outer": 246.24 / 252.39, "mas_level0_symv": 145.10 / 146.79,
                      "residual_spmv_prec": 133.98 / 132.83}
 

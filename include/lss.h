@@ -248,9 +248,11 @@ lss_status lss_factorize_batched_device(lss_solver *const *solvers, int32_t coun
  *     their number; all on the current device;
  *   - stream: a cudaStream_t of the current device (NULL = legacy default).
  * Allocates nothing: every intermediate lives in one static device scratch
- * area of 8,610,304 bytes inside liblss.so.  The first call on a device
- * resolves the scratch address (cudaGetSymbolAddress, which can load the
- * module): make it before any stream capture.  Calls share the scratch, so
+ * area of 8,716,800 bytes inside liblss.so.  Every call looks the scratch
+ * address up in the current context (cudaGetSymbolAddress, which allocates
+ * nothing, so the address stays valid across cudaDeviceReset); the first call
+ * on a device, or the first after a reset, can load the module: make it
+ * before any stream capture.  Calls share the scratch, so
  * calls that can overlap (other streams or threads) race and must be
  * serialised by the caller.  Only the scratch's grid-reduction arrival counter
  * must start at zero: it is zero at module load and every reduction leaves it

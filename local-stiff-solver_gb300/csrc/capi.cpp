@@ -1,5 +1,6 @@
 // extern "C" entry points (include/lss.h).  Every call converts exceptions
 // into status codes and records the message; nothing here exits the process.
+#include <algorithm>
 #include <atomic>
 #include <cstring>
 #include <mutex>
@@ -13,14 +14,14 @@
 #include "solver.hpp"
 
 namespace lss {
-size_t &alloc_cap_bytes()
+std::atomic<size_t> &alloc_cap_bytes()
 {
-    static size_t cap = 0;
+    static std::atomic<size_t> cap{0};
     return cap;
 }
-size_t &alloc_cap_base()
+std::atomic<size_t> &alloc_cap_base()
 {
-    static size_t base = 0;
+    static std::atomic<size_t> base{0};
     return base;
 }
 std::atomic<unsigned long long> &launch_count()
@@ -28,10 +29,30 @@ std::atomic<unsigned long long> &launch_count()
     static std::atomic<unsigned long long> c{0};
     return c;
 }
-size_t &alloc_live_bytes()
+std::atomic<size_t> &alloc_live_bytes()
 {
-    static size_t live = 0;
+    static std::atomic<size_t> live{0};
     return live;
+}
+int sm_grid(int per_sm)
+{
+    constexpr int MAX_DEVICES = 64;
+    static std::atomic<int> sms[MAX_DEVICES] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
+        cudaGetLastError();
+        dev = -1;
+    }
+    int n = dev >= 0 && dev < MAX_DEVICES ? sms[dev].load() : 0;
+    if (n <= 0) {
+        if (dev < 0 || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            n = 1;
+        }
+        if (dev >= 0 && dev < MAX_DEVICES) sms[dev] = n;
+    }
+    const long long g = (long long)n * (per_sm > 0 ? per_sm : 1);
+    return (int)std::min<long long>(g, GRID_MAX);
 }
 }  // namespace lss
 
@@ -113,7 +134,8 @@ lss_status lss_create(const char *params_json, lss_solver **out)
     lss_status st = guarded(nullptr, [&]() {
         lss::Params p = lss::parse_params(params_json, lss::Params());
         if (p.memory_cap_bytes) {
-            lss::alloc_cap_base() = lss::alloc_live_bytes();
+            lss::alloc_cap_bytes() = 0;
+            lss::alloc_cap_base() = lss::alloc_live_bytes().load();
             lss::alloc_cap_bytes() = p.memory_cap_bytes;
         }
         impl = new lss::HybridSolver(p);
@@ -337,7 +359,8 @@ lss_status lss_op_time(lss_solver *s, int32_t kind, int32_t reps, double *ms_per
 
 lss_status lss_set_memory_cap(size_t bytes)
 {
-    lss::alloc_cap_base() = lss::alloc_live_bytes();
+    lss::alloc_cap_bytes() = 0;  // no reservation sees the new base with the old cap
+    lss::alloc_cap_base() = lss::alloc_live_bytes().load();
     lss::alloc_cap_bytes() = bytes;
     return LSS_OK;
 }
@@ -373,6 +396,22 @@ lss_status for_each_system(lss_solver *const *solvers, int32_t count, int32_t th
                 return LSS_ERR_INVALID_ARGUMENT;
             }
     if (count == 0) return LSS_OK;
+    // the calling thread runs a worker, which selects each solver's device:
+    // the caller's current device is restored on every exit path
+    struct DeviceRestore {
+        int dev = -1;
+        DeviceRestore()
+        {
+            if (cudaGetDevice(&dev) != cudaSuccess) {
+                cudaGetLastError();
+                dev = -1;
+            }
+        }
+        ~DeviceRestore()
+        {
+            if (dev >= 0) cudaSetDevice(dev);
+        }
+    } restore;
     const int nthreads = threads > 0 ? std::min<int>(threads, count) : count;
     std::atomic<int32_t> next{0};
     std::mutex mu;

@@ -9,8 +9,12 @@
 
 namespace lss {
 
-constexpr int RED_MAX_VALUES = 8;   // values per grid reduction
-constexpr int GRID_MAX = 152 * 16;  // upper bound of CTAs of any reducing kernel (16 per SM)
+constexpr int RED_MAX_VALUES = 8;  // values per grid reduction
+constexpr int GRID_MAX = 4096;     // CTAs of any reducing kernel at most (size of the reduction partials)
+
+// CTAs for `per_sm` resident CTAs on every SM of the current device (the SM
+// count is queried once per device), capped at GRID_MAX.
+int sm_grid(int per_sm);
 
 // Scratch of the deterministic grid reductions (device memory, counter zeroed once).
 struct GridReduce {
@@ -18,7 +22,7 @@ struct GridReduce {
     unsigned *counter = nullptr; // one arrival counter
 };
 
-inline int grid_for(long long work_items, int items_per_cta, int max_ctas = GRID_MAX)
+inline int grid_for(long long work_items, int items_per_cta, int max_ctas)
 {
     long long g = (work_items + items_per_cta - 1) / items_per_cta;
     if (g < 1) g = 1;
@@ -167,8 +171,14 @@ int64_t mas_tile_elems(int bd);
 // Galerkin assembly into per-bank dense N x N FP64 staging (N = 32 bd)
 void launch_mas_assemble0(const BsrDev &A, const int32_t *part_of, const int32_t *part_off, double *stage,
                           cudaStream_t s);
+// members of the coarse items (CoarseSpace::memb_*), device copies
+struct CoarseMembers {
+    const int32_t *ptr = nullptr;
+    const int32_t *rows = nullptr;
+    int64_t base[MAS_MAXL] = {};
+};
 void launch_mas_assemble_coarse(const BsrDev &A, const MasDev &m, const int32_t *cmap /* nb*(L-1) */,
-                                double *stage, cudaStream_t s);
+                                const CoarseMembers &mb, double *stage, cudaStream_t s);
 // pad zero diagonals, invert (symmetric sweep), write bank tiles (FP32 or FP64)
 void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, bool fp32, int *bad,
                        cudaStream_t s, bool bf16_offdiag = false);

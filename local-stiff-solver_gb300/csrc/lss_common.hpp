@@ -49,10 +49,28 @@ std::atomic<unsigned long long> &launch_count();
 
 // Optional allocation cap for fault testing of the OOM path: at most
 // alloc_cap_bytes() more bytes than were live when the cap was set
-// (alloc_cap_base()); 0 = no cap.
-size_t &alloc_cap_bytes();
-size_t &alloc_cap_base();
-size_t &alloc_live_bytes();
+// (alloc_cap_base()); 0 = no cap.  Atomic: the batched entry points allocate
+// from several host threads at once.
+std::atomic<size_t> &alloc_cap_bytes();
+std::atomic<size_t> &alloc_cap_base();
+std::atomic<size_t> &alloc_live_bytes();
+
+// Books `bytes` against the live total before a cudaMalloc; the check against
+// the cap and the addition are one compare-and-swap, so concurrent
+// allocations can neither slip past the cap nor lose an update.
+inline void alloc_reserve(size_t bytes)
+{
+    std::atomic<size_t> &live = alloc_live_bytes();
+    size_t cur = live.load();
+    for (;;) {
+        const size_t cap = alloc_cap_bytes().load();
+        if (cap && cur + bytes > alloc_cap_base().load() + cap)
+            fail(LSS_ERR_OOM, "device allocation of " + std::to_string(bytes) +
+                                  " bytes exceeds the configured memory cap");
+        if (live.compare_exchange_weak(cur, cur + bytes)) return;
+    }
+}
+inline void alloc_unreserve(size_t bytes) { alloc_live_bytes().fetch_sub(bytes); }
 
 // Owning device allocation (cudaMalloc), move-only.
 template <typename T>
@@ -75,19 +93,21 @@ public:
         if (n == n_) return;
         release();
         if (n == 0) return;
-        size_t bytes = n * sizeof(T);
-        if (alloc_cap_bytes() && alloc_live_bytes() + bytes > alloc_cap_base() + alloc_cap_bytes())
-            fail(LSS_ERR_OOM, "device allocation of " + std::to_string(bytes) +
-                                  " bytes exceeds the configured memory cap");
-        LSS_CUDA(cudaMalloc(&p_, bytes));
-        alloc_live_bytes() += bytes;
+        const size_t bytes = n * sizeof(T);
+        alloc_reserve(bytes);
+        const cudaError_t e = cudaMalloc(&p_, bytes);
+        if (e != cudaSuccess) {
+            p_ = nullptr;
+            alloc_unreserve(bytes);
+            cuda_check(e, "cudaMalloc", __FILE__, __LINE__);
+        }
         n_ = n;
     }
     void release()
     {
         if (p_) {
             cudaFree(p_);
-            alloc_live_bytes() -= n_ * sizeof(T);
+            alloc_unreserve(n_ * sizeof(T));
         }
         p_ = nullptr;
         n_ = 0;

@@ -154,56 +154,69 @@ __global__ void __launch_bounds__(256) assemble0_kernel(BsrDev A, const int32_t 
     }
 }
 
+// Galerkin blocks of every coarse level, deterministically: one warp per
+// coarse item ci (its row strip of the bank matrix), lane c accumulating the
+// BD x BD block of the column items cj with cj % 32 == c.  The item's fine
+// rows come in ascending order and each row's blocks in column order; the
+// blocks of a 32-wide chunk whose column item falls into the same bank are
+// handed to their owner lanes one at a time by shuffles, so every sum runs in
+// one fixed order (no atomics): two factorizations of the same matrix give
+// bit-identical coarse inverses.  Only the upper triangle is written; each
+// entry belongs to exactly one item, so the stores never collide.
 template <int BD>
-__device__ __forceinline__ void add_coarse_block(double *base, int32_t ci, int32_t cj, const double (&acc)[BD * BD])
+__global__ void __launch_bounds__(256) assemble_coarse_kernel(BsrDev A, MasDev m, const int32_t *__restrict__ cmap,
+                                                              CoarseMembers mb, double *__restrict__ stage)
 {
     constexpr int N = 32 * BD;
+    const int lane = threadIdx.x & 31;
+    int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int l = 1;
+    while (l < m.L && w >= m.nitems[l]) w -= m.nitems[l++];
+    if (l >= m.L) return;
+    const int32_t ci = (int32_t)w;
+    const int32_t *map = cmap + (int64_t)(l - 1) * A.nb;
+    const int32_t g = m.boff[l] + (ci >> 5);
+    double acc[BD * BD];
+#pragma unroll
+    for (int k = 0; k < BD * BD; ++k) acc[k] = 0.0;
+    const int32_t r0 = mb.ptr[mb.base[l] + ci], r1 = mb.ptr[mb.base[l] + ci + 1];
+    for (int32_t r = r0; r < r1; ++r) {
+        const int32_t i = mb.rows[r];
+        const int32_t b = A.rows[i], len = A.rows[i + 1] - b;
+        const double *v = A.vals + (int64_t)b * BD * BD;
+        for (int32_t q0 = 0; q0 < len; q0 += 32) {
+            const int32_t q = q0 + lane;
+            int32_t cj = -1;
+            double val[BD * BD];
+            if (q < len) {
+                cj = map[A.cols[b + q]];
+#pragma unroll
+                for (int k = 0; k < BD * BD; ++k) val[k] = v[(int64_t)k * len + q];
+            } else {
+#pragma unroll
+                for (int k = 0; k < BD * BD; ++k) val[k] = 0.0;
+            }
+            unsigned pending = __ballot_sync(0xffffffffu, cj >= 0 && (cj >> 5) == (ci >> 5));
+            while (pending) {
+                const int src = __ffs(pending) - 1;
+                pending &= pending - 1;
+                const int32_t c = __shfl_sync(0xffffffffu, cj, src);
+#pragma unroll
+                for (int k = 0; k < BD * BD; ++k) {
+                    const double x = __shfl_sync(0xffffffffu, val[k], src);
+                    if ((c & 31) == lane) acc[k] += x;
+                }
+            }
+        }
+    }
+    double *base = stage + (int64_t)g * N * N;
 #pragma unroll
     for (int bi = 0; bi < BD; ++bi)
 #pragma unroll
         for (int bj = 0; bj < BD; ++bj) {
-            const int row = bi * 32 + (ci & 31), col = bj * 32 + (cj & 31);
-            if (row > col) continue;  // upper triangle only
-            atomicAdd(base + (int64_t)row * N + col, acc[bi * BD + bj]);
+            const int row = bi * 32 + (ci & 31), col = bj * 32 + lane;
+            if (row <= col) base[(int64_t)row * N + col] = acc[bi * BD + bj];
         }
-}
-
-// Galerkin blocks of every coarse level, one thread per block row.  The
-// row's blocks arrive in column order, so neighbours that fall into the same
-// coarse item come in runs: a run is summed in registers and leaves as one
-// set of atomics (at the coarser levels nearly the whole row is one run).
-template <int BD>
-__global__ void __launch_bounds__(256) assemble_coarse_kernel(BsrDev A, MasDev m, const int32_t *__restrict__ cmap,
-                                                              double *__restrict__ stage)
-{
-    constexpr int N = 32 * BD;
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.nb) return;
-    const int32_t b = A.rows[i], len = A.rows[i + 1] - b;
-    const double *v = A.vals + (int64_t)b * BD * BD;
-    for (int l = 1; l < m.L; ++l) {
-        const int32_t *map = cmap + (int64_t)(l - 1) * A.nb;
-        const int32_t ci = map[i];
-        const int32_t g = m.boff[l] + (ci >> 5);
-        double *base = stage + (int64_t)g * N * N;
-        int32_t cur = -1;
-        double acc[BD * BD];
-#pragma unroll
-        for (int k = 0; k < BD * BD; ++k) acc[k] = 0.0;
-        for (int32_t q = 0; q < len; ++q) {
-            const int32_t cj = map[A.cols[b + q]];
-            if ((cj >> 5) != (ci >> 5)) continue;
-            if (cj != cur) {
-                if (cur >= 0) add_coarse_block<BD>(base, ci, cur, acc);
-                cur = cj;
-#pragma unroll
-                for (int k = 0; k < BD * BD; ++k) acc[k] = 0.0;
-            }
-#pragma unroll
-            for (int k = 0; k < BD * BD; ++k) acc[k] += v[(int64_t)k * len + q];
-        }
-        if (cur >= 0) add_coarse_block<BD>(base, ci, cur, acc);
-    }
 }
 
 // Symmetric sweep inversion of S (N x N, leading dimension ld, in shared
@@ -506,15 +519,15 @@ void mas_apply_dot_t(const MasDev &m, const T *inv0, const T *invc, T *v, T *u, 
                      const int *done, cudaStream_t s, float *z32, float *z_lo)
 {
     if (m.L > 1) {
-        restrict0_kernel<BD, T, XT><<<grid_for((int64_t)m.nparts * 32, 256, 152 * 16), 256, 0, s>>>(m, xin, v, done);
+        restrict0_kernel<BD, T, XT><<<grid_for((int64_t)m.nparts * 32, 256, sm_grid(16)), 256, 0, s>>>(m, xin, v, done);
         for (int l = 1; l + 1 < m.L; ++l)
-            restrict_kernel<BD, T><<<grid_for((int64_t)m.nbanks[l] * 32, 256, 152 * 16), 256, 0, s>>>(m, l, v, done);
-        symv_coarse_kernel<BD, T><<<grid_for((int64_t)m.ncoarse * 32, 256, 152 * 16), 256, 0, s>>>(m, invc, v, u,
+            restrict_kernel<BD, T><<<grid_for((int64_t)m.nbanks[l] * 32, 256, sm_grid(16)), 256, 0, s>>>(m, l, v, done);
+        symv_coarse_kernel<BD, T><<<grid_for((int64_t)m.ncoarse * 32, 256, sm_grid(16)), 256, 0, s>>>(m, invc, v, u,
                                                                                                    done);
         if (m.L > 2)
             prolong_all_kernel<BD, T><<<grid_for(m.nitems[1], 256, 1 << 30), 256, 0, s>>>(m, u, done);
     }
-    const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
+    const int grid = grid_for((int64_t)m.nparts * 32, 256, sm_grid(16));
 #define LSS_S0(A_, D_)                                                                                          \
     do {                                                                                                        \
         if (std::is_same<T, float>::value && m.bank_bytes0 > 0)                                                 \
@@ -553,15 +566,17 @@ void launch_mas_assemble0(const BsrDev &A, const int32_t *part_of, const int32_t
     LSS_LAUNCH_CHECK();
 }
 
-void launch_mas_assemble_coarse(const BsrDev &A, const MasDev &m, const int32_t *cmap, double *stage,
-                                cudaStream_t s)
+void launch_mas_assemble_coarse(const BsrDev &A, const MasDev &m, const int32_t *cmap, const CoarseMembers &mb,
+                                double *stage, cudaStream_t s)
 {
-    const int grid = (int)((A.nb + 255) / 256);
-    if (grid == 0 || m.L < 2) return;
+    int64_t items = 0;
+    for (int l = 1; l < m.L; ++l) items += m.nitems[l];
+    if (items == 0 || m.L < 2) return;
+    const int grid = (int)((items * 32 + 255) / 256);
     switch (A.bd) {
-    case 1: assemble_coarse_kernel<1><<<grid, 256, 0, s>>>(A, m, cmap, stage); break;
-    case 2: assemble_coarse_kernel<2><<<grid, 256, 0, s>>>(A, m, cmap, stage); break;
-    default: assemble_coarse_kernel<3><<<grid, 256, 0, s>>>(A, m, cmap, stage); break;
+    case 1: assemble_coarse_kernel<1><<<grid, 256, 0, s>>>(A, m, cmap, mb, stage); break;
+    case 2: assemble_coarse_kernel<2><<<grid, 256, 0, s>>>(A, m, cmap, mb, stage); break;
+    default: assemble_coarse_kernel<3><<<grid, 256, 0, s>>>(A, m, cmap, mb, stage); break;
     }
     LSS_LAUNCH_CHECK();
 }
@@ -607,7 +622,7 @@ void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, b
 void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp32, const double *xin, double *z,
                        cudaStream_t s)
 {
-    const int grid = grid_for((int64_t)m.nparts * 32, 256, GRID_MAX);
+    const int grid = grid_for((int64_t)m.nparts * 32, 256, sm_grid(16));
     GridReduce gr{};
 #define LSS_L0(BD_, T_)                                                                                        \
     symv0_kernel<BD_, T_, false, 0, double><<<grid, 256, 0, s>>>(m, (const T_ *)inv0, (const T_ *)u, xin, z, 1.0,   \

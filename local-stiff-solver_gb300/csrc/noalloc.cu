@@ -20,8 +20,6 @@
 //   counter       one unsigned                      grid-reduction arrivals
 // Only `counter` must start at zero: static device memory is zero when the
 // module loads, and every grid reduction resets it to zero on completion.
-#include <mutex>
-
 #include "device_common.cuh"
 #include "kernels.hpp"
 #include "lss_common.hpp"
@@ -46,30 +44,23 @@ static_assert(SCRATCH_BYTES == NOALLOC_SCRATCH_BYTES, "scratch size out of sync 
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
-constexpr int MAX_DEVICES = 64;
-
-// Device address of the scratch on the current device, resolved once per
-// device (cudaGetSymbolAddress; may load the module, so the first call on a
-// device must not happen inside a stream capture).
+// Device address of the scratch in the current context.  Looked up on every
+// call rather than cached: after cudaDeviceReset, or in another context on the
+// same device, the module is loaded again and the array can move, and a cached
+// address would then point at unmapped memory.  cudaGetSymbolAddress
+// allocates nothing; the lookup that first loads the module on a device (the
+// first call there, or the first after a reset) must not happen inside a
+// stream capture.
 unsigned char *scratch_base()
 {
-    static std::mutex mu;
-    static unsigned char *base[MAX_DEVICES] = {};
-    int dev = 0;
-    LSS_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= MAX_DEVICES) fail(LSS_ERR_INVALID_ARGUMENT, "device index beyond the scratch table");
-    std::lock_guard<std::mutex> lock(mu);
-    if (!base[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            fail(e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? LSS_ERR_NO_DEVICE : LSS_ERR_CUDA,
-                 std::string("cudaGetSymbolAddress of the selection scratch failed: ") + cudaGetErrorString(e));
-        }
-        base[dev] = (unsigned char *)p;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        fail(e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? LSS_ERR_NO_DEVICE : LSS_ERR_CUDA,
+             std::string("cudaGetSymbolAddress of the selection scratch failed: ") + cudaGetErrorString(e));
     }
-    return base[dev];
+    return (unsigned char *)p;
 }
 
 // Exclusive prefix sum of the per-CTA counts (one CTA of 1024 threads, each

@@ -15,7 +15,7 @@ namespace lss {
 // 8 MiB of row norms plus the reduction partials, per-CTA counts and offsets,
 // the GMM state and the arrival counter.
 constexpr int32_t NOALLOC_MAX_ROWS = LSS_NOALLOC_MAX_ROWS;
-constexpr size_t NOALLOC_SCRATCH_BYTES = 8610304;
+constexpr size_t NOALLOC_SCRATCH_BYTES = 8716800;
 
 // Throws lss::Error (LSS_ERR_INVALID_ARGUMENT for n > NOALLOC_MAX_ROWS, before
 // any device work).  Stream-ordered on s; no host synchronisation.

@@ -291,6 +291,23 @@ CoarseSpace build_coarse_space(const Pattern &P, int max_coarse_levels)
     cs.key.resize(L);
     cs.cbase.resize(L);
     cs.ccnt.resize(L);
+    // member lists (counting sort of cmap per level; rows ascending)
+    cs.memb_base.assign(L, 0);
+    cs.memb_rows.resize((size_t)(L - 1) * nb);
+    for (int l = 1; l < L; ++l) {
+        const int32_t items = cs.nitems[l];
+        const int32_t *map = cs.cmap.data() + (int64_t)(l - 1) * nb;
+        const int64_t base = (int64_t)cs.memb_ptr.size();
+        cs.memb_base[l] = base;
+        cs.memb_ptr.resize(base + items + 1, 0);
+        int32_t *ptr = cs.memb_ptr.data() + base;
+        for (int32_t i = 0; i < nb; ++i) ++ptr[map[i] + 1];
+        const int32_t first = (int32_t)((int64_t)(l - 1) * nb);
+        ptr[0] = first;
+        for (int32_t t = 0; t < items; ++t) ptr[t + 1] += ptr[t];
+        std::vector<int32_t> fill(ptr, ptr + items);
+        for (int32_t i = 0; i < nb; ++i) cs.memb_rows[fill[map[i]]++] = i;
+    }
     return cs;
 }
 

@@ -40,6 +40,12 @@ struct CoarseSpace {
     std::vector<std::vector<int32_t>> cbase;      // level l: nbanks[l]
     std::vector<std::vector<uint8_t>> ccnt;       // level l: nbanks[l]
     std::vector<int32_t> cmap;                    // (L-1) * nb: item of every node at level l
+    // members of every coarse item, levels 1..L-1 concatenated: item t of level
+    // l owns memb_rows[memb_ptr[memb_base[l] + t] .. memb_ptr[memb_base[l] + t + 1])
+    // (fine block rows, ascending) -- the fixed summation order of the
+    // deterministic Galerkin assembly
+    std::vector<int32_t> memb_ptr, memb_rows;
+    std::vector<int64_t> memb_base;               // L entries (level 0 unused)
 };
 
 CoarseSpace build_coarse_space(const Pattern &P, int max_coarse_levels);

@@ -382,7 +382,7 @@ __global__ void row_of_kernel(int32_t n, const int32_t *__restrict__ outer, int3
 template <int BD>
 void spmv_dispatch(const BsrDev &A, const double *x, double *y, const int *done, cudaStream_t s)
 {
-    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, 152 * 16);
+    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, sm_grid(16));
     switch (A.lanes) {
     case 1: spmv_kernel<BD, 1><<<grid, 256, 0, s>>>(A, x, y, done); break;
     case 2: spmv_kernel<BD, 2><<<grid, 256, 0, s>>>(A, x, y, done); break;
@@ -398,7 +398,7 @@ void residual_dispatch(const BsrDev &A, const VT *vals, const double *r, const X
                        const int *done, cudaStream_t s)
 {
     const int lanes = sizeof(VT) == 4 ? A.lanes32 : A.lanes;
-    const int grid = grid_for((int64_t)A.nb * lanes, 256, 152 * 16);
+    const int grid = grid_for((int64_t)A.nb * lanes, 256, sm_grid(16));
     switch (lanes) {
     case 1: residual_kernel<BD, 1, VT, ACC, XT><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
     case 2: residual_kernel<BD, 2, VT, ACC, XT><<<grid, 256, 0, s>>>(A, vals, r, x, y, done); break;
@@ -412,7 +412,7 @@ void residual_dispatch(const BsrDev &A, const VT *vals, const double *r, const X
 template <int BD>
 void spmv_alpha_dispatch(const BsrDev &A, const double *p, double *Ap, PcgState *st, GridReduce gr, cudaStream_t s)
 {
-    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, GRID_MAX);
+    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, sm_grid(16));
     switch (A.lanes) {
     case 1: spmv_alpha_kernel<BD, 1><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
     case 2: spmv_alpha_kernel<BD, 2><<<grid, 256, 0, s>>>(A, p, Ap, st, gr); break;
@@ -429,7 +429,7 @@ void launch_gather_values(int64_t count, const int64_t *src, const double *csc, 
                           cudaStream_t s, float2 *vals_df)
 {
     if (count == 0) return;
-    gather_values_kernel<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(count, src, csc, vals, vals32, vals_df);
+    gather_values_kernel<<<grid_for(count, 256, sm_grid(16)), 256, 0, s>>>(count, src, csc, vals, vals32, vals_df);
     LSS_LAUNCH_CHECK();
 }
 
@@ -454,7 +454,7 @@ template <int BD>
 void residual32_dispatch(const BsrDev &A, const float *r32, const float *x32, float *y32, const uint8_t *precise,
                          const double *r64, const float *x_lo, const int *done, cudaStream_t s)
 {
-    const int grid = grid_for((int64_t)A.nb * A.lanes32, 256, 152 * 16);
+    const int grid = grid_for((int64_t)A.nb * A.lanes32, 256, sm_grid(16));
 #define LSS_R32(L_) residual32_kernel<BD, L_><<<grid, 256, 0, s>>>(A, r32, x32, y32, precise, r64, x_lo, done)
     switch (A.lanes32) {
     case 1: LSS_R32(1); break;
@@ -482,7 +482,7 @@ void launch_residual32(const BsrDev &A, const float *r32, const float *x32, floa
 
 void launch_dot(int64_t n, const double *a, const double *b, double *out, GridReduce gr, cudaStream_t s)
 {
-    dot_kernel<<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, a, b, out, gr);
+    dot_kernel<<<grid_for(n, 1024, sm_grid(16)), 256, 0, s>>>(n, a, b, out, gr);
     LSS_LAUNCH_CHECK();
 }
 
@@ -498,7 +498,7 @@ template <int BD>
 void spmv_alpha_df_dispatch(const BsrDev &A, const float2 *pd, float2 *Ap, PcgState *st, GridReduce gr,
                             cudaStream_t s)
 {
-    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, GRID_MAX);
+    const int grid = grid_for((int64_t)A.nb * A.lanes, 256, sm_grid(16));
     switch (A.lanes) {
     case 1: spmv_alpha_df_kernel<BD, 1><<<grid, 256, 0, s>>>(A, pd, Ap, st, gr); break;
     case 2: spmv_alpha_df_kernel<BD, 2><<<grid, 256, 0, s>>>(A, pd, Ap, st, gr); break;
@@ -534,7 +534,7 @@ __global__ void probe_kernel(int64_t nb, int bd, const int32_t *__restrict__ per
 void launch_probe(int64_t nb, int bd, const int32_t *perm, double *dst, cudaStream_t s)
 {
     if (nb == 0) return;
-    probe_kernel<<<grid_for(nb * bd, 1024, 152 * 16), 256, 0, s>>>(nb, bd, perm, dst);
+    probe_kernel<<<grid_for(nb * bd, 1024, sm_grid(16)), 256, 0, s>>>(nb, bd, perm, dst);
     LSS_LAUNCH_CHECK();
 }
 
@@ -547,7 +547,7 @@ __global__ void df_to_double_kernel(int64_t n, const float2 *__restrict__ src, d
 void launch_df_to_double(int64_t n, const float2 *src, double *dst, cudaStream_t s)
 {
     if (n == 0) return;
-    df_to_double_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, src, dst);
+    df_to_double_kernel<<<grid_for(n, 1024, sm_grid(16)), 256, 0, s>>>(n, src, dst);
     LSS_LAUNCH_CHECK();
 }
 
@@ -555,54 +555,54 @@ void launch_split(int64_t n, const double *src, float2 *dst, cudaStream_t s)
 {
     if (n == 0) return;
     if (!src || !dst) fail(LSS_ERR_INTERNAL, "split launched without its arrays");
-    split_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, src, dst);
+    split_kernel<<<grid_for(n, 1024, sm_grid(16)), 256, 0, s>>>(n, src, dst);
     LSS_LAUNCH_CHECK();
 }
 
 void launch_pcg_update_xr(int64_t n, double *x, double *r, const double *p, const double *Ap, PcgState *st,
                           GridReduce gr, cudaStream_t s, float *r32)
 {
-    update_xr_kernel<double><<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, x, r, p, Ap, st, gr, r32);
+    update_xr_kernel<double><<<grid_for(n, 1024, sm_grid(16)), 256, 0, s>>>(n, x, r, p, Ap, st, gr, r32);
     LSS_LAUNCH_CHECK();
 }
 
 void launch_pcg_update_xr_df(int64_t n, double *x, double *r, const double *p, const float2 *Ap_df, PcgState *st,
                              GridReduce gr, cudaStream_t s, float *r32)
 {
-    update_xr_kernel<float2><<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, x, r, p, Ap_df, st, gr, r32);
+    update_xr_kernel<float2><<<grid_for(n, 1024, sm_grid(16)), 256, 0, s>>>(n, x, r, p, Ap_df, st, gr, r32);
     LSS_LAUNCH_CHECK();
 }
 
 void launch_pcg_update_p(int64_t n, double *p, const double *z, const PcgState *st, cudaStream_t s, float2 *p_df)
 {
-    update_p_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, p, z, st, p_df);
+    update_p_kernel<<<grid_for(n, 1024, sm_grid(16)), 256, 0, s>>>(n, p, z, st, p_df);
     LSS_LAUNCH_CHECK();
 }
 
 void launch_copy(int64_t n, const double *src, double *dst, const int *done, cudaStream_t s)
 {
-    copy_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, src, dst, done);
+    copy_kernel<<<grid_for(n, 1024, sm_grid(16)), 256, 0, s>>>(n, src, dst, done);
     LSS_LAUNCH_CHECK();
 }
 
 void launch_permute(int64_t nb, int bd, const int32_t *perm, const double *src, double *dst, bool to_new,
                     cudaStream_t s)
 {
-    permute_kernel<<<grid_for(nb * bd, 1024, 152 * 16), 256, 0, s>>>(nb, bd, perm, src, dst, to_new);
+    permute_kernel<<<grid_for(nb * bd, 1024, sm_grid(16)), 256, 0, s>>>(nb, bd, perm, src, dst, to_new);
     LSS_LAUNCH_CHECK();
 }
 
 void launch_pcg_rz(int64_t n, const double *r, const double *z, PcgState *st, int dot_mode, GridReduce gr,
                    cudaStream_t s)
 {
-    rz_kernel<<<grid_for(n, 1024, GRID_MAX), 256, 0, s>>>(n, r, z, st, dot_mode, gr);
+    rz_kernel<<<grid_for(n, 1024, sm_grid(16)), 256, 0, s>>>(n, r, z, st, dot_mode, gr);
     LSS_LAUNCH_CHECK();
 }
 
 void launch_check_finite(int64_t n, const double *v, int *flag, cudaStream_t s)
 {
     if (n == 0) return;
-    check_finite_kernel<<<grid_for(n, 1024, 152 * 16), 256, 0, s>>>(n, v, flag);
+    check_finite_kernel<<<grid_for(n, 1024, sm_grid(16)), 256, 0, s>>>(n, v, flag);
     LSS_LAUNCH_CHECK();
 }
 
@@ -611,21 +611,21 @@ void launch_grad_params(int32_t nparams, const int64_t *mt_rowptr, const int32_t
                         double *dtheta, cudaStream_t s)
 {
     if (nparams <= 0) return;
-    grad_params_kernel<<<grid_for((int64_t)nparams * 32, 256, 152 * 16), 256, 0, s>>>(
+    grad_params_kernel<<<grid_for((int64_t)nparams * 32, 256, sm_grid(16)), 256, 0, s>>>(
         nparams, mt_rowptr, mt_cols, mt_vals, row_of, inner, lambda, x, dtheta);
     LSS_LAUNCH_CHECK();
 }
 
 void launch_row_of(int32_t n, const int32_t *outer, int32_t *row_of, cudaStream_t s)
 {
-    row_of_kernel<<<grid_for((int64_t)n * 32, 256, 152 * 16), 256, 0, s>>>(n, outer, row_of);
+    row_of_kernel<<<grid_for((int64_t)n * 32, 256, sm_grid(16)), 256, 0, s>>>(n, outer, row_of);
     LSS_LAUNCH_CHECK();
 }
 
 void launch_grad_pattern(int32_t n, const int32_t *outer, const int32_t *inner, const double *lambda,
                          const double *x, double *dA, cudaStream_t s)
 {
-    grad_pattern_kernel<<<grid_for((int64_t)n * 32, 256, 152 * 16), 256, 0, s>>>(n, outer, inner, lambda, x, dA);
+    grad_pattern_kernel<<<grid_for((int64_t)n * 32, 256, sm_grid(16)), 256, 0, s>>>(n, outer, inner, lambda, x, dA);
     LSS_LAUNCH_CHECK();
 }
 

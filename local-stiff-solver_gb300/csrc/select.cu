@@ -342,7 +342,7 @@ void launch_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer, const dou
                          cudaStream_t s)
 {
     const double avg = n > 0 ? (double)nnz / n : 0.0;
-    const int grid = grid_for((long long)n * 8, 256, 152 * 16);
+    const int grid = grid_for((long long)n * 8, 256, sm_grid(16));
     if (avg <= 6) l1_norm_kernel<4><<<grid, 256, 0, s>>>(n, outer, vals, rn);
     else if (avg <= 16) l1_norm_kernel<8><<<grid, 256, 0, s>>>(n, outer, vals, rn);
     else if (avg <= 40) l1_norm_kernel<16><<<grid, 256, 0, s>>>(n, outer, vals, rn);
@@ -353,7 +353,7 @@ void launch_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer, const dou
 void launch_gmm(int32_t n, const double *rn, GmmState *st, int max_iterations, double tol, GridReduce gr,
                 cudaStream_t s)
 {
-    const int grid = grid_for(n, 256, 152 * 8);
+    const int grid = grid_for(n, 256, sm_grid(8));
     stats_kernel<<<grid, 256, 0, s>>>(n, rn, st, gr);
     LSS_LAUNCH_CHECK();
     var_kernel<<<grid, 256, 0, s>>>(n, rn, st, gr);

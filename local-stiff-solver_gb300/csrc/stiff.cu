@@ -409,7 +409,7 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
                 double *Sq = inv + hoff[q];
                 float2 *Wq = reinterpret_cast<float2 *>(Sq);
                 const int64_t mm = (int64_t)m * m;
-                to_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, t>>>(Sq, mm);
+                to_df_kernel<<<grid_for(mm, 1024, sm_grid(8)), 256, 0, t>>>(Sq, mm);
                 const unsigned gp = (unsigned)(((int64_t)m * SW_T + 255) / 256);
                 const unsigned gr = (unsigned)((m + 127) / 128);
                 const dim3 gu((m + 31) / 32, (m + 31) / 32);
@@ -420,8 +420,8 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
                     blk_update_df_kernel<<<gu, 256, 0, t>>>(Wq, m, k0, w, P[i].data());
                     blk_write_df_kernel<<<gp, 256, 0, t>>>(Wq, m, k0, w, P[i].data(), Dinv[i].data());
                 }
-                mirror_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, t>>>(Wq, m);
-                finish_df_kernel<<<grid_for(mm, 1024, 152 * 8), 256, 0, t>>>(Sq, mm, bad);
+                mirror_df_kernel<<<grid_for(mm, 1024, sm_grid(8)), 256, 0, t>>>(Wq, m);
+                finish_df_kernel<<<grid_for(mm, 1024, sm_grid(8)), 256, 0, t>>>(Sq, mm, bad);
                 LSS_LAUNCH_CHECK();
             }
             for (int i = 0; i < ns; ++i) {
@@ -443,7 +443,7 @@ void launch_stiff_to_fp32(int64_t count, const double *src, float *dst, cudaStre
 {
     if (count > 0 && (!src || !dst)) fail(LSS_ERR_INTERNAL, "FP32 conversion launched without its arrays");
     if (count == 0) return;
-    to_fp32_kernel<<<grid_for(count, 256, 152 * 8), 256, 0, s>>>(count, src, dst);
+    to_fp32_kernel<<<grid_for(count, 256, sm_grid(8)), 256, 0, s>>>(count, src, dst);
     LSS_LAUNCH_CHECK();
 }
 

@@ -78,5 +78,7 @@ def build_generator(force: bool = False, verbose: bool = False) -> str:
     gsrc = os.path.join(_paths.CSRC, "gen_elasticity.cpp")
     glib = _paths.gen_lib_path()
     if force or _stale(glib, [gsrc]):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", gsrc, "-o", glib], verbose)
+        # no FMA contraction: the x86 and aarch64 builds assemble bit-identical matrices
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", gsrc, "-o", glib],
+             verbose)
     return glib

@@ -10,10 +10,16 @@ Two independent restatements of the reference's stiff-DOF selection
 Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` import this module; the product never does.
 
-Parity status: UNPINNED.  The reference ships no golden vectors or
-known-answer tests for this path and cannot be compiled here, so both
-restatements follow the cited reference code and are cross-checked against
-each other and against the committed fixtures in tests/golden/.
+Parity status: the selection is PINNED to the reference's own code.  The
+reference ships no golden vectors or known-answer tests for this path and its
+solver cannot be built here (hypre, cuDSS, MPI), but its selection stage can:
+``oracle/build_ref.py`` compiles GPUHybrid::select_bad_dofs and the three
+post-processing passes from the reference sources (thrust host backend) into
+``oracle/_ref/libgpuhybrid_ref.so``, wrapped by ``ref_select_pipeline``
+below.  tests/golden/ref_selection.npz holds that build's outputs
+(tests/golden/make_ref_golden.py), and the CPU tests require the C and numpy
+restatements to reproduce them.  The rest of the method (MAS, stiff factor,
+PCG) stays a restatement: those parts need hypre / cuDSS / CUDA.
 """
 from __future__ import annotations
 
@@ -499,3 +505,57 @@ class CpuSolver:
         if getattr(self, "h", None):
             lib().lsso_solver_destroy(self.h)
             self.h = None
+
+
+# --------------------------------------------------------------------------
+# the reference's own selection code, compiled on the host (oracle/build_ref.py)
+# --------------------------------------------------------------------------
+
+_ref_lib = None
+
+
+def ref_lib():
+    """oracle/_ref/libgpuhybrid_ref.so, built on first use; None when neither
+    the reference checkout nor its extracted sources are present."""
+    global _ref_lib
+    if _ref_lib is None:
+        from oracle import build_ref
+        path = build_ref.build()
+        if path is None:
+            return None
+        L = C.CDLL(path)
+        L.lssref_select.argtypes = [C.c_int32, _i32p, _i32p, _f64p, C.c_double, C.c_double, C.c_int32,
+                                    C.c_double, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                    _i32p, _i32p, _i32p, _i32p, _i32p, _f64p, C.c_char_p, C.c_int32]
+        L.lssref_select.restype = C.c_int32
+        _ref_lib = L
+    return _ref_lib
+
+
+def ref_select_pipeline(A, params: dict):
+    """GPUHybrid::factorize's selection stage run by the reference's own code
+    (GPUHybrid.cu:215-238 orchestrating :691-991).  Returns the GMM selection,
+    the subdomains in the reference's order, and the GMM statistics of its
+    "[bad_dof_selection]" log line."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("the reference build (oracle/_ref) is not available")
+    p = dict(DEFAULTS)
+    p.update(params)
+    n, indptr, indices, data = _csc(A)
+    raw = np.zeros(max(n, 1), np.int32)
+    sub_off = np.zeros(n + 2, np.int32)
+    sub_dofs = np.zeros(max(n, 1), np.int32)
+    nraw, nsub = C.c_int32(0), C.c_int32(0)
+    stats = np.zeros(8)
+    err = C.create_string_buffer(512)
+    st = L.lssref_select(n, _p(indptr, _i32p), _p(indices, _i32p), _p(data, _f64p), p["gmm_jump_threshold"],
+                         p["gmm_tol"], p["max_gmm_iterations"], p["conditioning_threshold"],
+                         int(p["decompose_subdomains"]), p["min_subdomain_size"], p["max_subdomain_size"],
+                         int(p["expand_subdomains"]), _p(raw, _i32p), C.byref(nraw), _p(sub_off, _i32p),
+                         _p(sub_dofs, _i32p), C.byref(nsub), _p(stats, _f64p), err, 512)
+    if st != 0:
+        raise RuntimeError("reference selection failed: " + err.value.decode())
+    subs = [sub_dofs[sub_off[k]:sub_off[k + 1]].copy() for k in range(nsub.value)]
+    keys = ["global_mean", "global_var", "mean0", "mean1", "var0", "var1", "gmm_iters", "num_selected"]
+    return raw[:nraw.value].copy(), subs, dict(zip(keys, stats.tolist()))

@@ -12,8 +12,8 @@ row-norm checksum, the GMM statistics, the raw GMM selection and the final
 post-processed stiff set with its subdomains -- produced by the C oracle and
 required to agree exactly with the independent numpy restatement.
 
-Run from the repository root, in a container that has the reference mounted:
-    python tests/golden/make_golden.py /root/reference
+Run from the repository root with the path of a reference checkout:
+    python tests/golden/make_golden.py <reference checkout>
 """
 import json
 import os
@@ -87,4 +87,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])
