@@ -202,6 +202,8 @@ void launch_mas_level0(const MasDev &m, const void *inv0, const void *u, bool fp
 // ---------------------------------------------------------------- stiff blocks
 struct StiffDev {
     int32_t nsub = 0, ndof = 0;
+    int32_t ndof_dense = 0;            // DOFs j < ndof_dense belong to subdomains with a dense inverse
+                                       // (the rest to the multifrontal factor, multifrontal.hpp)
     const int32_t *dofs = nullptr;     // ndof permuted scalar ids, grouped by subdomain
     const int32_t *sub_of = nullptr;   // ndof
     const int32_t *off = nullptr;      // nsub+1 (into dofs)
@@ -212,13 +214,15 @@ struct StiffDev {
 };
 
 void launch_stiff_extract(const BsrDev &A, const StiffDev &S, double *stage, cudaStream_t s);
-void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, const int64_t *h_inv_off,
-                         double *inv, int *bad, cudaStream_t s);
+// dense inverses of the subdomains 0 .. nsub-1 (each at most STIFF_DENSE_MAX DOFs)
+constexpr int STIFF_DENSE_MAX = 160;
+void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, double *inv, int *bad,
+                         cudaStream_t s);
 void launch_stiff_to_fp32(int64_t count, const double *src, float *dst, cudaStream_t s);
 // t = r_S - (A z)_S   (residual = true) or t = r_S
 void launch_stiff_gather(const BsrDev &A, const StiffDev &S, const double *r, const double *z, bool residual,
                          const int *done, cudaStream_t s);
-// z_S += Inv t
+// z_S += Inv t over the subdomains with a dense inverse
 // z32, z_lo (optional): FP32 shadow of z and its remainder, updated at the
 // DOFs the correction changes
 void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done, cudaStream_t s,

@@ -1,0 +1,622 @@
+// Numeric factorization and solve of the multifrontal stiff-block factor
+// (sm_103a, FP64).  The symbolic structure comes from mf_symbolic.cpp.
+//
+// Factorization, per tree level (leaves first):
+//   extend-add      one CTA per front, children summed in ascending order
+//   small fronts    f <= MF_SMEM_F: one CTA sweeps the own pivots in shared memory
+//   large fronts    blocked sweep over 32-pivot panels, batched over the
+//                   level's fronts: pivot-block inverse, panel P = S[:,K] D^-1,
+//                   rank-32 update of the upper-triangle tiles, panel write-back;
+//                   then the swept rows are mirrored into the lower triangle
+// (the original entries are assembled into every front once, before level 0).
+// Solve: one forward launch per level (leaves first), one backward launch per
+// level (root first), one scatter; each output is a fixed-order dot product
+// over a column of the front (coalesced across the 32 outputs of a warp).
+#include <algorithm>
+
+#include "device_common.cuh"
+#include "multifrontal.hpp"
+
+namespace lss {
+namespace {
+
+constexpr int PW = 32;  // panel width / outputs per CTA
+
+struct MfView {
+    const int32_t *p0, *s, *u, *woff, *bnd_off, *bnd_pos, *child_off, *child, *ea_map, *front_of_pos, *pos2j,
+        *j2pos, *poff;
+    const int64_t *foff;
+    int32_t j_base, npos;
+};
+
+__device__ __forceinline__ int find_front(const MfWork &w, int64_t cta)
+{
+    int lo = 0, hi = w.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (w.prefix[mid] <= cta) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// original entries: warp per position, upper triangle of its front row
+template <int BD>
+__global__ void __launch_bounds__(256) mf_assemble_kernel(BsrDev A, StiffDev S, MfView v, double *__restrict__ F)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (p >= v.npos) return;
+    const int32_t N = v.front_of_pos[p], p0 = v.p0[N], s = v.s[N], u = v.u[N], f = s + u;
+    const int32_t fi = (int32_t)p - p0;
+    const int32_t j = v.pos2j[p], d = S.dofs[j], sub = S.sub_of[j], lo = S.off[sub], m = S.off[sub + 1] - lo;
+    const int32_t *list = S.dofs + lo;
+    const int32_t *bp = v.bnd_pos + v.bnd_off[N];
+    double *row = F + v.foff[N] + (int64_t)fi * f;
+    const int32_t I = d / BD, comp = d % BD;
+    const int32_t b = A.rows[I], len = A.rows[I + 1] - b;
+    const double *vals = A.vals + (int64_t)b * BD * BD;
+    for (int32_t l = lane; l < len; l += 32) {
+        const int32_t J = A.cols[b + l];
+#pragma unroll
+        for (int k = 0; k < BD; ++k) {
+            const int32_t col = J * BD + k;
+            int32_t a = 0, e = m;
+            while (a < e) {
+                const int32_t mid = (a + e) >> 1;
+                if (list[mid] < col) a = mid + 1;
+                else e = mid;
+            }
+            if (a >= m || list[a] != col) continue;
+            const int32_t q = v.j2pos[lo + a - v.j_base];
+            if (q < p0) continue;  // an earlier front assembled this entry
+            int32_t fj;
+            if (q < p0 + s) {
+                fj = q - p0;
+                if (fj < fi) continue;  // upper triangle
+            } else {
+                int32_t x = 0, y = u;
+                while (x < y) {
+                    const int32_t mid = (x + y) >> 1;
+                    if (bp[mid] < q) x = mid + 1;
+                    else y = mid;
+                }
+                if (x >= u || bp[x] != q) continue;
+                fj = s + x;
+            }
+            row[fj] = vals[(int64_t)(comp * BD + k) * len + l];
+        }
+    }
+}
+
+// children's Schur complements into the parent (upper triangle), in child order
+__global__ void __launch_bounds__(256) mf_extend_add_kernel(MfView v, MfWork w, double *__restrict__ F)
+{
+    const int32_t N = w.front[blockIdx.x];
+    const int32_t fN = v.s[N] + v.u[N];
+    double *Fn = F + v.foff[N];
+    for (int32_t ci = v.child_off[N]; ci < v.child_off[N + 1]; ++ci) {
+        const int32_t c = v.child[ci], sc = v.s[c], uc = v.u[c], fc = sc + uc;
+        const double *Fc = F + v.foff[c];
+        const int32_t *map = v.ea_map + v.bnd_off[c];
+        const int64_t total = (int64_t)uc * uc;
+        for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+            const int32_t a = (int32_t)(e / uc), bb = (int32_t)(e % uc);
+            if (a > bb) continue;
+            Fn[(int64_t)map[a] * fN + map[bb]] += Fc[(int64_t)(sc + a) * fc + sc + bb];
+        }
+        __syncthreads();
+    }
+}
+
+// sweep of the leading `np` pivots of the n x n matrix S (ld, shared memory,
+// full square): S[t][c] -= S[t][p] S[p][c] / S[p][p] off the pivot row and
+// column, the pivot row and column scaled, the pivot replaced by -1 / piv
+__device__ void sweep_leading(double *S, int ld, int n, int np, double *col, double *scol, int *bad)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+    for (int p = 0; p < np; ++p) {
+        const double piv = S[p * ld + p];
+        const double rpiv = 1.0 / piv;
+        for (int t = tid; t < n; t += nt) {
+            const double cv = (t == p) ? 0.0 : S[t * ld + p];
+            col[t] = cv;
+            scol[t] = cv * rpiv;
+        }
+        if (tid == 0 && (!isfinite(piv) || piv == 0.0)) atomicOr(bad, 16);
+        __syncthreads();
+        for (int t = wid; t < n; t += nw) {
+            if (t == p) continue;
+            const double st = scol[t];
+            for (int c = lane; c < n; c += 32)
+                if (c != p) S[t * ld + c] -= st * col[c];
+        }
+        __syncthreads();
+        for (int t = tid; t < n; t += nt) {
+            if (t == p) S[p * ld + p] = -rpiv;
+            else {
+                S[t * ld + p] = scol[t];
+                S[p * ld + t] = scol[t];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) mf_sweep_small_kernel(MfView v, MfWork w, double *__restrict__ F, int *bad)
+{
+    extern __shared__ double sm[];
+    const int32_t N = w.front[blockIdx.x];
+    const int s = v.s[N], f = s + v.u[N], ld = f + 1;
+    double *S = sm, *col = sm + f * ld, *scol = col + f;
+    double *g = F + v.foff[N];
+    for (int idx = threadIdx.x; idx < f * f; idx += blockDim.x) {
+        const int r = idx / f, c = idx % f;
+        S[r * ld + c] = (r <= c) ? g[(int64_t)r * f + c] : g[(int64_t)c * f + r];
+    }
+    __syncthreads();
+    sweep_leading(S, ld, f, s, col, scol, bad);
+    for (int idx = threadIdx.x; idx < f * f; idx += blockDim.x) {
+        const int r = idx / f, c = idx % f;
+        const double val = S[r * ld + c];
+        if (!isfinite(val)) atomicOr(bad, 32);
+        g[(int64_t)r * f + c] = val;
+    }
+}
+
+// ---- blocked sweep of the large fronts of a level (upper-triangle storage)
+
+__device__ __forceinline__ double up(const double *Fn, int f, int r, int c)
+{
+    return r <= c ? Fn[(int64_t)r * f + c] : Fn[(int64_t)c * f + r];
+}
+
+// Dinv = (S[K][K])^-1 for the panel K = [k0, k0 + t)
+__global__ void __launch_bounds__(256) mf_blk_diag_kernel(MfView v, MfWork w, const double *__restrict__ F, int k0,
+                                                          double *__restrict__ Dinv, int *bad)
+{
+    __shared__ double D[PW * (PW + 1)], col[PW], scol[PW];
+    const int i = blockIdx.x;
+    const int32_t N = w.front[i];
+    const int s = v.s[N], f = s + v.u[N];
+    if (s <= k0) return;
+    const int t = min(PW, s - k0), ld = PW + 1;
+    const double *Fn = F + v.foff[N];
+    for (int e = threadIdx.x; e < t * t; e += blockDim.x) {
+        const int r = e / t, c = e % t;
+        D[r * ld + c] = up(Fn, f, k0 + r, k0 + c);
+    }
+    __syncthreads();
+    sweep_leading(D, ld, t, t, col, scol, bad);
+    for (int e = threadIdx.x; e < PW * PW; e += blockDim.x) {
+        const int r = e / PW, c = e % PW;
+        Dinv[(int64_t)i * PW * PW + e] = (r < t && c < t) ? -D[r * ld + c] : 0.0;
+    }
+}
+
+// P[r][:] = S[r][K] Dinv for every row r outside K (one thread per row)
+__global__ void __launch_bounds__(128) mf_blk_panel_kernel(MfView v, MfWork w, const double *__restrict__ F, int k0,
+                                                           const double *__restrict__ Dinv, double *__restrict__ P)
+{
+    __shared__ double Ds[PW * PW];
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    const int s = v.s[N], f = s + v.u[N];
+    if (s <= k0) return;
+    const int t = min(PW, s - k0);
+    for (int e = threadIdx.x; e < PW * PW; e += blockDim.x) Ds[e] = Dinv[(int64_t)i * PW * PW + e];
+    __syncthreads();
+    const int r = (int)(blockIdx.x - w.prefix[i]) * blockDim.x + threadIdx.x;
+    if (r >= f || (r >= k0 && r < k0 + t)) return;
+    const double *Fn = F + v.foff[N];
+    double acc[PW];
+#pragma unroll
+    for (int c = 0; c < PW; ++c) acc[c] = 0.0;
+    for (int q = 0; q < t; ++q) {
+        const double a = up(Fn, f, r, k0 + q);
+#pragma unroll
+        for (int c = 0; c < PW; ++c) acc[c] += a * Ds[q * PW + c];
+    }
+    double *Pr = P + v.poff[N] + (int64_t)r * PW;
+#pragma unroll
+    for (int c = 0; c < PW; ++c) Pr[c] = c < t ? acc[c] : 0.0;
+}
+
+// S[a][b] -= sum_q P[a][q] S[k0+q][b] on the upper-triangle 32 x 32 tiles,
+// every entry with a and b outside the panel K = [k0, k0 + t) (the last panel
+// can end inside its tile, whose remaining rows are boundary rows that still
+// take the update); four rows per thread
+__global__ void __launch_bounds__(256) mf_blk_update_kernel(MfView v, MfWork w, double *__restrict__ F, int k0,
+                                                            const double *__restrict__ P)
+{
+    __shared__ double Pt[32][PW + 1], Kt[PW][33];
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    const int s = v.s[N], f = s + v.u[N];
+    if (s <= k0) return;
+    const int t = min(PW, s - k0);
+    const int T = (f + 31) / 32, bk = k0 / 32;
+    int tile = (int)(blockIdx.x - w.prefix[i]), bi = 0;
+    while (tile >= T - bi) {
+        tile -= T - bi;
+        ++bi;
+    }
+    const int bj = bi + tile;
+    if ((bi == bk || bj == bk) && t == PW) return;  // a full panel covers its whole tile
+    double *Fn = F + v.foff[N];
+    const double *Pn = P + v.poff[N];
+    const int i0 = bi * 32, j0 = bj * 32;
+    for (int e = threadIdx.x; e < 32 * PW; e += blockDim.x) {
+        const int r = e / PW, q = e % PW;
+        const int a = i0 + r;
+        Pt[r][q] = (a < f && q < t) ? Pn[(int64_t)a * PW + q] : 0.0;
+    }
+    if (j0 < k0) {  // S[k0+q][b] = Fn[b][k0+q]
+        for (int e = threadIdx.x; e < 32 * PW; e += blockDim.x) {
+            const int cc = e / PW, q = e % PW;
+            const int b = j0 + cc;
+            Kt[q][cc] = (b < f && q < t) ? Fn[(int64_t)b * f + k0 + q] : 0.0;
+        }
+    } else {
+        for (int e = threadIdx.x; e < 32 * PW; e += blockDim.x) {
+            const int q = e / 32, cc = e % 32;
+            const int b = j0 + cc;
+            Kt[q][cc] = (b < f && q < t) ? Fn[(int64_t)(k0 + q) * f + b] : 0.0;
+        }
+    }
+    __syncthreads();
+    const int cc = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int b = j0 + cc;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 8
+    for (int q = 0; q < PW; ++q) {
+        const double kq = Kt[q][cc];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc[r] += Pt[wid + 8 * r][q] * kq;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int a = i0 + wid + 8 * r;
+        if (a >= f || b >= f || b < a) continue;
+        if ((a >= k0 && a < k0 + t) || (b >= k0 && b < k0 + t)) continue;  // the panel itself
+        Fn[(int64_t)a * f + b] -= acc[r];
+    }
+}
+
+// swept panel rows: S[r][K] = P[r] (r before K), S[K][r] = P[r] (after), S[K][K] = -Dinv
+__global__ void __launch_bounds__(256) mf_blk_write_kernel(MfView v, MfWork w, double *__restrict__ F, int k0,
+                                                           const double *__restrict__ P,
+                                                           const double *__restrict__ Dinv)
+{
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    const int s = v.s[N], f = s + v.u[N];
+    if (s <= k0) return;
+    const int t = min(PW, s - k0);
+    const int64_t idx = (int64_t)(blockIdx.x - w.prefix[i]) * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)f * PW) return;
+    const int r = (int)(idx / PW), c = (int)(idx % PW);
+    if (c >= t) return;
+    double *Fn = F + v.foff[N];
+    const double *Pn = P + v.poff[N];
+    if (r >= k0 && r < k0 + t) {
+        if (r - k0 <= c) Fn[(int64_t)r * f + k0 + c] = -Dinv[(int64_t)i * PW * PW + (r - k0) * PW + c];
+    } else if (r < k0) {
+        Fn[(int64_t)r * f + k0 + c] = Pn[(int64_t)r * PW + c];
+    } else {
+        Fn[(int64_t)(k0 + c) * f + r] = Pn[(int64_t)r * PW + c];
+    }
+}
+
+// lower triangle of the swept columns: Fn[r][c] = Fn[c][r] for c < min(r, s)
+__global__ void __launch_bounds__(256) mf_mirror_kernel(MfView v, MfWork w, double *__restrict__ F, int *bad)
+{
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    const int s = v.s[N], f = s + v.u[N];
+    const int64_t idx = (int64_t)(blockIdx.x - w.prefix[i]) * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)f * s) return;
+    const int r = (int)(idx / s), c = (int)(idx % s);
+    double *Fn = F + v.foff[N];
+    if (c < r) Fn[(int64_t)r * f + c] = Fn[(int64_t)c * f + r];
+    else if (!isfinite(Fn[(int64_t)r * f + c])) atomicOr(bad, 32);
+}
+
+// ---- solve
+
+// w_own = t[own] + children's contributions; c = w_bnd - P w_own for 32 outputs
+__global__ void __launch_bounds__(256) mf_forward_kernel(MfView v, MfWork w, const StiffDev S,
+                                                         const double *__restrict__ F, double *__restrict__ W,
+                                                         const int *done)
+{
+    if (done && *done) return;
+    extern __shared__ double sm[];
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    const int s = v.s[N], u = v.u[N], f = s + u;
+    const int chunk = (int)(blockIdx.x - w.prefix[i]);
+    double *wown = sm, *wb = sm + s, *red = wb + PW;
+    const int r0 = s + chunk * PW;  // first front row of this CTA's outputs
+    for (int k = threadIdx.x; k < s; k += blockDim.x) wown[k] = S.t[v.pos2j[v.p0[N] + k]];
+    if (threadIdx.x < PW) wb[threadIdx.x] = 0.0;
+    __syncthreads();
+    for (int32_t ci = v.child_off[N]; ci < v.child_off[N + 1]; ++ci) {
+        const int32_t c = v.child[ci], uc = v.u[c];
+        const double *cw = W + v.woff[c] + v.s[c];
+        const int32_t *map = v.ea_map + v.bnd_off[c];
+        for (int e = threadIdx.x; e < uc; e += blockDim.x) {
+            const int m = map[e];
+            if (m < s) wown[m] += cw[e];
+            else if (m >= r0 && m < r0 + PW) wb[m - r0] += cw[e];
+        }
+        __syncthreads();
+    }
+    double *Wn = W + v.woff[N];
+    if (chunk == 0)
+        for (int k = threadIdx.x; k < s; k += blockDim.x) Wn[k] = wown[k];
+    if (u == 0) return;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int col = r0 + lane;
+    const double *Fn = F + v.foff[N];
+    double acc = 0.0;
+    if (col < f)
+        for (int k = wid; k < s; k += 8) acc += Fn[(int64_t)k * f + col] * wown[k];
+    red[wid * 32 + lane] = acc;
+    __syncthreads();
+    if (wid == 0 && col < f) {
+        double sum = 0.0;
+        for (int q = 0; q < 8; ++q) sum += red[q * 32 + lane];
+        Wn[col] = wb[lane] - sum;
+    }
+}
+
+// x_own = -S[:, own]^T [w_own; x_bnd] for 32 outputs
+__global__ void __launch_bounds__(256) mf_backward_kernel(MfView v, MfWork w, const double *__restrict__ F,
+                                                          const double *__restrict__ W, double *__restrict__ X,
+                                                          const int *done)
+{
+    if (done && *done) return;
+    extern __shared__ double sm[];
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    const int s = v.s[N], u = v.u[N], f = s + u;
+    const int chunk = (int)(blockIdx.x - w.prefix[i]);
+    double *vec = sm, *red = sm + f;
+    const double *Wn = W + v.woff[N];
+    const int32_t *bp = v.bnd_pos + v.bnd_off[N];
+    for (int k = threadIdx.x; k < f; k += blockDim.x) vec[k] = k < s ? Wn[k] : X[bp[k - s]];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int c = chunk * PW + lane;
+    const double *Fn = F + v.foff[N];
+    double acc = 0.0;
+    if (c < s)
+        for (int k = wid; k < f; k += 8) acc += Fn[(int64_t)k * f + c] * vec[k];
+    red[wid * 32 + lane] = acc;
+    __syncthreads();
+    if (wid == 0 && c < s) {
+        double sum = 0.0;
+        for (int q = 0; q < 8; ++q) sum += red[q * 32 + lane];
+        X[v.p0[N] + c] = -sum;
+    }
+}
+
+__global__ void mf_scatter_kernel(MfView v, const StiffDev S, const double *__restrict__ X, double *__restrict__ z,
+                                  float *__restrict__ z32, float *__restrict__ z_lo, const int *done)
+{
+    if (done && *done) return;
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= v.npos) return;
+    const int32_t d = S.dofs[v.pos2j[p]];
+    const double nz = z[d] + X[p];
+    z[d] = nz;
+    if (z32) {
+        const float h = (float)nz;
+        z32[d] = h;
+        if (z_lo) z_lo[d] = (float)(nz - (double)h);
+    }
+}
+
+}  // namespace
+
+int64_t MfFactor::bytes() const
+{
+    return (int64_t)(d_F_.bytes() + d_w_.bytes() + d_x_.bytes() + d_P_.bytes() + d_D_.bytes() + d_i32_.bytes() +
+                     d_i64_.bytes());
+}
+
+void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
+{
+    // one CTA holds a front's solve vector in shared memory (227 KB per CTA)
+    if ((size_t)(sym.max_f + 8 * 32) * sizeof(double) > 227 * 1024)
+        fail(LSS_ERR_UNSUPPORTED, "a stiff subdomain's top separator front (" + std::to_string(sym.max_f) +
+                                      " variables) exceeds the multifrontal solve's shared-memory limit");
+    sym_ = sym;
+    levels_.clear();
+    if (sym_.nfront == 0) {
+        d_F_.release();
+        return;
+    }
+    const MfSymbolic &M = sym_;
+    const int32_t nf = M.nfront;
+    // per-level work lists; P scratch offsets per large front within its level
+    std::vector<int32_t> poff(nf, 0);
+    std::vector<std::vector<int32_t>> lv_all(M.levels), lv_small(M.levels), lv_large(M.levels), lv_ea(M.levels);
+    for (int32_t id = 0; id < nf; ++id) {
+        const int h = M.height[id];
+        lv_all[h].push_back(id);
+        if (M.child_off[id + 1] > M.child_off[id]) lv_ea[h].push_back(id);
+        (M.s[id] + M.u[id] <= MF_SMEM_F ? lv_small : lv_large)[h].push_back(id);
+    }
+    int64_t pmax = 0;
+    size_t dmax = 0;
+    for (int h = 0; h < M.levels; ++h) {
+        int64_t acc = 0;
+        for (int32_t id : lv_large[h]) {
+            poff[id] = (int32_t)acc;
+            acc += (int64_t)(M.s[id] + M.u[id]) * PW;
+        }
+        pmax = std::max(pmax, acc);
+        dmax = std::max(dmax, lv_large[h].size());
+    }
+    std::vector<int32_t> i32;
+    std::vector<int64_t> i64;
+    auto put32 = [&](const std::vector<int32_t> &a) {
+        const size_t at = i32.size();
+        i32.insert(i32.end(), a.begin(), a.end());
+        return at;
+    };
+    const size_t a_p0 = put32(M.p0), a_s = put32(M.s), a_u = put32(M.u), a_woff = put32(M.woff),
+                 a_bo = put32(M.bnd_off), a_bp = put32(M.bnd_pos), a_co = put32(M.child_off), a_ch = put32(M.child),
+                 a_ea = put32(M.ea_map), a_fp = put32(M.front_of_pos), a_pj = put32(M.pos2j),
+                 a_jp = put32(M.j2pos), a_po = put32(poff);
+    const size_t a_fo = i64.size();
+    i64.insert(i64.end(), M.foff.begin(), M.foff.end());
+    struct Pending {
+        MfWork *w;
+        size_t fat, pat;
+    };
+    std::vector<Pending> pend;
+    levels_.resize(M.levels);
+    auto make = [&](MfWork &w, const std::vector<int32_t> &fronts, auto ctas_of) {
+        w.count = (int32_t)fronts.size();
+        const size_t fat = put32(fronts);
+        const size_t pat = i64.size();
+        int64_t acc = 0;
+        i64.push_back(0);
+        for (int32_t id : fronts) {
+            acc += ctas_of(id);
+            i64.push_back(acc);
+        }
+        w.ctas = acc;
+        pend.push_back({&w, fat, pat});
+    };
+    auto F_of = [&](int32_t id) { return (int64_t)M.s[id] + M.u[id]; };
+    for (int h = 0; h < M.levels; ++h) {
+        Level &L = levels_[h];
+        make(L.ea, lv_ea[h], [](int32_t) { return (int64_t)1; });
+        make(L.small, lv_small[h], [](int32_t) { return (int64_t)1; });
+        make(L.diag, lv_large[h], [](int32_t) { return (int64_t)1; });
+        make(L.panel, lv_large[h], [&](int32_t id) { return (F_of(id) + 127) / 128; });
+        make(L.update, lv_large[h], [&](int32_t id) {
+            const int64_t T = (F_of(id) + 31) / 32;
+            return T * (T + 1) / 2;
+        });
+        make(L.write, lv_large[h], [&](int32_t id) { return (F_of(id) * PW + 255) / 256; });
+        make(L.mirror, lv_large[h], [&](int32_t id) { return (F_of(id) * M.s[id] + 255) / 256; });
+        make(L.fwd, lv_all[h], [&](int32_t id) { return std::max<int64_t>(1, (M.u[id] + PW - 1) / PW); });
+        make(L.bwd, lv_all[h], [&](int32_t id) { return (int64_t)(M.s[id] + PW - 1) / PW; });
+        for (int32_t id : lv_large[h]) L.max_s_large = std::max(L.max_s_large, M.s[id]);
+    }
+    d_i32_.upload(i32, st);
+    d_i64_.upload(i64, st);
+    const int32_t *b32 = d_i32_.data();
+    const int64_t *b64 = d_i64_.data();
+    for (const Pending &q : pend) {
+        q.w->front = b32 + q.fat;
+        q.w->prefix = b64 + q.pat;
+    }
+    p0_ = b32 + a_p0;
+    s_ = b32 + a_s;
+    u_ = b32 + a_u;
+    woff_ = b32 + a_woff;
+    bnd_off_ = b32 + a_bo;
+    bnd_pos_ = b32 + a_bp;
+    child_off_ = b32 + a_co;
+    child_ = b32 + a_ch;
+    ea_map_ = b32 + a_ea;
+    front_of_pos_ = b32 + a_fp;
+    pos2j_ = b32 + a_pj;
+    j2pos_ = b32 + a_jp;
+    poff_ = b32 + a_po;
+    foff_ = b64 + a_fo;
+    // shared memory of the solve kernels, set here: solve() runs inside graph captures
+    const size_t fsmem = (size_t)(M.max_s + PW + 8 * 32) * sizeof(double);
+    const size_t bsmem = (size_t)(M.max_f + 8 * 32) * sizeof(double);
+    LSS_CUDA(cudaFuncSetAttribute(mf_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+    LSS_CUDA(cudaFuncSetAttribute(mf_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem));
+    d_F_.resize(M.elems);
+    d_w_.resize(std::max<int64_t>(M.welems, 1));
+    d_x_.resize(std::max<int32_t>(M.npos, 1));
+    d_P_.resize(std::max<int64_t>(pmax, 1));
+    d_D_.resize(std::max<size_t>(dmax, 1) * PW * PW);
+}
+
+namespace {
+MfView make_view(const int32_t *p0, const int32_t *s, const int32_t *u, const int32_t *woff, const int32_t *bo,
+                 const int32_t *bp, const int32_t *co, const int32_t *ch, const int32_t *ea, const int32_t *fp,
+                 const int32_t *pj, const int32_t *jp, const int32_t *po, const int64_t *fo, int32_t j_base,
+                 int32_t npos)
+{
+    MfView v;
+    v.p0 = p0; v.s = s; v.u = u; v.woff = woff; v.bnd_off = bo; v.bnd_pos = bp; v.child_off = co; v.child = ch;
+    v.ea_map = ea; v.front_of_pos = fp; v.pos2j = pj; v.j2pos = jp; v.poff = po; v.foff = fo;
+    v.j_base = j_base; v.npos = npos;
+    return v;
+}
+}  // namespace
+
+void MfFactor::factorize(const BsrDev &A, const StiffDev &S, int *bad, cudaStream_t st)
+{
+    if (sym_.nfront == 0) return;
+    const MfView v = make_view(p0_, s_, u_, woff_, bnd_off_, bnd_pos_, child_off_, child_, ea_map_, front_of_pos_,
+                               pos2j_, j2pos_, poff_, foff_, sym_.j_base, sym_.npos);
+    double *F = d_F_.data();
+    d_F_.zero(st);
+    const unsigned ga = (unsigned)(((int64_t)sym_.npos * 32 + 255) / 256);
+    switch (A.bd) {
+    case 1: mf_assemble_kernel<1><<<ga, 256, 0, st>>>(A, S, v, F); break;
+    case 2: mf_assemble_kernel<2><<<ga, 256, 0, st>>>(A, S, v, F); break;
+    default: mf_assemble_kernel<3><<<ga, 256, 0, st>>>(A, S, v, F); break;
+    }
+    LSS_LAUNCH_CHECK();
+    const size_t small_smem = (size_t)(MF_SMEM_F * (MF_SMEM_F + 1) + 2 * MF_SMEM_F) * sizeof(double);
+    LSS_CUDA(cudaFuncSetAttribute(mf_sweep_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
+    for (const Level &L : levels_) {
+        if (L.ea.count) {
+            mf_extend_add_kernel<<<L.ea.count, 256, 0, st>>>(v, L.ea, F);
+            LSS_LAUNCH_CHECK();
+        }
+        if (L.small.count) {
+            mf_sweep_small_kernel<<<L.small.count, 256, small_smem, st>>>(v, L.small, F, bad);
+            LSS_LAUNCH_CHECK();
+        }
+        if (L.diag.count) {
+            for (int k0 = 0; k0 < L.max_s_large; k0 += PW) {
+                mf_blk_diag_kernel<<<L.diag.count, 256, 0, st>>>(v, L.diag, F, k0, d_D_.data(), bad);
+                mf_blk_panel_kernel<<<(unsigned)L.panel.ctas, 128, 0, st>>>(v, L.panel, F, k0, d_D_.data(),
+                                                                            d_P_.data());
+                mf_blk_update_kernel<<<(unsigned)L.update.ctas, 256, 0, st>>>(v, L.update, F, k0, d_P_.data());
+                mf_blk_write_kernel<<<(unsigned)L.write.ctas, 256, 0, st>>>(v, L.write, F, k0, d_P_.data(),
+                                                                            d_D_.data());
+                LSS_LAUNCH_CHECK();
+            }
+            mf_mirror_kernel<<<(unsigned)L.mirror.ctas, 256, 0, st>>>(v, L.mirror, F, bad);
+            LSS_LAUNCH_CHECK();
+        }
+    }
+}
+
+void MfFactor::solve(const StiffDev &S, double *z, float *z32, float *z_lo, const int *done, cudaStream_t st)
+{
+    if (sym_.nfront == 0) return;
+    const MfView v = make_view(p0_, s_, u_, woff_, bnd_off_, bnd_pos_, child_off_, child_, ea_map_, front_of_pos_,
+                               pos2j_, j2pos_, poff_, foff_, sym_.j_base, sym_.npos);
+    const size_t fsmem = (size_t)(sym_.max_s + PW + 8 * 32) * sizeof(double);
+    const size_t bsmem = (size_t)(sym_.max_f + 8 * 32) * sizeof(double);
+    for (const Level &L : levels_) {
+        mf_forward_kernel<<<(unsigned)L.fwd.ctas, 256, fsmem, st>>>(v, L.fwd, S, d_F_.data(), d_w_.data(), done);
+        LSS_LAUNCH_CHECK();
+    }
+    for (int h = (int)levels_.size() - 1; h >= 0; --h) {
+        const Level &L = levels_[h];
+        mf_backward_kernel<<<(unsigned)L.bwd.ctas, 256, bsmem, st>>>(v, L.bwd, d_F_.data(), d_w_.data(), d_x_.data(),
+                                                                      done);
+        LSS_LAUNCH_CHECK();
+    }
+    mf_scatter_kernel<<<(unsigned)((sym_.npos + 255) / 256), 256, 0, st>>>(v, S, d_x_.data(), z, z32, z_lo, done);
+    LSS_LAUNCH_CHECK();
+}
+
+}  // namespace lss

@@ -3,11 +3,13 @@
 
 #include <chrono>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
 #include "kernels.hpp"
 #include "lss_common.hpp"
+#include "multifrontal.hpp"
 #include "pattern.hpp"
 #include "postproc.hpp"
 
@@ -125,6 +127,8 @@ private:
     DBuf<int64_t> d_sinvoff_;
     DBuf<double> d_sinv_, d_st_;
     DBuf<float> d_sinv32_;
+    std::unique_ptr<MfFactor> mf_;  // subdomains above STIFF_DENSE_MAX DOFs
+    void stiff_correct(double *z, const int *done, float *z32 = nullptr, float *z_lo = nullptr);
     // PCG
     DBuf<double> d_x_, d_b_, d_r_, d_p_, d_z_, d_ap_, d_w_, d_tmp_;
     DBuf<float> d_z32_;  // mixed precision: FP32 shadow of z, input of the FP32 residual SpMV
@@ -152,6 +156,7 @@ private:
     int graph_iters_ = 0;
     size_t graph_nodes_ = 0;
     PinnedBuf pin_;
+    cudaEvent_t copy_ev_[2] = {nullptr, nullptr};  // staged uploads: the two pinned halves
 
     // last solve
     int num_iterations_ = 0;
