@@ -154,6 +154,16 @@ lss_status lss_subdomains(const lss_solver *s, int32_t *offsets, int32_t cap_off
 lss_status lss_partition(const lss_solver *s, int32_t *perm, int32_t cap_perm,
                          int32_t *part_offsets, int32_t cap_offsets, int32_t *nparts);
 
+/* The same partition computed from a pattern alone, on the host (no device
+ * needed): the graph_partition step of MASSolverImpl::factorize
+ * (MASSolver.cu:389-406 calling GraphPartition.cpp:176-289, KaMinPar with
+ * k = ceil(n / 30) parts of at most 32 block rows) as this library does it.
+ * threads <= 0: all host cores (the result does not depend on it).  With
+ * perm == NULL or part_offsets == NULL only *nparts is written. */
+lss_status lss_partition_pattern(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                                 int32_t block_size, int32_t threads, int32_t *perm, int32_t cap_perm,
+                                 int32_t *part_offsets, int32_t cap_offsets, int32_t *nparts);
+
 /* ---- operator-level entry points (parity tests and benchmarks) ---------- */
 
 /* rn[i] = sum |values| of outer slice i, on the GPU (GPUHybrid.cu:753-765). */

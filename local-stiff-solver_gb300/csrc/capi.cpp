@@ -299,6 +299,25 @@ lss_status lss_partition(const lss_solver *s, int32_t *perm, int32_t cap_perm, i
     return LSS_OK;
 }
 
+lss_status lss_partition_pattern(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                                 int32_t block_size, int32_t threads, int32_t *perm, int32_t cap_perm,
+                                 int32_t *part_offsets, int32_t cap_offsets, int32_t *nparts)
+{
+    if (n <= 0 || nnz < 0 || !outer || !inner || block_size < 1 || !nparts) {
+        g_create_error = "invalid partition arguments";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    return guarded(nullptr, [&]() {
+        const lss::Pattern P = lss::analyze_pattern(n, nnz, outer, inner, block_size, threads);
+        *nparts = (int32_t)P.part.part_offsets.size() - 1;
+        if (!perm || !part_offsets) return;
+        if (cap_perm < (int32_t)P.part.perm.size() || cap_offsets < (int32_t)P.part.part_offsets.size())
+            lss::fail(LSS_ERR_BUFFER_TOO_SMALL, "partition output buffers too small");
+        std::memcpy(perm, P.part.perm.data(), P.part.perm.size() * sizeof(int32_t));
+        std::memcpy(part_offsets, P.part.part_offsets.data(), P.part.part_offsets.size() * sizeof(int32_t));
+    });
+}
+
 lss_status lss_op_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer, const double *values, double *rn)
 {
     if (n <= 0 || nnz < 0 || !outer || !values || !rn) return LSS_ERR_INVALID_ARGUMENT;

@@ -71,6 +71,8 @@ def load(path: str | None = None):
     L.lss_set_parameters.argtypes = [vp, C.c_char_p]
     L.lss_get_info.argtypes = [vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]
     L.lss_name.argtypes = [vp, C.c_char_p, C.c_size_t]
+    L.lss_partition_pattern.argtypes = [C.c_int32, C.c_int64, _i32p, _i32p, C.c_int32, C.c_int32, _i32p, C.c_int32,
+                                        _i32p, C.c_int32, _i32p]
     L.lss_analyze_pattern.argtypes = [vp, C.c_int32, C.c_int64, _i32p, _i32p]
     L.lss_factorize.argtypes = [vp, C.c_int32, C.c_int64, _i32p, _i32p, _f64p]
     L.lss_factorize_device.argtypes = [vp, vp, vp]
@@ -138,6 +140,22 @@ def row_l1_norms(A):
     if st:
         raise LssError(st, L.lss_last_error(None).decode())
     return out
+
+
+def partition_pattern(A, block_size: int, threads: int = 0):
+    """The MAS partition of A's block graph, computed on the host
+    (lss_partition_pattern): (perm[old block] = new block, part_offsets)."""
+    L = load()
+    n, outer, inner, _ = _csc_arrays(A)
+    nparts = C.c_int32(0)
+    nb = n // block_size
+    perm = np.zeros(max(nb, 1), np.int32)
+    offs = np.zeros(nb + 2, np.int32)
+    st = L.lss_partition_pattern(n, len(inner), _p(outer, _i32p), _p(inner, _i32p), block_size, threads,
+                                 _p(perm, _i32p), len(perm), _p(offs, _i32p), len(offs), C.byref(nparts))
+    if st != 0:
+        raise LssError(st, L.lss_last_error(None).decode())
+    return perm[:nb].copy(), offs[:nparts.value + 1].copy()
 
 
 def solve_batched_device(solvers, d_b, d_x, nrhs: int, threads: int = 0) -> np.ndarray:

@@ -9,7 +9,9 @@ connected :972-991, decompose_subdomains_to_disjoint_subsets :691-735, with
 disjointSet from Hybrid.hpp:223-260) is std + Eigen's InnerIterator.  This
 script copies those definitions verbatim, located by their signatures and
 brace matching, from the reference checkout into oracle/_ref/*.inc (build
-output, git-ignored) and compiles oracle/ref/harness.cpp around them with g++
+output, git-ignored; the polysolve Types.hpp and Solver.hpp headers are staged
+there too, for the adapter's compile check) and compiles oracle/ref/harness.cpp
+around them with g++
 against CCCL's thrust (sequential host backend) and the Eigen stand-in in
 oracle/stubs, into oracle/_ref/libgpuhybrid_ref.so.
 
@@ -78,8 +80,16 @@ def _extract(src: str, path: str, signature: str, struct: bool = False) -> str:
     return f'#line {line} "{path}"\n' + src[k:end] + "\n"
 
 
+HEADERS = [os.path.join("src", "polysolve", "Types.hpp"), os.path.join("src", "polysolve", "linear", "Solver.hpp")]
+
+
 def extract(reference: str) -> None:
     os.makedirs(OUT, exist_ok=True)
+    # the polysolve interface headers, for the adapter's compile check
+    for h in HEADERS:
+        dst = os.path.join(OUT, "include", os.path.relpath(h, "src"))
+        os.makedirs(os.path.dirname(dst), exist_ok=True)
+        shutil.copyfile(os.path.join(reference, h), dst)
     gh = open(os.path.join(reference, GPUHYBRID)).read()
     hy = open(os.path.join(reference, HYBRID_HPP)).read()
     head = f"// generated by oracle/build_ref.py from the reference checkout at {reference}; do not edit\n"

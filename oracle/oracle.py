@@ -514,6 +514,24 @@ class CpuSolver:
 _ref_lib = None
 
 
+def greedy_partition(G, max_part=32):
+    """The oracle's greedy breadth-first partition (lsso_greedy_partition) of
+    a block graph G (scipy CSR, no self loops): (perm[old] = new, offsets)."""
+    G = G.tocsr()
+    nb = G.shape[0]
+    rows = np.ascontiguousarray(G.indptr, np.int32)
+    cols = np.ascontiguousarray(G.indices, np.int32)
+    part_of = np.zeros(max(nb, 1), np.int32)
+    nparts = lib().lsso_greedy_partition(nb, _p(rows, _i32p), _p(cols, _i32p), max_part, _p(part_of, _i32p))
+    part_of = part_of[:nb]
+    counts = np.bincount(part_of, minlength=nparts)
+    offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    order = np.argsort(part_of, kind="stable")
+    perm = np.empty(nb, np.int32)
+    perm[order] = np.arange(nb, dtype=np.int32)
+    return perm, offs
+
+
 def ref_lib():
     """oracle/_ref/libgpuhybrid_ref.so, built on first use; None when neither
     the reference checkout nor its extracted sources are present."""
