@@ -38,7 +38,7 @@ EXPORTS = [
     "lss_grad_A_pattern_device", "lss_grad_params_device", "lss_selected_dofs", "lss_gmm_selection", "lss_subdomains",
     "lss_partition", "lss_op_row_l1_norms", "lss_op_spmv", "lss_op_spmv_outer", "lss_op_mas_apply", "lss_op_precond",
     "lss_op_time", "lss_set_memory_cap", "lss_gmm_select_device_noalloc", "lss_solve_batched_device",
-    "lss_factorize_batched_device", "lss_op_row_scores", "lss_op_select_bad_dofs",
+    "lss_factorize_batched_device", "lss_op_row_scores", "lss_op_select_bad_dofs", "lss_partition_pattern",
 ]
 
 
