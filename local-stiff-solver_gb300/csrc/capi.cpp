@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
@@ -33,6 +34,18 @@ std::atomic<size_t> &alloc_live_bytes()
 {
     static std::atomic<size_t> live{0};
     return live;
+}
+void raise_smem_limit(const void *kernel, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> set;
+    int dev = 0;
+    LSS_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = set[{dev, kernel}];
+    if (bytes <= cur) return;
+    LSS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
 }
 int sm_grid(int per_sm)
 {

@@ -16,6 +16,12 @@ constexpr int GRID_MAX = 4096;     // CTAs of any reducing kernel at most (size 
 // count is queried once per device), capped at GRID_MAX.
 int sm_grid(int per_sm);
 
+// Raises a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes` (never lowers it): solvers driven from several host threads
+// set different sizes for the same kernel, and a lower value set by one
+// would make another's launch invalid.
+void raise_smem_limit(const void *kernel, size_t bytes);
+
 // Scratch of the deterministic grid reductions (device memory, counter zeroed once).
 struct GridReduce {
     double *partials = nullptr;  // GRID_MAX * RED_MAX_VALUES
@@ -171,14 +177,18 @@ int64_t mas_tile_elems(int bd);
 // Galerkin assembly into per-bank dense N x N FP64 staging (N = 32 bd)
 void launch_mas_assemble0(const BsrDev &A, const int32_t *part_of, const int32_t *part_off, double *stage,
                           cudaStream_t s);
-// members of the coarse items (CoarseSpace::memb_*), device copies
+// members of the coarse items in chunks (CoarseSpace::memb_rows,
+// item_chunk, chunk_r0), device copies; items are numbered flat over levels
+// 1..L-1
 struct CoarseMembers {
-    const int32_t *ptr = nullptr;
     const int32_t *rows = nullptr;
-    int64_t base[MAS_MAXL] = {};
+    const int32_t *item_chunk = nullptr;  // nitem + 1
+    const int32_t *chunk_r0 = nullptr;    // nchunk + 1
+    int64_t nitem = 0, nchunk = 0;
 };
+// partial: nchunk * bd * bd * 32 doubles of scratch
 void launch_mas_assemble_coarse(const BsrDev &A, const MasDev &m, const int32_t *cmap /* nb*(L-1) */,
-                                const CoarseMembers &mb, double *stage, cudaStream_t s);
+                                const CoarseMembers &mb, double *partial, double *stage, cudaStream_t s);
 // pad zero diagonals, invert (symmetric sweep), write bank tiles (FP32 or FP64)
 void launch_mas_invert(int bd, int64_t nbanks, const double *stage, void *out, bool fp32, int *bad,
                        cudaStream_t s, bool bf16_offdiag = false);

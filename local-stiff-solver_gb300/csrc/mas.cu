@@ -154,33 +154,46 @@ __global__ void __launch_bounds__(256) assemble0_kernel(BsrDev A, const int32_t 
     }
 }
 
-// Galerkin blocks of every coarse level, deterministically: one warp per
-// coarse item ci (its row strip of the bank matrix), lane c accumulating the
-// BD x BD block of the column items cj with cj % 32 == c.  The item's fine
-// rows come in ascending order and each row's blocks in column order; the
-// blocks of a 32-wide chunk whose column item falls into the same bank are
-// handed to their owner lanes one at a time by shuffles, so every sum runs in
-// one fixed order (no atomics): two factorizations of the same matrix give
-// bit-identical coarse inverses.  Only the upper triangle is written; each
-// entry belongs to exactly one item, so the stores never collide.
-template <int BD>
-__global__ void __launch_bounds__(256) assemble_coarse_kernel(BsrDev A, MasDev m, const int32_t *__restrict__ cmap,
-                                                              CoarseMembers mb, double *__restrict__ stage)
+// Galerkin blocks of every coarse level, deterministically, in two passes.
+// Pass 1: one warp per chunk of at most MEMB_CHUNK member rows of a coarse
+// item ci (its row strip of the bank matrix), lane c accumulating the BD x BD
+// block of the column items cj with cj % 32 == c.  The chunk's rows come in
+// ascending order and each row's blocks in column order; the blocks of a
+// 32-wide piece whose column item falls into the same bank are handed to
+// their owner lanes one at a time by shuffles.  Pass 2: one warp per item sums
+// its chunks' partial strips in chunk order and writes the upper triangle
+// (each entry belongs to exactly one item, so the stores never collide).
+// Every sum runs in one fixed order (no atomics): two factorizations of the
+// same matrix give bit-identical coarse inverses.
+__device__ __forceinline__ void flat_item(const MasDev &m, int64_t w, int &l, int32_t &ci)
 {
-    constexpr int N = 32 * BD;
-    const int lane = threadIdx.x & 31;
-    int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int l = 1;
+    l = 1;
     while (l < m.L && w >= m.nitems[l]) w -= m.nitems[l++];
-    if (l >= m.L) return;
-    const int32_t ci = (int32_t)w;
+    ci = (int32_t)w;
+}
+
+template <int BD>
+__global__ void __launch_bounds__(256) assemble_coarse_chunk_kernel(BsrDev A, MasDev m, const int32_t *__restrict__ cmap,
+                                                                    CoarseMembers mb, double *__restrict__ partial)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= mb.nchunk) return;
+    // the chunk's item: last i with item_chunk[i] <= c
+    int32_t lo = 0, hi = mb.nitem - 1;
+    while (lo < hi) {
+        const int32_t mid = (lo + hi + 1) >> 1;
+        if (mb.item_chunk[mid] <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    int l;
+    int32_t ci;
+    flat_item(m, lo, l, ci);
     const int32_t *map = cmap + (int64_t)(l - 1) * A.nb;
-    const int32_t g = m.boff[l] + (ci >> 5);
     double acc[BD * BD];
 #pragma unroll
     for (int k = 0; k < BD * BD; ++k) acc[k] = 0.0;
-    const int32_t r0 = mb.ptr[mb.base[l] + ci], r1 = mb.ptr[mb.base[l] + ci + 1];
-    for (int32_t r = r0; r < r1; ++r) {
+    for (int32_t r = mb.chunk_r0[c]; r < mb.chunk_r0[c + 1]; ++r) {
         const int32_t i = mb.rows[r];
         const int32_t b = A.rows[i], len = A.rows[i + 1] - b;
         const double *v = A.vals + (int64_t)b * BD * BD;
@@ -200,14 +213,40 @@ __global__ void __launch_bounds__(256) assemble_coarse_kernel(BsrDev A, MasDev m
             while (pending) {
                 const int src = __ffs(pending) - 1;
                 pending &= pending - 1;
-                const int32_t c = __shfl_sync(0xffffffffu, cj, src);
+                const int32_t cc = __shfl_sync(0xffffffffu, cj, src);
 #pragma unroll
                 for (int k = 0; k < BD * BD; ++k) {
                     const double x = __shfl_sync(0xffffffffu, val[k], src);
-                    if ((c & 31) == lane) acc[k] += x;
+                    if ((cc & 31) == lane) acc[k] += x;
                 }
             }
         }
+    }
+    double *out = partial + c * (BD * BD * 32);
+#pragma unroll
+    for (int k = 0; k < BD * BD; ++k) out[k * 32 + lane] = acc[k];
+}
+
+template <int BD>
+__global__ void __launch_bounds__(256) assemble_coarse_sum_kernel(MasDev m, CoarseMembers mb,
+                                                                  const double *__restrict__ partial,
+                                                                  double *__restrict__ stage)
+{
+    constexpr int N = 32 * BD;
+    const int lane = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= mb.nitem) return;
+    int l;
+    int32_t ci;
+    flat_item(m, w, l, ci);
+    const int32_t g = m.boff[l] + (ci >> 5);
+    double acc[BD * BD];
+#pragma unroll
+    for (int k = 0; k < BD * BD; ++k) acc[k] = 0.0;
+    for (int32_t c = mb.item_chunk[w]; c < mb.item_chunk[w + 1]; ++c) {
+        const double *p = partial + (int64_t)c * (BD * BD * 32);
+#pragma unroll
+        for (int k = 0; k < BD * BD; ++k) acc[k] += p[k * 32 + lane];
     }
     double *base = stage + (int64_t)g * N * N;
 #pragma unroll
@@ -567,16 +606,23 @@ void launch_mas_assemble0(const BsrDev &A, const int32_t *part_of, const int32_t
 }
 
 void launch_mas_assemble_coarse(const BsrDev &A, const MasDev &m, const int32_t *cmap, const CoarseMembers &mb,
-                                double *stage, cudaStream_t s)
+                                double *partial, double *stage, cudaStream_t s)
 {
-    int64_t items = 0;
-    for (int l = 1; l < m.L; ++l) items += m.nitems[l];
-    if (items == 0 || m.L < 2) return;
-    const int grid = (int)((items * 32 + 255) / 256);
+    if (mb.nitem == 0 || m.L < 2) return;
+    const int g1 = (int)((mb.nchunk * 32 + 255) / 256), g2 = (int)((mb.nitem * 32 + 255) / 256);
     switch (A.bd) {
-    case 1: assemble_coarse_kernel<1><<<grid, 256, 0, s>>>(A, m, cmap, mb, stage); break;
-    case 2: assemble_coarse_kernel<2><<<grid, 256, 0, s>>>(A, m, cmap, mb, stage); break;
-    default: assemble_coarse_kernel<3><<<grid, 256, 0, s>>>(A, m, cmap, mb, stage); break;
+    case 1:
+        assemble_coarse_chunk_kernel<1><<<g1, 256, 0, s>>>(A, m, cmap, mb, partial);
+        assemble_coarse_sum_kernel<1><<<g2, 256, 0, s>>>(m, mb, partial, stage);
+        break;
+    case 2:
+        assemble_coarse_chunk_kernel<2><<<g1, 256, 0, s>>>(A, m, cmap, mb, partial);
+        assemble_coarse_sum_kernel<2><<<g2, 256, 0, s>>>(m, mb, partial, stage);
+        break;
+    default:
+        assemble_coarse_chunk_kernel<3><<<g1, 256, 0, s>>>(A, m, cmap, mb, partial);
+        assemble_coarse_sum_kernel<3><<<g2, 256, 0, s>>>(m, mb, partial, stage);
+        break;
     }
     LSS_LAUNCH_CHECK();
 }

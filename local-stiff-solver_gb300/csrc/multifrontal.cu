@@ -534,8 +534,8 @@ void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
     // shared memory of the solve kernels, set here: solve() runs inside graph captures
     const size_t fsmem = (size_t)(M.max_s + PW + 8 * 32) * sizeof(double);
     const size_t bsmem = (size_t)(M.max_f + 8 * 32) * sizeof(double);
-    LSS_CUDA(cudaFuncSetAttribute(mf_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
-    LSS_CUDA(cudaFuncSetAttribute(mf_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem));
+    raise_smem_limit((const void *)mf_forward_kernel, fsmem);
+    raise_smem_limit((const void *)mf_backward_kernel, bsmem);
     d_F_.resize(M.elems);
     d_w_.resize(std::max<int64_t>(M.welems, 1));
     d_x_.resize(std::max<int32_t>(M.npos, 1));
@@ -572,7 +572,7 @@ void MfFactor::factorize(const BsrDev &A, const StiffDev &S, int *bad, cudaStrea
     }
     LSS_LAUNCH_CHECK();
     const size_t small_smem = (size_t)(MF_SMEM_F * (MF_SMEM_F + 1) + 2 * MF_SMEM_F) * sizeof(double);
-    LSS_CUDA(cudaFuncSetAttribute(mf_sweep_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
+    raise_smem_limit((const void *)mf_sweep_small_kernel, small_smem);
     for (const Level &L : levels_) {
         if (L.ea.count) {
             mf_extend_add_kernel<<<L.ea.count, 256, 0, st>>>(v, L.ea, F);

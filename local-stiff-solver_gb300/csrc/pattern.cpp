@@ -308,6 +308,15 @@ CoarseSpace build_coarse_space(const Pattern &P, int max_coarse_levels)
         std::vector<int32_t> fill(ptr, ptr + items);
         for (int32_t i = 0; i < nb; ++i) cs.memb_rows[fill[map[i]]++] = i;
     }
+    cs.item_chunk.assign(1, 0);
+    for (int l = 1; l < L; ++l) {
+        const int32_t *ptr = cs.memb_ptr.data() + cs.memb_base[l];
+        for (int32_t t = 0; t < cs.nitems[l]; ++t) {
+            for (int32_t r = ptr[t]; r < ptr[t + 1]; r += MEMB_CHUNK) cs.chunk_r0.push_back(r);
+            cs.item_chunk.push_back((int32_t)cs.chunk_r0.size());
+        }
+    }
+    cs.chunk_r0.push_back((int32_t)cs.memb_rows.size());  // end of the last chunk
     return cs;
 }
 

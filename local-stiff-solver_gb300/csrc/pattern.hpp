@@ -46,7 +46,13 @@ struct CoarseSpace {
     // deterministic Galerkin assembly
     std::vector<int32_t> memb_ptr, memb_rows;
     std::vector<int64_t> memb_base;               // L entries (level 0 unused)
+    // the members split into chunks of at most MEMB_CHUNK rows (one warp
+    // each); item i (flat over levels 1..L-1) owns chunks
+    // [item_chunk[i], item_chunk[i+1]); chunk c covers memb_rows[chunk_r0[c] ..
+    // chunk_r0[c+1]) -- consecutive chunks of an item are contiguous
+    std::vector<int32_t> item_chunk, chunk_r0;
 };
+constexpr int32_t MEMB_CHUNK = 128;
 
 CoarseSpace build_coarse_space(const Pattern &P, int max_coarse_levels);
 

@@ -198,12 +198,15 @@ void HybridSolver::analyze(int32_t n, int64_t nnz, const int32_t *outer, const i
     d_ccnt0_.upload(cs_.ccnt0, stream_);
     d_cbase0_.upload(cs_.cbase0, stream_);
     d_cmap_.upload(cs_.cmap, stream_);
-    d_memb_ptr_.upload(cs_.memb_ptr, stream_);
+    d_memb_ptr_.upload(cs_.item_chunk, stream_);
     d_memb_rows_.upload(cs_.memb_rows, stream_);
+    d_chunk_r0_.upload(cs_.chunk_r0, stream_);
     memb_ = CoarseMembers();
-    memb_.ptr = d_memb_ptr_.data();
     memb_.rows = d_memb_rows_.data();
-    for (int l = 0; l < cs_.L && l < MAS_MAXL; ++l) memb_.base[l] = cs_.memb_base[l];
+    memb_.item_chunk = d_memb_ptr_.data();
+    memb_.chunk_r0 = d_chunk_r0_.data();
+    memb_.nitem = (int64_t)cs_.item_chunk.size() - 1;
+    memb_.nchunk = (int64_t)cs_.chunk_r0.size() - 1;
     d_key_.clear();
     d_ccnt_.clear();
     d_cbase_.clear();
@@ -636,7 +639,8 @@ void HybridSolver::setup_mas()
     if (ncoarse > 0) {
         DBuf<double> stage((size_t)ncoarse * N * N);
         stage.zero(stream_);
-        launch_mas_assemble_coarse(A_, mas_, d_cmap_.data(), memb_, stage.data(), stream_);
+        DBuf<double> partial((size_t)std::max<int64_t>(memb_.nchunk, 1) * bd * bd * 32);
+        launch_mas_assemble_coarse(A_, mas_, d_cmap_.data(), memb_, partial.data(), stage.data(), stream_);
         launch_mas_invert(bd, ncoarse, stage.data(), d_invc_.data(), mas_fp32_, d_bad_.data(), stream_);
         LSS_CUDA(cudaStreamSynchronize(stream_));
     }

@@ -114,7 +114,7 @@ private:
     DBuf<int64_t> d_src_;
     // MAS
     MasDev mas_;
-    DBuf<int32_t> d_part_off_, d_cbase0_, d_part_of_, d_cmap_, d_memb_ptr_, d_memb_rows_;
+    DBuf<int32_t> d_part_off_, d_cbase0_, d_part_of_, d_cmap_, d_memb_ptr_, d_memb_rows_, d_chunk_r0_;
     CoarseMembers memb_;
     DBuf<uint8_t> d_key0_, d_ccnt0_;
     std::vector<DBuf<uint8_t>> d_key_, d_ccnt_;

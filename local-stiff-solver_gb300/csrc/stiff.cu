@@ -190,7 +190,7 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
     }
     // (160 * 161 + 320) doubles = 204 KB of shared memory at most
     const size_t smem = (size_t)(maxm * (maxm + 1) + 2 * maxm) * sizeof(double);
-    LSS_CUDA(cudaFuncSetAttribute(invert_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    raise_smem_limit((const void *)invert_small_kernel, smem);
     DBuf<int32_t> d_ids;
     d_ids.upload(ids, s);
     invert_small_kernel<<<(unsigned)nsub, 256, smem, s>>>(d_ids.data(), S.off, S.inv_off, inv, bad);

@@ -613,6 +613,212 @@ void lsso_mas_destroy(lsso_mas *m)
 }
 
 /* ===================================================================== */
+/* The library's partition, restated: recursive breadth-first bisection   */
+/* into k = ceil(m / 30) connected, bank-aligned parts of <= 32 block rows */
+/* (the product's csrc/partition.cpp; it stands in for KaMinPar,          */
+/* GraphPartition.cpp:176-289).  Restated here so that the CPU method runs */
+/* with the GPU's partition without loading the product library; the CPU  */
+/* tests require the two to agree exactly.                                */
+/* ===================================================================== */
+typedef struct {
+    const int32_t *rows, *cols;
+    int32_t *owner, *seen;
+    int32_t next_task, next_stamp;
+    int32_t **parts;
+    int32_t *part_len;
+} bp_ctx;
+
+typedef struct { int32_t *v; int32_t n, cap; } ivec;
+
+static void iv_push(ivec *a, int32_t x)
+{
+    if (a->n == a->cap) {
+        a->cap = a->cap ? 2 * a->cap : 16;
+        a->v = (int32_t *)realloc(a->v, sizeof(int32_t) * (size_t)a->cap);
+    }
+    a->v[a->n++] = x;
+}
+
+/* breadth-first order of `nodes` (owned by task) from `start`, restarting at
+ * the next unvisited node of `nodes` for disconnected pieces */
+static void bp_bfs(bp_ctx *c, int32_t task, const int32_t *nodes, int32_t m, int32_t start, int32_t *order)
+{
+    const int32_t stamp = c->next_stamp++;
+    int32_t len = 0, head = 0, scan = 0, s = start;
+    for (;;) {
+        if (c->seen[s] != stamp) {
+            c->seen[s] = stamp;
+            order[len++] = s;
+            while (head < len) {
+                const int32_t u = order[head++];
+                for (int32_t k = c->rows[u]; k < c->rows[u + 1]; ++k) {
+                    const int32_t v = c->cols[k];
+                    if (c->owner[v] == task && c->seen[v] != stamp) {
+                        c->seen[v] = stamp;
+                        order[len++] = v;
+                    }
+                }
+            }
+        }
+        while (scan < m && c->seen[nodes[scan]] == stamp) ++scan;
+        if (scan == m) break;
+        s = nodes[scan];
+    }
+}
+
+/* connected components of `nodes` (owned by task), in order of first node:
+ * flat[] holds them one after the other, off[] their offsets; returns the count */
+static int32_t bp_components(bp_ctx *c, int32_t task, const int32_t *nodes, int32_t m, int32_t *flat, int32_t *off)
+{
+    const int32_t stamp = c->next_stamp++;
+    int32_t nc = 0, len = 0;
+    off[0] = 0;
+    for (int32_t i = 0; i < m; ++i) {
+        const int32_t s = nodes[i];
+        if (c->seen[s] == stamp) continue;
+        int32_t h = len;
+        flat[len++] = s;
+        c->seen[s] = stamp;
+        for (; h < len; ++h) {
+            const int32_t u = flat[h];
+            for (int32_t k = c->rows[u]; k < c->rows[u + 1]; ++k) {
+                const int32_t v = c->cols[k];
+                if (c->owner[v] == task && c->seen[v] != stamp) {
+                    c->seen[v] = stamp;
+                    flat[len++] = v;
+                }
+            }
+        }
+        off[++nc] = len;
+    }
+    return nc;
+}
+
+/* parts in the left child of a subtree with k leaves: a multiple of the
+ * largest power of 32 below k */
+static int32_t bp_left_parts(int32_t k)
+{
+    int64_t B = 1;
+    while (B * 32 < k) B *= 32;
+    const int64_t g = (k + B - 1) / B;
+    int64_t k1 = (g / 2) * B;
+    if (k1 <= 0 || k1 >= k) k1 = k / 2;
+    return (int32_t)k1;
+}
+
+static void bp_split(bp_ctx *c, int32_t task, int32_t *nodes, int32_t m, int32_t part0, int32_t k)
+{
+    if (k <= 1 || m <= 1) {
+        int32_t *o = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)m);
+        if (m > 1) {
+            bp_bfs(c, task, nodes, m, nodes[0], o);
+            const int32_t last = o[m - 1];
+            bp_bfs(c, task, nodes, m, last, o);
+        } else {
+            memcpy(o, nodes, sizeof(int32_t) * (size_t)m);
+        }
+        c->parts[part0] = o;
+        c->part_len[part0] = m;
+        free(nodes);
+        return;
+    }
+    const int32_t k1 = bp_left_parts(k), k2 = k - k1;
+    int64_t m1 = ((int64_t)m * k1 + k / 2) / k;
+    if (m1 < (int64_t)m - 32 * (int64_t)k2) m1 = (int64_t)m - 32 * (int64_t)k2;
+    if (m1 > 32 * (int64_t)k1) m1 = 32 * (int64_t)k1;
+    if (m1 > m - 1) m1 = m - 1;
+    if (m1 < 1) m1 = 1;
+    int32_t *order = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)m);
+    bp_bfs(c, task, nodes, m, nodes[0], order);
+    const int32_t last = order[m - 1];
+    bp_bfs(c, task, nodes, m, last, order);
+    free(nodes);
+    const int32_t tl = c->next_task++, tr = c->next_task++;
+    ivec left = {0, 0, 0}, right = {0, 0, 0};
+    for (int32_t i = 0; i < m; ++i) iv_push(i < m1 ? &left : &right, order[i]);
+    free(order);
+    for (int32_t i = 0; i < left.n; ++i) c->owner[left.v[i]] = tl;
+    for (int32_t i = 0; i < right.n; ++i) c->owner[right.v[i]] = tr;
+    /* reconnect the right side: swap its small pieces with the prefix's tail */
+    for (int round = 0; round < 4; ++round) {
+        int32_t *flat = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)(right.n + 1));
+        int32_t *off = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)(right.n + 2));
+        const int32_t nc = bp_components(c, tr, right.v, right.n, flat, off);
+        if (nc <= 1) { free(flat); free(off); break; }
+        int32_t big = 0;
+        for (int32_t q = 1; q < nc; ++q)
+            if (off[q + 1] - off[q] > off[big + 1] - off[big]) big = q;
+        const int32_t npieces = right.n - (off[big + 1] - off[big]);
+        if (npieces >= left.n) { free(flat); free(off); break; }
+        /* the last nodes of the prefix go right, the pieces go left */
+        int32_t *moved = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)npieces);
+        memcpy(moved, left.v + left.n - npieces, sizeof(int32_t) * (size_t)npieces);
+        left.n -= npieces;
+        for (int32_t q = 0; q < nc; ++q) {
+            if (q == big) continue;
+            for (int32_t t = off[q]; t < off[q + 1]; ++t) {
+                c->owner[flat[t]] = tl;
+                iv_push(&left, flat[t]);
+            }
+        }
+        for (int32_t t = 0; t < npieces; ++t) c->owner[moved[t]] = tr;
+        right.n = 0;
+        for (int32_t t = off[big]; t < off[big + 1]; ++t) iv_push(&right, flat[t]);
+        for (int32_t t = 0; t < npieces; ++t) iv_push(&right, moved[t]);
+        free(moved); free(flat); free(off);
+    }
+    bp_split(c, tl, left.v, left.n, part0, k1);
+    bp_split(c, tr, right.v, right.n, part0 + k1, k2);
+}
+
+int32_t lsso_bisect_partition(int32_t nb, const int32_t *rows, const int32_t *cols, int32_t *perm,
+                              int32_t *part_offsets)
+{
+    part_offsets[0] = 0;
+    if (nb <= 0) return 0;
+    bp_ctx c;
+    c.rows = rows;
+    c.cols = cols;
+    c.owner = (int32_t *)xcalloc((size_t)nb, sizeof(int32_t));
+    c.seen = (int32_t *)xcalloc((size_t)nb, sizeof(int32_t));
+    c.next_task = 1;
+    c.next_stamp = 1;
+    int32_t *coupled = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)nb);
+    int32_t *isolated = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)nb);
+    int32_t m = 0, ni = 0;
+    for (int32_t i = 0; i < nb; ++i) {
+        int any = 0;
+        for (int32_t q = rows[i]; q < rows[i + 1] && !any; ++q) any = cols[q] != i;
+        if (any) coupled[m++] = i;
+        else isolated[ni++] = i;
+    }
+    for (int32_t t = 0; t < ni; ++t) c.owner[isolated[t]] = -1;
+    const int32_t k = m == 0 ? 0 : (m <= 32 ? 1 : (m + 29) / 30);
+    c.parts = (int32_t **)xcalloc((size_t)(k > 0 ? k : 1), sizeof(int32_t *));
+    c.part_len = (int32_t *)xcalloc((size_t)(k > 0 ? k : 1), sizeof(int32_t));
+    if (k > 0) bp_split(&c, 0, coupled, m, 0, k);
+    else free(coupled);
+    int32_t next = 0, np = 0;
+    for (int32_t p = 0; p < k; ++p) {
+        const int32_t len = c.part_len[p];
+        /* a leaf larger than a bank (possible only after the reconnect swaps) is cut in BFS order */
+        for (int32_t s0 = 0; s0 < len; s0 += 32) {
+            const int32_t e = s0 + 32 < len ? s0 + 32 : len;
+            for (int32_t q = s0; q < e; ++q) perm[c.parts[p][q]] = next++;
+            part_offsets[++np] = next;
+        }
+        free(c.parts[p]);
+    }
+    for (int32_t s0 = 0; s0 < ni; s0 += 32) {
+        const int32_t e = s0 + 32 < ni ? s0 + 32 : ni;
+        for (int32_t q = s0; q < e; ++q) perm[isolated[q]] = next++;
+        part_offsets[++np] = next;
+    }
+    free(isolated); free(c.parts); free(c.part_len); free(c.owner); free(c.seen);
+    return np;
+}
+
+/* ===================================================================== */
 /* Oracle partition: greedy BFS region growing into parts of <= max_part   */
 /* (a simple, independent stand-in for KaMinPar, GraphPartition.cpp:176)  */
 /* ===================================================================== */
@@ -684,6 +890,7 @@ void lsso_default_params(lsso_params *p)
     p->mas_omega = 0.0;
     p->omega_iters = 20;
     p->omega_factor = 1.5;
+    p->greedy_partition = 0;
 }
 
 void lsso_probe_vector(int32_t n, double *v)
@@ -914,6 +1121,9 @@ lsso_solver *lsso_solver_create(int32_t n, const int32_t *outer, const int32_t *
         nparts = nparts_in;
         poff = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)(nparts + 1));
         memcpy(poff, part_offsets_in, sizeof(int32_t) * (size_t)(nparts + 1));
+    } else if (!p->greedy_partition) {
+        poff = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)(nb + 2));
+        nparts = lsso_bisect_partition(nb, brow, bcol, s->perm, poff);
     } else {
         int32_t *part_of = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)nb);
         nparts = lsso_greedy_partition(nb, brow, bcol, BANK, part_of);

@@ -107,6 +107,7 @@ typedef struct {
     double mas_omega;            /* damping of MAS in the multiplicative form; <= 0: auto */
     int32_t omega_iters;         /* PCG-Lanczos steps of the automatic estimate */
     double omega_factor;         /* omega = omega_factor / lambda_max(M A) */
+    int32_t greedy_partition;    /* 1: the oracle's greedy partition; 0: the library's bisection */
 } lsso_params;
 
 void lsso_default_params(lsso_params *p);
@@ -139,6 +140,12 @@ int32_t lsso_solver_num_subdomains(const lsso_solver *s);
 /* Apply the hybrid preconditioner once (z = M^-1 r, original ordering). */
 void lsso_solver_precond(lsso_solver *s, const double *r, double *z);
 void lsso_solver_destroy(lsso_solver *s);
+
+/* the library's partition restated (recursive breadth-first bisection,
+ * k = ceil(m / 30) parts of <= 32 block rows, uncoupled rows last):
+ * perm[old] = new, part_offsets[nparts + 1] (capacity nb + 1); returns nparts */
+int32_t lsso_bisect_partition(int32_t nb, const int32_t *rows, const int32_t *cols, int32_t *perm,
+                              int32_t *part_offsets);
 
 /* the oracle's own partition: part id per block row of a CSR block graph */
 int32_t lsso_greedy_partition(int32_t nb, const int32_t *rows, const int32_t *cols,

@@ -58,7 +58,7 @@ class Params(C.Structure):
         ("decompose", C.c_int32), ("min_sub", C.c_int32), ("max_sub", C.c_int32),
         ("expand", C.c_int32), ("max_coarse_levels", C.c_int32), ("threads", C.c_int32),
         ("additive", C.c_int32), ("mas_omega", C.c_double), ("omega_iters", C.c_int32),
-        ("omega_factor", C.c_double),
+        ("omega_factor", C.c_double), ("greedy_partition", C.c_int32),
     ]
 
 
@@ -125,6 +125,8 @@ def lib():
         L.lsso_probe_vector.argtypes = [C.c_int32, _f64p]
         L.lsso_solver_destroy.argtypes = [C.c_void_p]
         L.lsso_greedy_partition.argtypes = [C.c_int32, _i32p, _i32p, C.c_int32, _i32p]
+        L.lsso_bisect_partition.argtypes = [C.c_int32, _i32p, _i32p, _i32p, _i32p]
+        L.lsso_bisect_partition.restype = C.c_int32
         L.lsso_greedy_partition.restype = C.c_int32
         L.lsso_mas_select_elbow.argtypes = [C.c_int32, _f64p, _i32p]
         L.lsso_mas_select_elbow.restype = C.c_int32
@@ -421,7 +423,7 @@ class Mas:
 
 
 def make_params(params: dict, threads=0, max_coarse_levels=4, additive=False, mas_omega=0.0,
-                omega_iters=20, omega_factor=1.5) -> Params:
+                omega_iters=20, omega_factor=1.5, greedy_partition=False) -> Params:
     p = dict(DEFAULTS)
     p.update(params)
     P = Params()
@@ -446,6 +448,7 @@ def make_params(params: dict, threads=0, max_coarse_levels=4, additive=False, ma
     P.mas_omega = float(mas_omega)
     P.omega_iters = int(omega_iters)
     P.omega_factor = float(omega_factor)
+    P.greedy_partition = int(bool(greedy_partition))
     return P
 
 
@@ -530,6 +533,19 @@ def greedy_partition(G, max_part=32):
     perm = np.empty(nb, np.int32)
     perm[order] = np.arange(nb, dtype=np.int32)
     return perm, offs
+
+
+def bisect_partition(G):
+    """The library's partition restated in C (lsso_bisect_partition) on a
+    block graph G (scipy CSR): (perm[old] = new, part_offsets)."""
+    G = G.tocsr()
+    nb = G.shape[0]
+    rows = np.ascontiguousarray(G.indptr, np.int32)
+    cols = np.ascontiguousarray(G.indices, np.int32)
+    perm = np.zeros(max(nb, 1), np.int32)
+    offs = np.zeros(nb + 2, np.int32)
+    np_ = lib().lsso_bisect_partition(nb, _p(rows, _i32p), _p(cols, _i32p), _p(perm, _i32p), _p(offs, _i32p))
+    return perm[:nb].copy(), offs[:np_ + 1].copy()
 
 
 def ref_lib():

@@ -287,8 +287,11 @@ def test_large_stiff_subdomain(precision, built):
     """A 0.3-radius x1e6 inclusion on a 16^3-node cube makes one stiff
     subdomain of 3,168 DOFs: the FP64 multifrontal factor (nested dissection,
     blocks above 160 DOFs).  The preconditioner matches the oracle's (exact
-    Cholesky of the same block, same partition and damping) to 1e-10 in FP64,
-    and the solve reaches the parity bar."""
+    Cholesky of the same block, same partition and damping) to 1e-7 in FP64:
+    the block's condition number is 6.6e7 (cond * eps = 1.5e-8; two FP64
+    direct solvers, Cholesky and SuperLU, already differ by 2.5e-10 on it),
+    and the composition multiplies the stiff solve's error by A before the
+    second MAS pass.  The solve reaches the parity bar."""
     from lss import gen
     A, b, _ = gen.workload_elasticity_inclusion(seed=2, nodes=16, radius=0.3)
     A = A.tocsc()
@@ -302,7 +305,7 @@ def test_large_stiff_subdomain(precision, built):
         o = _oracle_with_product_partition(A, s, params, mas_omega=info["mas_omega"])
         r = np.random.default_rng(5).standard_normal(A.shape[0])
         z, zo = s.precond(r), o.precond(r)
-        assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < 1e-10
+        assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < 1e-7
     x = s.solve(b)
     _check_solution(A, b, x)
     assert s.get_info()["status"] == "converged_rel"
@@ -312,8 +315,10 @@ def test_multifrontal_matches_sparse_lu(built):
     """The stiff-block solve alone, on a 14k-DOF subdomain (0.35-radius x1e6
     inclusion in a 30^3-node cube): with the additive composition,
     precond(r) - mas(r) is exactly A_SS^-1 r_S on the stiff DOFs and zero
-    elsewhere.  Compared with scipy's sparse LU of every stiff block to 1e-10
-    (FP64 throughout), twice (the factor and the solve are deterministic)."""
+    elsewhere.  Compared with scipy's sparse LU of every stiff block to 1e-9
+    (FP64 throughout; the blocks' condition numbers near 1e8 put two FP64
+    direct solvers about 1e-10 apart), twice (the factor and the solve are
+    deterministic)."""
     import scipy.sparse.linalg as spla
     from lss import gen
     A, _, _ = gen.workload_elasticity_inclusion(seed=3, nodes=30, radius=0.35)
@@ -331,7 +336,7 @@ def test_multifrontal_matches_sparse_lu(built):
         sub = np.asarray(sub)
         covered[sub] = True
         x = spla.splu(Ar[sub][:, sub].tocsc()).solve(r[sub])
-        assert np.linalg.norm(d[sub] - x) <= 1e-10 * np.linalg.norm(x), len(sub)
+        assert np.linalg.norm(d[sub] - x) <= 1e-9 * np.linalg.norm(x), len(sub)
     assert np.all(d[~covered] == 0.0)
     np.testing.assert_array_equal(s.precond(r) - s.mas_apply(r), d)
 

@@ -111,3 +111,16 @@ def test_partition_quality(case, built):
     assert q["edge_cut"] <= 1.3 * qg["edge_cut"]
     assert q["parts_connected"] >= 0.75
     assert q["banks_connected"] >= 0.75 and q["banks_connected"] >= qg["banks_connected"] + 0.5
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_oracle_restatement_gives_the_same_partition(case, built):
+    """The oracle's C restatement of the partitioner (used by the CPU method
+    of the reference arm and the CPU baseline) reproduces it exactly."""
+    from oracle import oracle as O
+    make, bd = CASES[case]
+    A = make().tocsc()
+    perm, offs = lss.partition_pattern(A, bd)
+    operm, ooffs = O.bisect_partition(_block_graph(A, bd))
+    np.testing.assert_array_equal(operm, perm)
+    np.testing.assert_array_equal(ooffs, offs)
