@@ -2,29 +2,36 @@
 """Benchmark: time to 1e-8 relative residual, mixed precision vs plain FP64,
 on one GB300 (one process per GPU; N > 1 runs independent replicas).
 
-Workload (default ``elasticity_3m``): P1-tet linear elasticity on a
+Headline workload (``elasticity_3m``): P1-tet linear elasticity on a
 100x100x100-node grid (3.0M DOFs, 3x3 blocks), Young's modulus lognormal(0, 1)
-per tet, penalty springs of stiffness 1e8 on a seeded 1% of the top-face nodes,
-z = 0 face clamped, RHS N(0, 1) -- the mixed-precision configuration.
-``--workload delaunay_1m`` runs the 2D Delaunay Laplacian (1,000,000 points,
-2% collapsed triangles) and ``elasticity_24k`` the 20^3-node inclusion cube.
-All inputs are synthetic (seeded numpy PCG64).
+per tet, penalty springs of stiffness 1e8 on a seeded 1% of the top-face
+nodes, z = 0 face clamped, RHS N(0, 1) -- the mixed-precision configuration.
+All inputs are synthetic (seeded numpy PCG64, bit-identical on x86 and
+aarch64).
 
-One step = factorize (stiff-DOF selection, stiff-block inverses, MAS setup)
+One step = factorize (stiff-DOF selection, stiff-block factor, MAS setup)
 with the matrix values resident in HBM and the pattern analysed beforehand,
 then the PCG solve to a true relative residual <= 1e-8 with b resident in HBM.
 ``value`` is the mixed-precision ms per step (CUDA events on the solver's
 stream), ``e2e`` the same step through the C ABI with host arrays (the H2D
 copy of the values, b and x0 and the D2H copy of x inside the timed region).
-The plain-FP64 form of the same method is timed the same way and reported
-in ``config``.  Inputs exceed the 129 MB L2 (no flush needed).
+The plain-FP64 form of the same method is timed the same way.  The line also
+carries the correctness checks of the timed configuration (stiff-DOF set
+against the oracle and the reference build, solution against a tight FP64
+solve and against SuperLU on a 24^3-node box of the same generator) and, under
+``configs``, the other configurations: the 1M-point Delaunay Laplacian
+(``delaunay_1m``), the 500k-DOF differentiation workload (``adjoint_500k``)
+and the batched systems (``batched``), each with its own checks.
+``--workload NAME`` runs one configuration alone.  Inputs exceed the 129 MB
+L2 (no flush needed).
 
-``--impl reference`` times the CPU restatement of the method (oracle/) on the
-host cores instead: a bounded sample (setup + a block of PCG iterations on the
-full system), scaled to time-to-solution with the iteration count estimated
-from the sampled residual decay.
+``--impl reference`` runs the CPU restatement of the method (oracle/) on all
+host cores, with the same partition as the GPU: one complete factorize +
+solve to 1e-8 is timed once (``value``), then every timed step is a sample of
+``--ref-iters`` PCG iterations (``ms_per_step``).
 """
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -49,6 +56,8 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 NCU_TRAFFIC_RATIO = {"spmv_outer": 246.24 / 252.39, "mas_level0_symv": 145.10 / 146.79,
                      "residual_spmv_prec": 133.98 / 132.83}
 
+DTYPE_MIXED = "f64 PCG recurrences and dots, df32 (FP32-pair) A.p, f32 MAS, f64 stiff factor"
+
 
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -65,8 +74,8 @@ def workload(name, seed):
     # = false (a lone stiff node is a 3-DOF, well-conditioned component that the
     # size and Gershgorin filters would drop) and the small cube uses the
     # reference's example configuration (spec/CPUHybrid.json).
-    if name in ("elasticity_3m", "elasticity_650k"):
-        nodes = 100 if name == "elasticity_3m" else 60
+    if name in ("elasticity_3m", "elasticity_650k", "elasticity_subbox"):
+        nodes = {"elasticity_3m": 100, "elasticity_650k": 60, "elasticity_subbox": 24}[name]
         A, b, info = gen.workload_elasticity_lognormal(seed=seed, nodes=nodes)
         params = {"block_size": 3, "relative_tolerance": 1e-8, "decompose_subdomains": False, "max_iter": 20000}
         desc = f"elasticity_lognormal_{nodes}^3_nodes_springs1e8"
@@ -81,7 +90,9 @@ def workload(name, seed):
         desc = "elasticity_inclusion_20^3_nodes_E1e6"
     else:
         raise SystemExit(f"unknown workload {name}")
-    return A.tocsc(), np.ascontiguousarray(b, np.float64), params, desc, info
+    A = A.tocsc()
+    A.sum_duplicates()
+    return A, np.ascontiguousarray(b, np.float64), params, desc, info
 
 
 class ClockSampler:
@@ -138,6 +149,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -145,8 +164,27 @@ def dist_env():
     return ws, rank, local
 
 
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
+def sha256_i32(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<i4").tobytes()).hexdigest()
+
+
+def as_rows(A):
+    """The operator the solver applies: outer index = row (GPUHybrid.cu:203-209)."""
+    import scipy.sparse as sp
+    return sp.csr_matrix((A.data, A.indices, A.indptr), shape=A.shape)
+
+
+# ---------------------------------------------------------------- reference arm
+
 def run_reference(args):
-    """CPU restatement of the method on the host cores (bounded sample)."""
+    """CPU restatement of the method (oracle/) on the host cores, same partition
+    as the GPU (the oracle restates the library's partitioner exactly).  One
+    complete factorize + solve to 1e-8 is measured (value); the timed steps are
+    samples of --ref-iters PCG iterations (ms_per_step)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
@@ -156,55 +194,44 @@ def run_reference(args):
     O.build()
     A, b, params, desc, info = workload(args.workload, args.seed)
     threads = os.cpu_count() or 1
-    setup_s, per_iter, res_hist = [], [], []
-    bnorm = float(np.linalg.norm(b))
-    block = args.ref_iters
-    total_steps = args.warmup + args.steps
+    bn = float(np.linalg.norm(b))
     t0 = time.perf_counter()
     s = O.CpuSolver(A, params, threads=threads)
     setup = time.perf_counter() - t0
-    # one step = a block of PCG iterations continued from the previous x
-    x = np.zeros_like(b)
-    r0 = bnorm
-    it_done = 0
-    for step in range(total_steps):
-        t1 = time.perf_counter()
-        x, inf = _oracle_block(O, s, b, x, block)
-        dt = time.perf_counter() - t1
-        it_done += inf["num_iterations"]
-        res_hist.append((it_done, inf["final_res_norm"]))
-        if step >= args.warmup:
-            per_iter.append(dt / max(inf["num_iterations"], 1))
-        if inf["final_res_norm"] / r0 <= 1e-8:
-            break
-    # iterations to 1e-8 from the observed true-residual decay (last half of the sample)
-    its = [h[0] for h in res_hist]
-    rs = [max(h[1], 1e-300) / r0 for h in res_hist]
-    if rs[-1] <= 1e-8:
-        n_est = its[-1]
-    else:
-        k0 = len(its) // 2
-        slope = (np.log(rs[-1]) - np.log(rs[k0])) / max(its[-1] - its[k0], 1) if len(its) > 1 else 0.0
-        n_est = its[-1] + (np.log(1e-8) - np.log(rs[-1])) / slope if slope < 0 else float("inf")
-    t_iter = statistics.mean(per_iter) if per_iter else float("nan")
-    value_ms = 1e3 * (setup + t_iter * n_est)
+    t1 = time.perf_counter()
+    x, inf = s.solve(b)
+    full = time.perf_counter() - t1
+    rel = float(np.linalg.norm(b - as_rows(A) @ x) / bn)
+    log(f"reference: setup {setup:.2f} s, solve {full:.2f} s, {inf['num_iterations']} iterations, rel {rel:.2e}")
+    samples = []
+    for step in range(args.warmup - 1 + args.steps):
+        t2 = time.perf_counter()
+        _oracle_block(O, s, b, np.zeros_like(b), args.ref_iters)
+        dt = time.perf_counter() - t2
+        if step >= args.warmup - 1:
+            samples.append(dt)
+    ms_step = 1e3 * statistics.mean(samples)
+    value_ms = 1e3 * (setup + full)
+    per_iter = ms_step / args.ref_iters
     line = {"impl": "reference", "metric": "time_to_1e-8_rel_residual", "value": value_ms, "unit": "ms",
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value_ms,
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": desc, "n": int(A.shape[0]), "nnz": int(A.nnz),
-                                            "seed": args.seed},
+            "data": "synthetic (seeded, generated on the host)",
+            "config": {"workload": desc, "n": int(A.shape[0]), "nnz": int(A.nnz), "block_size": params["block_size"],
+                       "seed": args.seed, "iterations": int(inf["num_iterations"]), "rel_residual": rel,
+                       "setup_ms": 1e3 * setup, "solve_ms": 1e3 * full, "per_iteration_ms_in_samples": per_iter,
+                       "partition": "the library's recursive bisection, restated in the oracle (same as the GPU)"},
             "cpu_baseline": {"value": value_ms, "unit": "ms", "cores": threads, "kind": "port",
-                             "sample": f"CPU restatement (oracle/) on the full system: setup {setup:.2f} s, "
-                                       f"{its[-1]} PCG iterations in blocks of {block} "
-                                       f"({1e3 * t_iter:.2f} ms/iteration), iterations to 1e-8 "
-                                       f"{'measured' if rs[-1] <= 1e-8 else 'extrapolated from the residual decay'}"
-                                       f" = {n_est:.0f}"},
+                             "sample": f"value: one complete CPU factorize ({setup:.2f} s) + PCG solve to 1e-8 "
+                                       f"({inf['num_iterations']} iterations, {full:.2f} s), measured once; "
+                                       f"each timed step: {args.ref_iters} PCG iterations of the same solver "
+                                       f"({per_iter:.1f} ms/iteration)"},
             "e2e": {"value": value_ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 def _oracle_block(O, s, b, x0, block):
-    """Run `block` more PCG iterations of the CPU solver, restarted from x0."""
+    """Run `block` PCG iterations of the CPU solver from x0."""
     import ctypes as C
     L = O.lib()
     x = np.array(x0, np.float64, copy=True)
@@ -216,36 +243,93 @@ def _oracle_block(O, s, b, x0, block):
     return x, {"num_iterations": it.value, "final_res_norm": res.value}
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="elasticity_3m",
-                    choices=["elasticity_3m", "delaunay_1m", "elasticity_24k", "elasticity_650k", "batched",
-                             "adjoint_500k"])
-    ap.add_argument("--batch-count", type=int, default=64, help="systems of the batched workload")
-    ap.add_argument("--batch-rhs", type=int, default=16, help="right-hand sides per batched system")
-    ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--mas-offdiag", default="fp32", choices=["fp32", "bf16"],
-                    help="storage of the mixed solver's level-0 off-diagonal MAS inverse tiles")
-    ap.add_argument("--ref-iters", type=int, default=25, help="PCG iterations per reference-arm step")
-    ap.add_argument("--cpu-iters", type=int, default=10, help="PCG iterations of the CPU-baseline sample")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", action="store_true",
-                    help="one factorize + solve of the mixed solver only (for the ncu launch list)")
-    args = ap.parse_args()
-    if args.profile:
-        return run_profile(args)
-    args.warmup = max(args.warmup, 3)
-    if args.impl == "reference":
-        return run_reference(args)
-    if args.workload == "batched":
-        return run_batched(args)
-    if args.workload == "adjoint_500k":
-        return run_adjoint(args)
+def cpu_baseline(A, b, params):
+    """The oracle's method on all host cores with the GPU's partition: one
+    complete factorize + solve to 1e-8, measured."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    s = O.CpuSolver(A, params, threads=threads)
+    setup = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    x, inf = s.solve(b)
+    solve = time.perf_counter() - t1
+    rel = float(np.linalg.norm(b - as_rows(A) @ x) / np.linalg.norm(b))
+    return {"value": 1e3 * (setup + solve), "unit": "ms", "cores": threads, "kind": "port",
+            "sample": f"the complete workload, measured once: CPU restatement (oracle/) with the GPU's partition, "
+                      f"factorize {setup:.2f} s + PCG to 1e-8 {solve:.2f} s ({inf['num_iterations']} iterations, "
+                      f"true rel. residual {rel:.2e})",
+            "iterations": int(inf["num_iterations"])}
 
+
+# ---------------------------------------------------------------- GPU arms
+
+def _make_solver(lss, params, precision, device, extra=None):
+    gb = {"precision": precision, "device": device}
+    if extra:
+        gb.update(extra)
+    return lss.Solver.create({"solver": "GPUHybrid", "GPUHybrid": dict(params), "gb300": gb})
+
+
+def _timed_steps(torch, s, step, stream, k, warmup, barrier, clocks=None):
+    for _ in range(warmup):
+        with torch.cuda.stream(stream):
+            step(s)
+    barrier()
+    l0 = s.get_info()["kernel_launches"]
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with clocks if clocks is not None else _Null():
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(k):
+                step(s)
+            e1.record(stream)
+        barrier()
+    return e0.elapsed_time(e1) / k, (s.get_info()["kernel_launches"] - l0) / k
+
+
+def selection_checks(s, A, params, name):
+    """The GPU's stiff-DOF set against the oracle on the full matrix, and
+    against the reference build's digest committed for this configuration."""
+    from oracle import oracle as O
+    t = time.perf_counter()
+    ref_all, _, _ = O.c_select_pipeline(A, params)
+    got = s.selected_dofs()
+    out = {"selection_matches_oracle": bool(np.array_equal(got, ref_all)), "stiff_dofs": int(len(got)),
+           "oracle_selection_s": round(time.perf_counter() - t, 2)}
+    full = os.path.join(ROOT, "tests", "golden", "ref_selection_full.json")
+    if os.path.exists(full):
+        ref = json.load(open(full)).get(name)
+        if ref is not None:
+            out["selection_sha256_matches_reference_build"] = sha256_i32(got) == ref["sha256_selected"]
+            out["gmm_selection_sha256_matches_reference_build"] = \
+                sha256_i32(s.gmm_selection()) == ref["sha256_gmm_selection"]
+    return out
+
+
+def partition_quality(s, A, bd):
+    import scipy.sparse as sp
+    perm, offs = s.partition()
+    Ar = A.tocsr()
+    n = A.shape[0]
+    r = np.repeat(np.arange(n) // bd, np.diff(Ar.indptr))
+    c = Ar.indices // bd
+    nb = n // bd
+    inv = np.empty(nb, np.int64)
+    inv[perm] = np.arange(nb)
+    part = np.empty(nb, np.int64)
+    sizes = np.diff(offs)
+    part[inv] = np.repeat(np.arange(len(sizes)), sizes)
+    off = r != c
+    G = sp.csr_matrix((np.ones(int(off.sum())), (r[off], c[off])), shape=(nb, nb))
+    G.sum_duplicates()
+    Gc = G.tocoo()
+    return {"parts": int(len(sizes)), "part_fill": float(sizes.mean() / 32),
+            "edge_cut": float((part[Gc.row] != part[Gc.col]).mean())}
+
+
+def run_ours(args):
     ws, rank, local = dist_env()
     import torch
     torch.cuda.set_device(local)
@@ -256,25 +340,35 @@ def main():
     g.build()
     import lss
 
+    t_gen = time.perf_counter()
     A, b, params, desc, info = workload(args.workload, args.seed + rank)
+    log(f"{desc}: generated n={A.shape[0]} nnz={A.nnz} in {time.perf_counter() - t_gen:.1f} s")
     n = A.shape[0]
     nnz = A.nnz
+    bd = params["block_size"]
     dev = torch.device("cuda", local)
-    gb300_common = {"device": local}
 
-    def make(precision):
-        gb = dict(gb300_common, precision=precision)
-        if precision == "mixed" and args.mas_offdiag != "fp32":
-            gb["mas_offdiag"] = args.mas_offdiag
-        p = {"solver": "GPUHybrid", "GPUHybrid": dict(params), "gb300": gb}
-        return lss.Solver.create(p)
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
 
+    # cold: a fresh solver, analyze + factorize + solve with host arrays
+    barrier()
     t0 = time.perf_counter()
-    s_mixed = make("mixed")
-    s_mixed.analyze_pattern(A)
+    s_cold = _make_solver(lss, params, "mixed", local)
+    s_cold.analyze_pattern(A)
     analyze_ms = 1e3 * (time.perf_counter() - t0)
+    s_cold.factorize(A)
+    s_cold.solve(b)
+    barrier()
+    cold_ms = 1e3 * (time.perf_counter() - t0)
+    del s_cold
+
+    s_mixed = _make_solver(lss, params, "mixed", local)
+    s_mixed.analyze_pattern(A)
     s_mixed.factorize(A)
-    s_plain = make("fp64")
+    s_plain = _make_solver(lss, params, "fp64", local)
     s_plain.factorize(A)
 
     d_vals = torch.from_numpy(np.ascontiguousarray(A.data, np.float64)).to(dev)
@@ -288,48 +382,28 @@ def main():
         d_x.zero_()
         s.solve_device(d_b.data_ptr(), d_x.data_ptr(), sh)
 
-    def barrier():
-        torch.cuda.synchronize()
-        if ws > 1:
-            torch.distributed.barrier()
-
-    def timed(s, k, clocks=None):
-        for _ in range(args.warmup):
-            with torch.cuda.stream(stream):
-                step(s)
-        barrier()
-        l0 = s.get_info()["kernel_launches"]
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        ctx = clocks if clocks is not None else _Null()
-        with ctx:
-            with torch.cuda.stream(stream):
-                e0.record(stream)
-                for _ in range(k):
-                    step(s)
-                e1.record(stream)
-            barrier()
-        ms = e0.elapsed_time(e1) / k
-        launches = (s.get_info()["kernel_launches"] - l0) / k
-        return ms, launches
-
     clocks = ClockSampler(local)
-    ms_mixed, launches = timed(s_mixed, args.steps, clocks)
+    ms_mixed, launches = _timed_steps(torch, s_mixed, step, stream, args.steps, args.warmup, barrier, clocks)
     info_m = s_mixed.get_info()
     x_m = d_x.cpu().numpy()
-    ms_plain, _ = timed(s_plain, args.steps)
+    ms_plain, _ = _timed_steps(torch, s_plain, step, stream, args.steps, args.warmup, barrier)
     info_p = s_plain.get_info()
     x_p = d_x.cpu().numpy()
+    log(f"mixed {ms_mixed:.1f} ms, plain {ms_plain:.1f} ms")
 
     # correctness of the timed solves (outer index = row, as the solver applies it)
-    import scipy.sparse as sp
-    Ar = sp.csr_matrix((A.data, A.indices, A.indptr), shape=A.shape)
+    Ar = as_rows(A)
     bn = float(np.linalg.norm(b))
     rel_m = float(np.linalg.norm(b - Ar @ x_m) / bn)
     rel_p = float(np.linalg.norm(b - Ar @ x_p) / bn)
-    # no sparse direct solve is feasible at this size: the mixed solution is
-    # compared with the plain FP64 one (both to 1e-8)
     diff_mp = float(np.linalg.norm(x_m - x_p) / np.linalg.norm(x_p))
+    # a tight FP64 solve (relative tolerance 1e-12) as the reference solution
+    s_tight = _make_solver(lss, dict(params, relative_tolerance=1e-12), "fp64", local)
+    s_tight.factorize(A)
+    x_t = s_tight.solve(b)
+    err_tight = float(np.linalg.norm(x_m - x_t) / np.linalg.norm(x_t))
+    rel_t = float(np.linalg.norm(b - Ar @ x_t) / bn)
+    del s_tight
 
     # end to end through the C ABI with host buffers (pattern analysed above)
     e2e = []
@@ -337,7 +411,7 @@ def main():
         barrier()
         t1 = time.perf_counter()
         s_mixed.factorize(A)
-        xh = s_mixed.solve(b)
+        s_mixed.solve(b)
         barrier()
         if k > 0:
             e2e.append(1e3 * (time.perf_counter() - t1))
@@ -348,6 +422,9 @@ def main():
     for kind, name in ((6, "spmv_outer"), (0, "spmv_fp64"), (4, "mas_level0_symv"), (5, "residual_spmv_prec"),
                        (1, "mas_apply")):
         ms_k, by = s_mixed.time_op(kind, 30)
+        kern[name] = {"ms": ms_k, "bytes": by, "gbs": by / (ms_k * 1e-3) / 1e9 if ms_k > 0 else None}
+    for kind, name in ((1, "mas_apply_fp64"), (4, "mas_level0_symv_fp64")):
+        ms_k, by = s_plain.time_op(kind, 30)
         kern[name] = {"ms": ms_k, "bytes": by, "gbs": by / (ms_k * 1e-3) / 1e9 if ms_k > 0 else None}
     pk, pk_src = peaks()
     hbm = float(pk.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
@@ -364,72 +441,272 @@ def main():
             "frac": ach / hbm if ach else None, "traffic": traffic, "traffic_source": traffic_src,
             "peak_source": pk_src, "per_kernel": kern}
 
-    # CPU baseline: the oracle's method on the host cores, same partition, bounded sample
+    config = {
+        "workload": desc, "n": n, "nnz": int(nnz), "block_size": bd,
+        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+        "l2": "inputs larger than L2 (matrix + MAS inverses > 129 MB), no flush",
+        "step": "factorize (values in HBM, pattern analysed once) + PCG solve to true rel. residual 1e-8",
+        "plain_fp64_ms": ms_plain, "mixed_speedup_vs_plain": ms_plain / ms_mixed,
+        "iterations_mixed": info_m["num_iterations"], "iterations_plain": info_p["num_iterations"],
+        "rel_residual_mixed": rel_m, "rel_residual_plain": rel_p,
+        "rel_diff_mixed_vs_plain_solution": diff_mp,
+        "err_vs_tight_fp64_solve": err_tight, "tight_fp64_rel_residual": rel_t,
+        "factorize_ms_mixed": 1e3 * info_m.get("time_factorize", 0.0),
+        "analyze_pattern_ms": analyze_ms, "cold_ms": cold_ms,
+        "stiff_subdomains": info_m["num_subdomains"], "max_subdomain_dofs": info_m.get("max_subdomain_dofs"),
+        "mas_levels": info_m.get("mas_levels"), "mas_omega": info_m.get("mas_omega"),
+        "spmv_gbs": kern["spmv_outer"]["gbs"], "outer_spmv": info_m.get("outer_spmv"),
+    }
+    if rank == 0:
+        config.update(selection_checks(s_mixed, A, params, args.workload))
+        config["partition"] = partition_quality(s_mixed, A, bd)
+        if args.workload == "elasticity_3m":
+            config["subbox_check"] = subbox_check(lss, local, args.seed)
+    del s_plain
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(A, b, params, s_mixed, info_m["num_iterations"], args.cpu_iters)
+        cpu = cpu_baseline(A, b, params)
+        log(f"cpu baseline {cpu['value']:.0f} ms")
 
-    res = {"ms_mixed": ms_mixed, "ms_plain": ms_plain}
     if ws > 1:
         t = torch.tensor([ms_mixed, ms_plain, e2e_ms], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms_mixed, ms_plain, e2e_ms = [float(v) for v in t.cpu()]
+        config["plain_fp64_ms"] = ms_plain
+        config["mixed_speedup_vs_plain"] = ms_plain / ms_mixed
     if rank != 0:
         return
+    extras = {}
+    if not args.no_extras and args.workload == "elasticity_3m":
+        del s_mixed
+        torch.cuda.empty_cache()
+        extras = run_extras(args, local)
     h2d = nnz * 8 + 2 * n * 8
     d2h = n * 8
     line = {
         "metric": "time_to_1e-8_rel_residual", "value": ms_mixed, "unit": "ms", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64 outer PCG / f32 MAS",
+        "scaling": "weak", "vs_baseline": None, "dtype": DTYPE_MIXED,
         "data": "synthetic (seeded, generated on the host)",
-        "config": {
-            "workload": desc, "n": n, "nnz": int(nnz), "block_size": params["block_size"],
-            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-            "l2": "inputs larger than L2 (matrix + MAS inverses > 129 MB), no flush",
-            "step": "factorize (values in HBM, pattern analysed once) + PCG solve to true rel. residual 1e-8",
-            "plain_fp64_ms": ms_plain, "mixed_speedup_vs_plain": ms_plain / ms_mixed,
-            "iterations_mixed": info_m["num_iterations"], "iterations_plain": info_p["num_iterations"],
-            "rel_residual_mixed": rel_m, "rel_residual_plain": rel_p,
-            "rel_diff_mixed_vs_plain_solution": diff_mp,
-            "factorize_ms_mixed": 1e3 * info_m.get("time_factorize", 0.0),
-            "analyze_pattern_ms": analyze_ms,
-            "stiff_dofs": info_m["num_stiff_dofs"], "stiff_subdomains": info_m["num_subdomains"],
-            "mas_levels": info_m.get("mas_levels"), "mas_omega": info_m.get("mas_omega"),
-            "spmv_gbs": kern["spmv_outer"]["gbs"], "outer_spmv": info_m.get("outer_spmv"),
-        },
+        "config": config,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": roof,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
     }
+    if extras:
+        line["configs"] = extras
     print(json.dumps(line), flush=True)
+
+
+def subbox_check(lss, device, seed):
+    """The headline's solution anchor: a 24^3-node box of the same generator
+    (41,472 DOFs), the mixed solver against SuperLU (scipy)."""
+    import scipy.sparse.linalg as spla
+    A, b, params, desc, _ = workload("elasticity_subbox", seed)
+    s = _make_solver(lss, params, "mixed", device)
+    s.factorize(A)
+    x = s.solve(b)
+    t = time.perf_counter()
+    xd = spla.splu(as_rows(A).tocsc()).solve(b)
+    return {"workload": desc, "n": int(A.shape[0]), "iterations": s.get_info()["num_iterations"],
+            "rel_residual": float(np.linalg.norm(b - as_rows(A) @ x) / np.linalg.norm(b)),
+            "err_vs_superlu": float(np.linalg.norm(x - xd) / np.linalg.norm(xd)),
+            "superlu_s": round(time.perf_counter() - t, 1)}
+
+
+# ---------------------------------------------------------------- other configurations
+
+def run_extras(args, local):
+    out = {}
+    for name, fn in (("delaunay_1m", extra_delaunay), ("adjoint_500k", extra_adjoint), ("batched", extra_batched)):
+        t = time.perf_counter()
+        try:
+            out[name] = fn(args, local)
+        except Exception as e:  # one configuration failing must not hide the others
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = round(time.perf_counter() - t, 1)
+        log(f"{name}: {json.dumps(out[name])[:400]}")
+    return out
+
+
+def extra_delaunay(args, local, steps=3, warmup=1):
+    """The 2D Delaunay Laplacian, 1M points, block size 1 (CSR): mixed vs plain
+    FP64, stiff-DOF set vs the oracle, solution vs SuperLU."""
+    import torch
+    import lss
+    import scipy.sparse.linalg as spla
+    A, b, params, desc, info = workload("delaunay_1m", args.seed)
+    n = A.shape[0]
+    dev = torch.device("cuda", local)
+    s_mixed = _make_solver(lss, params, "mixed", local)
+    s_mixed.factorize(A)
+    s_plain = _make_solver(lss, params, "fp64", local)
+    s_plain.factorize(A)
+    d_vals = torch.from_numpy(np.ascontiguousarray(A.data, np.float64)).to(dev)
+    d_b = torch.from_numpy(b).to(dev)
+    d_x = torch.zeros(n, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    def step(s):
+        s.factorize_device(d_vals.data_ptr(), stream.cuda_stream)
+        d_x.zero_()
+        s.solve_device(d_b.data_ptr(), d_x.data_ptr(), stream.cuda_stream)
+
+    ms_m, launches = _timed_steps(torch, s_mixed, step, stream, steps, warmup, torch.cuda.synchronize)
+    x_m, info_m = d_x.cpu().numpy(), s_mixed.get_info()
+    ms_p, _ = _timed_steps(torch, s_plain, step, stream, steps, warmup, torch.cuda.synchronize)
+    x_p, info_p = d_x.cpu().numpy(), s_plain.get_info()
+    Ar = as_rows(A)
+    bn = float(np.linalg.norm(b))
+    out = {"workload": desc, "n": n, "nnz": int(A.nnz), "block_size": 1, "steps": steps,
+           "mixed_ms": ms_m, "plain_fp64_ms": ms_p, "mixed_speedup_vs_plain": ms_p / ms_m,
+           "iterations_mixed": info_m["num_iterations"], "iterations_plain": info_p["num_iterations"],
+           "rel_residual_mixed": float(np.linalg.norm(b - Ar @ x_m) / bn),
+           "rel_residual_plain": float(np.linalg.norm(b - Ar @ x_p) / bn),
+           "factorize_ms_mixed": 1e3 * info_m.get("time_factorize", 0.0),
+           "stiff_subdomains": info_m["num_subdomains"], "max_subdomain_dofs": info_m.get("max_subdomain_dofs"),
+           "multifrontal_subdomains": info_m.get("multifrontal_subdomains", 0), "gpu_launches": int(launches),
+           "outer_spmv": info_m.get("outer_spmv")}
+    out.update(selection_checks(s_mixed, A, params, "delaunay_1m"))
+    t = time.perf_counter()
+    xd = spla.spsolve(Ar.tocsc(), b)
+    out["err_vs_superlu"] = float(np.linalg.norm(x_m - xd) / np.linalg.norm(xd))
+    out["superlu_rel_residual"] = float(np.linalg.norm(b - Ar @ xd) / bn)
+    out["superlu_s"] = round(time.perf_counter() - t, 1)
+    return out
+
+
+def extra_adjoint(args, local):
+    return adjoint_measure(args.seed, local, steps=2, warmup=1, fd_budget_s=45.0)
+
+
+def extra_batched(args, local):
+    return batched_measure(args.seed, local, args.batch_count, args.batch_rhs, steps=1, warmup=1)
+
+
+def adjoint_measure(seed, local, steps, warmup, fd_budget_s, max_dirs=20):
+    """Differentiation workload: x = A(theta)^-1 b on the 55^3-node Kuhn-tet cube
+    (499,125 DOFs), theta_e = exp(z_e), z ~ N(0, 1), a seeded sphere of tets
+    x1e5; L = 1/2 ||x - x*||^2.  One step = forward (assemble the values on the
+    GPU, factorize, solve to 1e-8) + backward (adjoint solve with the same
+    factorization, fused parameter-gradient kernel), through the
+    torch.autograd.Function.  The gradient is checked against finite
+    differences of the solver's own loss (FP64, tolerance 1e-10) on random
+    relative directions with the five-point stencil, within a time budget."""
+    import torch
+    from lss import gen
+    from lss import autograd as AG
+    dev = torch.device("cuda", local)
+    nodes = 55
+    t0 = time.perf_counter()
+    pattern, M, c = gen.elasticity_parametric(nodes)
+    gen_s = time.perf_counter() - t0
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ntet = M.shape[1]
+    theta = np.exp(rng.standard_normal(ntet))
+    cen = gen.tet_centroids(nodes, nodes, nodes)
+    centre = rng.uniform(0.3, 0.7, 3)
+    inside = ((cen - centre) ** 2).sum(1) < 0.2 ** 2
+    theta[inside] *= 1e5
+    n = pattern.shape[0]
+    b = rng.standard_normal(n)
+    xstar = rng.standard_normal(n)
+    base = {"block_size": 3, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4}
+
+    def system(tol, precision, max_iter):
+        p = {"solver": "GPUHybrid", "GPUHybrid": dict(base, relative_tolerance=tol, max_iter=max_iter),
+             "gb300": {"precision": precision, "device": local, "max_refinements": 2}}
+        return AG.LinearSystem(pattern, M, c, p, device=dev)
+
+    sysm = system(1e-8, "mixed", 20000)
+    bt = torch.tensor(b, dtype=torch.float64, device=dev)
+    xs = torch.tensor(xstar, dtype=torch.float64, device=dev)
+
+    def step(sys_):
+        th = torch.tensor(theta, dtype=torch.float64, device=dev, requires_grad=True)
+        x = AG.solve(th, bt, sys_)
+        L = 0.5 * ((x - xs) ** 2).sum()
+        L.backward()
+        return th.grad
+
+    for _ in range(warmup):
+        step(sysm)
+    torch.cuda.synchronize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record()
+    for _ in range(steps):
+        step(sysm)
+    e1.record()
+    e1.synchronize()
+    step_ms = e0.elapsed_time(e1) / steps
+    fwd = []
+    for _ in range(steps):
+        th = torch.tensor(theta, dtype=torch.float64, device=dev)
+        e0.record()
+        with torch.no_grad():
+            AG.solve(th, bt, sysm)
+        e2.record()
+        e2.synchronize()
+        fwd.append(e0.elapsed_time(e2))
+    info = sysm.solver.get_info()
+    fwd_ms = statistics.mean(fwd)
+    syst = system(1e-10, "fp64", 4000)
+    gt = step(syst).cpu().numpy()
+
+    def loss(t):
+        with torch.no_grad():
+            xx = AG.solve(torch.tensor(t, dtype=torch.float64, device=dev), bt, syst)
+            return 0.5 * float(((xx - xs) ** 2).sum())
+
+    drng = np.random.Generator(np.random.PCG64(7))
+    h = 1e-2
+    errs = []
+    t_fd = time.perf_counter()
+    for _ in range(max_dirs):
+        if time.perf_counter() - t_fd > fd_budget_s:
+            break
+        d = drng.standard_normal(ntet) * theta
+        fd = (-loss(theta + 2 * h * d) + 8 * loss(theta + h * d) - 8 * loss(theta - h * d)
+              + loss(theta - 2 * h * d)) / (12 * h)
+        an = float(gt @ d)
+        errs.append(abs(fd - an) / max(abs(an), 1e-300))
+    gm = step(sysm).cpu().numpy()
+    return {"metric": "adjoint_step_ms", "value": step_ms, "unit": "ms", "higher_is_better": False,
+            "workload": "elasticity_55^3_nodes_lognormal_theta_inclusion_1e5", "n": int(n),
+            "nnz": int(pattern.nnz), "parameters": int(ntet), "generate_s": round(gen_s, 1), "steps": steps,
+            "step": "forward (GPU assembly + factorize + solve to 1e-8) + backward (adjoint solve + dL/dtheta)",
+            "forward_ms": fwd_ms, "backward_ms": step_ms - fwd_ms,
+            "iterations_forward": info["num_iterations"], "max_subdomain_dofs": info.get("max_subdomain_dofs"),
+            "factorize_ms": 1e3 * info.get("time_factorize", 0.0),
+            "multifrontal_fronts": info.get("multifrontal_fronts"),
+            "fd_check": {"directions": len(errs), "stencil": "5-point, relative step 1e-2",
+                         "solver": "fp64, relative tolerance 1e-10", "budget_s": fd_budget_s,
+                         "worst_rel_err": max(errs) if errs else None,
+                         "median_rel_err": float(np.median(errs)) if errs else None},
+            "mixed_1e-8_gradient_rel_err_vs_tight": float(np.linalg.norm(gm - gt) / np.linalg.norm(gt))}
 
 
 BATCH_PARAMS = {"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4,
                 "max_iter": 20000}
 
 
-def run_batched(args):
-    """Many systems of uneven size with several right-hand sides each: all
-    systems factorized and solved at once (lss_factorize_batched_device +
-    lss_solve_batched_device, mixed precision, one host thread and one stream
-    per system) against the same solves one after another in plain FP64.
-    One step = factorize every system (values in HBM) + solve every
-    right-hand side to a true relative residual of 1e-8 (b in HBM)."""
-    ws, rank, local = dist_env()
+def batched_measure(seed, local, count, nrhs, steps, warmup):
+    """Many systems of uneven size with several right-hand sides each, all
+    factorized and solved at once (lss_factorize_batched_device +
+    lss_solve_batched_device, mixed precision) against the same solves one
+    after another in plain FP64.  One step = factorize every system (values
+    in HBM) + solve every right-hand side to a true relative residual of 1e-8
+    (b in HBM)."""
     import torch
-    torch.cuda.set_device(local)
-    import __graft_entry__ as g
-    g.build()
     import lss
     from lss import gen
     dev = torch.device("cuda", local)
     t0 = time.perf_counter()
-    systems = gen.workload_batched(seed=args.seed + rank, count=args.batch_count, nrhs=args.batch_rhs)
+    systems = gen.workload_batched(seed=seed, count=count, nrhs=nrhs)
     gen_s = time.perf_counter() - t0
-    nrhs = args.batch_rhs
     mats, vals, bs = [], [], []
     for A, B, info in systems:
         A = A.tocsc()
@@ -471,36 +748,26 @@ def run_batched(args):
                 its.append(s.get_info()["num_iterations"])
         return np.array(its)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batched_step()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local)
     l0 = s_mixed[0].get_info()["kernel_launches"]
-    with clocks:
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        t1 = time.perf_counter()
-        for _ in range(args.steps):
-            its_m = batched_step()
-        torch.cuda.synchronize()
-        e1.record()
-        e1.synchronize()
-        wall_m = (time.perf_counter() - t1) / args.steps
-    launches = (s_mixed[0].get_info()["kernel_launches"] - l0) / args.steps
-    # accuracy of the batched solves (true residual per system and right-hand side)
-    import scipy.sparse as sp
+    t1 = time.perf_counter()
+    for _ in range(steps):
+        its_m = batched_step()
+    torch.cuda.synchronize()
+    wall_m = (time.perf_counter() - t1) / steps
+    launches = (s_mixed[0].get_info()["kernel_launches"] - l0) / steps
     worst, worst_vs_floor = 0.0, 0.0
     for si, A in enumerate(mats):
         X = xs[si].cpu().numpy()
         B = bs[si].cpu().numpy()
-        Ar = A.tocsr()
+        Ar = as_rows(A)
         bn = np.linalg.norm(B.T, axis=0)
         rel = np.linalg.norm((Ar @ X.T) - B.T, axis=0) / bn
-        # FP64 rounding floor of the residual itself, eps || |A| |x| || / ||b||
         floor = np.finfo(np.float64).eps * np.linalg.norm(abs(Ar) @ abs(X.T), axis=0) / bn
         worst = max(worst, float(rel.max()))
         worst_vs_floor = max(worst_vs_floor, float((rel / np.maximum(1e-8, floor)).max()))
-    sequential_plain()  # warm-up of the plain solvers' graphs
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     its_p = sequential_plain()
@@ -508,154 +775,32 @@ def run_batched(args):
     wall_p = time.perf_counter() - t2
     nsolve = len(mats) * nrhs
     dofs = [A.shape[0] for A in mats]
-    line = {
-        "metric": "batched_throughput_solves_per_s", "value": nsolve / wall_m, "unit": "solves/s",
-        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall_m,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 outer PCG (df32 A p) / f32 MAS", "data": "synthetic (seeded, generated on the host)",
-        "config": {
-            "workload": f"batched_{len(mats)}_elasticity_inclusions_x{nrhs}_rhs",
-            "systems": len(mats), "rhs_per_system": nrhs, "dofs_min": min(dofs), "dofs_max": max(dofs),
-            "dofs_total": int(sum(dofs)), "generate_s": gen_s,
+    return {"metric": "batched_throughput_solves_per_s", "value": nsolve / wall_m, "unit": "solves/s",
+            "higher_is_better": True,
+            "workload": f"batched_{len(mats)}_elasticity_inclusions_x{nrhs}_rhs", "systems": len(mats),
+            "rhs_per_system": nrhs, "dofs_min": min(dofs), "dofs_max": max(dofs), "dofs_total": int(sum(dofs)),
+            "generate_s": round(gen_s, 1), "steps": steps, "ms_per_step": 1e3 * wall_m,
             "step": "factorize every system (values in HBM) + solve every right-hand side to true rel. residual 1e-8",
             "sequential_plain_fp64_ms": 1e3 * wall_p, "batched_speedup_vs_sequential_plain": wall_p / wall_m,
             "iterations_mixed_mean": float(its_m.mean()), "iterations_mixed_max": int(its_m.max()),
             "iterations_plain_mean": float(its_p.mean()), "iterations_plain_max": int(its_p.max()),
-            "worst_rel_residual_batched": worst,
-            "worst_rel_residual_over_max_1e-8_and_fp64_floor": worst_vs_floor,
-            "l2": "inputs larger than L2 (64 systems' matrices and MAS inverses), no flush",
-        },
-        "gpu_launches": int(launches) if launches > 0 else None,
-        "clocks": clocks.summary(),
-    }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+            "worst_rel_residual_batched": worst, "worst_rel_residual_over_max_1e-8_and_fp64_floor": worst_vs_floor,
+            "gpu_launches": int(launches) if launches > 0 else None}
 
 
-def run_adjoint(args):
-    """Differentiation workload: x = A(theta)^-1 b on the 55^3-node Kuhn-tet cube
-    (499,125 DOFs), theta_e = exp(z_e), z ~ N(0, 1), a seeded sphere of tets
-    x1e5; L = 1/2 ||x - x*||^2.  One step = forward (assemble the values on the
-    GPU, factorize, solve to 1e-8) + backward (adjoint solve with the same
-    factorization, fused parameter-gradient kernel), through the
-    torch.autograd.Function.  The gradient is checked against finite
-    differences of the solver's own loss (FP64, tolerance 1e-10) on up to 20 random
-    relative directions with the five-point stencil."""
+def run_single_extra(args, fn):
     ws, rank, local = dist_env()
     import torch
     torch.cuda.set_device(local)
     import __graft_entry__ as g
     g.build()
-    from lss import gen
-    from lss import autograd as AG
-    dev = torch.device("cuda", local)
-    nodes = 55
-    t0 = time.perf_counter()
-    pattern, M, c = gen.elasticity_parametric(nodes)
-    gen_s = time.perf_counter() - t0
-    rng = np.random.Generator(np.random.PCG64(args.seed + rank))
-    ntet = M.shape[1]
-    theta = np.exp(rng.standard_normal(ntet))
-    cen = gen.tet_centroids(nodes, nodes, nodes)
-    centre = rng.uniform(0.3, 0.7, 3)
-    inside = ((cen - centre) ** 2).sum(1) < 0.2 ** 2
-    theta[inside] *= 1e5
-    n = pattern.shape[0]
-    b = rng.standard_normal(n)
-    xstar = rng.standard_normal(n)
-    base = {"block_size": 3, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4}
-
-    def log(msg):
-        print(f"[adjoint {time.perf_counter() - t0:7.1f}s] {msg}", file=sys.stderr, flush=True)
-
-    log(f"generated {n} DOFs, {ntet} parameters in {gen_s:.1f}s")
-
-    def system(tol, precision, max_iter):
-        p = {"solver": "GPUHybrid", "GPUHybrid": dict(base, relative_tolerance=tol, max_iter=max_iter),
-             "gb300": {"precision": precision, "device": local, "max_refinements": 2}}
-        return AG.LinearSystem(pattern, M, c, p, device=dev)
-
-    sysm = system(1e-8, "mixed", 20000)
-    bt = torch.tensor(b, dtype=torch.float64, device=dev)
-    xs = torch.tensor(xstar, dtype=torch.float64, device=dev)
-
-    def step(sys_):
-        th = torch.tensor(theta, dtype=torch.float64, device=dev, requires_grad=True)
-        x = AG.solve(th, bt, sys_)
-        L = 0.5 * ((x - xs) ** 2).sum()
-        L.backward()
-        return th.grad
-
-    for _ in range(args.warmup):
-        step(sysm)
-    torch.cuda.synchronize()
     clocks = ClockSampler(local)
     with clocks:
-        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-        fwd = []
-        e0.record()
-        for _ in range(args.steps):
-            step(sysm)
-        e1.record()
-        e1.synchronize()
-        step_ms = e0.elapsed_time(e1) / args.steps
-        for _ in range(args.steps):
-            th = torch.tensor(theta, dtype=torch.float64, device=dev)
-            e0.record()
-            with torch.no_grad():
-                AG.solve(th, bt, sysm)
-            e2.record()
-            e2.synchronize()
-            fwd.append(e0.elapsed_time(e2))
-    info = sysm.solver.get_info()
-    fwd_ms = statistics.mean(fwd)
-    log(f"step {step_ms:.1f} ms, forward {fwd_ms:.1f} ms, {info['num_iterations']} iterations")
-    # finite-difference check of the gradient (tight tolerance: the loss carries
-    # solve noise of about cond(A) * tol relative), within a wall-clock budget
-    syst = system(1e-10, "fp64", 4000)
-    gt = step(syst).cpu().numpy()
-    log(f"tight gradient: {syst.solver.get_info()['num_iterations']} iterations, "
-        f"status {syst.solver.get_info()['status']}, rel. residual {syst.solver.get_info()['relative_residual']:.2e}")
-
-    def loss(t):
-        with torch.no_grad():
-            xx = AG.solve(torch.tensor(t, dtype=torch.float64, device=dev), bt, syst)
-            return 0.5 * float(((xx - xs) ** 2).sum())
-
-    drng = np.random.Generator(np.random.PCG64(7))
-    h = 1e-2
-    errs = []
-    t_fd = time.perf_counter()
-    for _ in range(20):
-        if time.perf_counter() - t_fd > 240.0:
-            break
-        d = drng.standard_normal(ntet) * theta
-        fd = (-loss(theta + 2 * h * d) + 8 * loss(theta + h * d) - 8 * loss(theta - h * d)
-              + loss(theta - 2 * h * d)) / (12 * h)
-        an = float(gt @ d)
-        errs.append(abs(fd - an) / max(abs(an), 1e-300))
-        log(f"direction {len(errs)}: rel. err {errs[-1]:.2e}")
-    # the production (mixed, 1e-8) gradient against the tight one
-    gm = step(sysm).cpu().numpy()
-    line = {
-        "metric": "adjoint_step_ms", "value": step_ms, "unit": "ms", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 outer PCG (df32 A p) / f32 MAS", "data": "synthetic (seeded)",
-        "config": {
-            "workload": "elasticity_55^3_nodes_lognormal_theta_inclusion_1e5", "n": int(n),
-            "nnz": int(pattern.nnz), "parameters": int(ntet), "generate_s": gen_s,
-            "step": "forward (GPU assembly + factorize + solve to 1e-8) + backward (adjoint solve + dL/dtheta)",
-            "forward_ms": fwd_ms, "backward_ms": step_ms - fwd_ms,
-            "iterations_forward": info["num_iterations"],
-            "fd_check": {"directions": len(errs), "stencil": "5-point, relative step 1e-2",
-                         "solver": "fp64, relative tolerance 1e-10",
-                         "worst_rel_err": max(errs), "median_rel_err": float(np.median(errs))},
-            "mixed_1e-8_gradient_rel_err_vs_tight": float(np.linalg.norm(gm - gt) / np.linalg.norm(gt)),
-        },
-        "clocks": clocks.summary(),
-    }
+        out = fn(args, local)
+    out["clocks"] = clocks.summary()
+    out["n_gpus"] = ws
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json.dumps(out), flush=True)
 
 
 def run_profile(args):
@@ -666,45 +811,48 @@ def run_profile(args):
     A, b, params, desc, info = workload(args.workload, args.seed)
     s = lss.Solver.create({"solver": "GPUHybrid", "GPUHybrid": dict(params), "gb300": {"precision": "mixed"}})
     s.factorize(A)
-    x = s.solve(b)
+    s.solve(b)
     torch.cuda.synchronize()
     inf = s.get_info()
     print(json.dumps({"profile": desc, "iterations": inf["num_iterations"], "status": inf["status"],
                       "relative_residual": inf["relative_residual"]}), flush=True)
 
 
-class _Null:
-    def __enter__(self):
-        return self
-
-    def __exit__(self, *a):
-        return False
-
-
-def cpu_baseline(A, b, params, s_gpu, gpu_iters, iters):
-    """Oracle method on the host cores with the GPU's partition: setup + `iters`
-    PCG iterations, scaled to time-to-solution with the GPU's iteration count."""
-    from oracle import oracle as O
-    import ctypes as C
-    threads = os.cpu_count() or 1
-    perm, offs = s_gpu.partition()
-    t0 = time.perf_counter()
-    s = O.CpuSolver(A, params, perm=perm, part_offsets=offs, threads=threads)
-    setup = time.perf_counter() - t0
-    O.lib().lsso_solver_set_max_iter(s.h, iters)
-    x = np.zeros_like(b)
-    it = C.c_int32(0)
-    res = C.c_double(0)
-    t1 = time.perf_counter()
-    O.lib().lsso_solver_solve(s.h, b.ctypes.data_as(C.POINTER(C.c_double)),
-                              x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(it), C.byref(res))
-    dt = time.perf_counter() - t1
-    per_iter = dt / max(it.value, 1)
-    value = 1e3 * (setup + per_iter * gpu_iters)
-    return {"value": value, "unit": "ms", "cores": threads, "kind": "port",
-            "sample": f"CPU restatement (oracle/) with the GPU's partition on the full system: setup "
-                      f"{setup:.2f} s + {it.value} PCG iterations ({1e3 * per_iter:.1f} ms each), "
-                      f"scaled to the GPU solve's {gpu_iters} iterations"}
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="elasticity_3m",
+                    choices=["elasticity_3m", "delaunay_1m", "elasticity_24k", "elasticity_650k", "batched",
+                             "adjoint_500k"])
+    ap.add_argument("--batch-count", type=int, default=64, help="systems of the batched workload")
+    ap.add_argument("--batch-rhs", type=int, default=16, help="right-hand sides per batched system")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--ref-iters", type=int, default=20, help="PCG iterations per reference-arm step")
+    ap.add_argument("--fd-budget", type=float, default=240.0, help="seconds of the adjoint FD check (alone)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="the headline configuration only")
+    ap.add_argument("--profile", action="store_true",
+                    help="one factorize + solve of the mixed solver only (for the ncu launch list)")
+    args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        if args.workload in ("batched", "adjoint_500k"):
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the headline "
+                              "configuration; the CPU method has no batched or adjoint form"}), flush=True)
+            return
+        return run_reference(args)
+    if args.workload == "batched":
+        return run_single_extra(args, lambda a, loc: batched_measure(a.seed, loc, a.batch_count, a.batch_rhs,
+                                                                       a.steps, a.warmup))
+    if args.workload == "adjoint_500k":
+        return run_single_extra(args, lambda a, loc: adjoint_measure(a.seed, loc, a.steps, a.warmup,
+                                                                       a.fd_budget))
+    return run_ours(args)
 
 
 if __name__ == "__main__":
