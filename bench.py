@@ -693,17 +693,19 @@ BATCH_PARAMS = {"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold
                 "max_iter": 20000}
 
 
-def batched_measure(seed, local, count, nrhs, steps, warmup):
-    """Many systems of uneven size with several right-hand sides each, all
-    factorized and solved at once (lss_factorize_batched_device +
-    lss_solve_batched_device, mixed precision) against the same solves one
-    after another in plain FP64.  One step = factorize every system (values
-    in HBM) + solve every right-hand side to a true relative residual of 1e-8
-    (b in HBM)."""
+def batched_measure(seed, local, count, nrhs, steps, warmup, sequential=True):
+    """Many systems of uneven size with 16 right-hand sides each, advanced by
+    the batched PCG (lss_batch_*: every kernel launch covers all systems and
+    right-hand sides).  One step = factorize every system (values in HBM) and
+    merge + solve every right-hand side to a true relative residual of 1e-8
+    (b in HBM).  Compared with the same work one solve after another, in
+    mixed precision (the gain of batching alone) and in plain FP64."""
     import torch
     import lss
     from lss import gen
     dev = torch.device("cuda", local)
+    if nrhs != lss.BATCH_RHS:
+        raise SystemExit(f"the batched PCG takes {lss.BATCH_RHS} right-hand sides per system")
     t0 = time.perf_counter()
     systems = gen.workload_batched(seed=seed, count=count, nrhs=nrhs)
     gen_s = time.perf_counter() - t0
@@ -725,7 +727,8 @@ def batched_measure(seed, local, count, nrhs, steps, warmup):
             out.append(s)
         return out
 
-    s_mixed, s_plain = make("mixed"), make("fp64")
+    s_mixed = make("mixed")
+    batch = lss.Batch(s_mixed)
     xs = [torch.zeros_like(b) for b in bs]
     vptr = [v.data_ptr() for v in vals]
     bptr = [b.data_ptr() for b in bs]
@@ -734,12 +737,12 @@ def batched_measure(seed, local, count, nrhs, steps, warmup):
     def batched_step():
         for x in xs:
             x.zero_()
-        lss.factorize_batched_device(s_mixed, vptr)
-        return lss.solve_batched_device(s_mixed, bptr, xptr, nrhs)
+        batch.factorize_device(vptr)
+        return batch.solve_device(bptr, xptr)
 
-    def sequential_plain():
+    def sequential(solvers):
         its = []
-        for si, s in enumerate(s_plain):
+        for si, s in enumerate(solvers):
             s.factorize_device(vptr[si])
             n = mats[si].shape[0]
             for k in range(nrhs):
@@ -751,13 +754,14 @@ def batched_measure(seed, local, count, nrhs, steps, warmup):
     for _ in range(warmup):
         batched_step()
     torch.cuda.synchronize()
-    l0 = s_mixed[0].get_info()["kernel_launches"]
+    l0 = batch.get_info()["kernel_launches"]
     t1 = time.perf_counter()
     for _ in range(steps):
         its_m = batched_step()
     torch.cuda.synchronize()
     wall_m = (time.perf_counter() - t1) / steps
-    launches = (s_mixed[0].get_info()["kernel_launches"] - l0) / steps
+    binfo = batch.get_info()
+    launches = (binfo["kernel_launches"] - l0) / steps
     worst, worst_vs_floor = 0.0, 0.0
     for si, A in enumerate(mats):
         X = xs[si].cpu().numpy()
@@ -768,24 +772,42 @@ def batched_measure(seed, local, count, nrhs, steps, warmup):
         floor = np.finfo(np.float64).eps * np.linalg.norm(abs(Ar) @ abs(X.T), axis=0) / bn
         worst = max(worst, float(rel.max()))
         worst_vs_floor = max(worst_vs_floor, float((rel / np.maximum(1e-8, floor)).max()))
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    its_p = sequential_plain()
-    torch.cuda.synchronize()
-    wall_p = time.perf_counter() - t2
     nsolve = len(mats) * nrhs
     dofs = [A.shape[0] for A in mats]
-    return {"metric": "batched_throughput_solves_per_s", "value": nsolve / wall_m, "unit": "solves/s",
-            "higher_is_better": True,
-            "workload": f"batched_{len(mats)}_elasticity_inclusions_x{nrhs}_rhs", "systems": len(mats),
-            "rhs_per_system": nrhs, "dofs_min": min(dofs), "dofs_max": max(dofs), "dofs_total": int(sum(dofs)),
-            "generate_s": round(gen_s, 1), "steps": steps, "ms_per_step": 1e3 * wall_m,
-            "step": "factorize every system (values in HBM) + solve every right-hand side to true rel. residual 1e-8",
-            "sequential_plain_fp64_ms": 1e3 * wall_p, "batched_speedup_vs_sequential_plain": wall_p / wall_m,
-            "iterations_mixed_mean": float(its_m.mean()), "iterations_mixed_max": int(its_m.max()),
-            "iterations_plain_mean": float(its_p.mean()), "iterations_plain_max": int(its_p.max()),
-            "worst_rel_residual_batched": worst, "worst_rel_residual_over_max_1e-8_and_fp64_floor": worst_vs_floor,
-            "gpu_launches": int(launches) if launches > 0 else None}
+    out = {"metric": "batched_throughput_solves_per_s", "value": nsolve / wall_m, "unit": "solves/s",
+           "higher_is_better": True,
+           "workload": f"batched_{len(mats)}_elasticity_inclusions_x{nrhs}_rhs", "systems": len(mats),
+           "rhs_per_system": nrhs, "dofs_min": min(dofs), "dofs_max": max(dofs), "dofs_total": int(sum(dofs)),
+           "generate_s": round(gen_s, 1), "steps": steps, "ms_per_step": 1e3 * wall_m,
+           "step": "factorize every system (values in HBM) + merge + solve every right-hand side to true rel. "
+                   "residual 1e-8 (batched PCG, one launch per kernel for all systems and right-hand sides)",
+           "factorize_ms": 1e3 * binfo["time_factorize"], "merge_ms": 1e3 * binfo["time_merge"],
+           "solve_ms": 1e3 * binfo["time_solve"], "kernels_per_graph_chunk": binfo["kernels_per_chunk"],
+           "iterations_batched_mean": float(its_m.mean()), "iterations_batched_max": int(its_m.max()),
+           "worst_rel_residual_batched": worst, "worst_rel_residual_over_max_1e-8_and_fp64_floor": worst_vs_floor,
+           "gpu_launches": int(launches) if launches > 0 else None,
+           "dtype": "f64 lane scalars and final residual, df32 vectors and A.p, f32 MAS, f64 stiff factor"}
+    if sequential:
+        sequential(s_mixed)  # warm-up of the single-system graphs
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        its_sm = sequential(s_mixed)
+        torch.cuda.synchronize()
+        wall_sm = time.perf_counter() - t2
+        del batch
+        s_plain = make("fp64")
+        sequential(s_plain[:1])
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        its_p = sequential(s_plain)
+        torch.cuda.synchronize()
+        wall_p = time.perf_counter() - t3
+        out.update({"sequential_mixed_ms": 1e3 * wall_sm, "batched_speedup_vs_sequential_mixed": wall_sm / wall_m,
+                    "sequential_plain_fp64_ms": 1e3 * wall_p,
+                    "batched_speedup_vs_sequential_plain": wall_p / wall_m,
+                    "iterations_sequential_mixed_mean": float(its_sm.mean()),
+                    "iterations_plain_mean": float(its_p.mean()), "iterations_plain_max": int(its_p.max())})
+    return out
 
 
 def run_single_extra(args, fn):

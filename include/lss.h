@@ -240,6 +240,45 @@ lss_status lss_solve_batched_device(lss_solver *const *solvers, int32_t count, c
 lss_status lss_factorize_batched_device(lss_solver *const *solvers, int32_t count, const double *const *d_values,
                                         int32_t threads);
 
+/* ---- batched PCG: one launch per step over all systems and right-hand sides */
+
+/* Number of right-hand sides per system of a batch (pad with zero columns:
+ * a zero right-hand side gives x = 0 after 0 iterations, GPUHybrid.cu:1428-1439). */
+#define LSS_BATCH_RHS 16
+
+typedef struct lss_batch lss_batch;
+
+/* No single counterpart in the reference, which solves one system per call
+ * (GPUHybrid::solve, GPUHybrid.cu:342-399).  A batch groups `count` solvers
+ * (distinct objects on one device; block size 3, "gb300": {"precision":
+ * "mixed"}, the GPUHybrid selection and the multiplicative composition).
+ * Each batched step runs the reference's PCG (GPUHybrid.cu:1413-1512) for
+ * every (system, right-hand side) lane -- own alpha, beta, gamma and stopping
+ * test -- with every kernel launch covering all systems and LSS_BATCH_RHS
+ * right-hand sides: each matrix, MAS inverse and stiff factor is read once per
+ * iteration for all of them.  The PCG vectors are double-float (FP32 pairs,
+ * about 2^-48 relative), the lane scalars and the final residual FP64.  The
+ * solvers stay owned by the caller and must outlive the batch. */
+lss_status lss_batch_create(lss_solver *const *solvers, int32_t count, lss_batch **out);
+lss_status lss_batch_destroy(lss_batch *b);
+/* Last error of `b` (NULL: of the last failed lss_batch_create on this thread). */
+const char *lss_batch_last_error(const lss_batch *b);
+
+/* GPUHybrid::factorize (GPUHybrid.cu:195-282) of every system from device
+ * values (d_values[s]: the storage order of solver s's analysed pattern), on a
+ * pool of host threads (threads <= 0: one per system), then the merge into the
+ * batch's device image. */
+lss_status lss_batch_factorize_device(lss_batch *b, const double *const *d_values, int32_t threads);
+
+/* Solve: d_b[s] and d_x[s] are device arrays of n_s x LSS_BATCH_RHS,
+ * column-major (leading dimension n_s); x is the initial guess on entry.
+ * iterations (optional, count x LSS_BATCH_RHS): PCG iterations per lane. */
+lss_status lss_batch_solve_device(lss_batch *b, const double *const *d_b, double *const *d_x,
+                                  int32_t *iterations);
+
+/* JSON: lanes' iteration statistics, timings, kernels per graph chunk. */
+lss_status lss_batch_get_info(const lss_batch *b, char *buf, size_t cap, size_t *len);
+
 /* ---- allocation-free entry point ----------------------------------------- */
 
 /* Largest n accepted by lss_gmm_select_device_noalloc. */

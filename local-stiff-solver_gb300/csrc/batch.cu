@@ -1,0 +1,856 @@
+// Kernels of the batched PCG (sm_103a): every launch covers all systems and
+// all BK right-hand sides of a batch (batch.hpp).  Block size 3.
+//
+// Precision.  GB300 issues 2 FP64 FMAs per clock and SM against 128 FP32
+// FMAs, and a batch multiplies the vector work by BK, so the PCG vectors x,
+// r, p and z are double-float pairs (hi, lo) of FP32 (the FP64 entry's 8
+// bytes, about 2^-48 relative) and every vector operation, dot product and the
+// operator product A p run on the FP32 pipe with error-free products and
+// compensated sums; the per-lane scalars alpha, beta, gamma and the stopping
+// tests are FP64, and the final residual b - A x is checked in FP64.  The
+// MAS apply is FP32, as in the single-system mixed mode; the preconditioner's
+// residual r - A z is FP32 except on the rows of stiff DOFs (double-float).
+//
+// Work decomposition.  A chunk is up to BATCH_CHUNK consecutive MAS
+// partitions of one system (<= 32 block rows each); row kernels run one CTA
+// per chunk, and a system whose lanes have all stopped skips its chunks.
+// Per-lane sums are reduced per CTA, written to a partials slot of the chunk,
+// and summed in chunk order by the last CTA of the system to arrive.
+#include <cfloat>
+
+#include "batch.hpp"
+#include "device_common.cuh"
+#include "spmv.cuh"
+
+namespace lss {
+namespace bk {
+
+constexpr int BD = 3;
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ float2 df_from(double v)
+{
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double df_val(float2 a) { return (double)a.x + (double)a.y; }
+
+// (ah, al) * b for an FP32 pair and a double-float scalar (bh, bl)
+__device__ __forceinline__ float2 df_mul(float2 a, float bh, float bl)
+{
+    const float p = __fmul_rn(a.x, bh);
+    const float e = __fmaf_rn(a.x, bh, -p);
+    const float lo = __fadd_rn(e, __fmaf_rn(a.x, bl, __fmul_rn(a.y, bh)));
+    const float s = __fadd_rn(p, lo);
+    return make_float2(s, __fsub_rn(lo, __fsub_rn(s, p)));
+}
+// a + b for pairs, renormalised
+__device__ __forceinline__ float2 df_sum(float2 a, float2 b)
+{
+    float h = a.x, l = a.y;
+    df_add(h, l, b.x, b.y);
+    const float s = __fadd_rn(h, l);
+    return make_float2(s, __fsub_rn(l, __fsub_rn(s, h)));
+}
+
+struct Chunk {
+    int sys;
+    int32_t r0, r1;  // block rows
+    int32_t p0, p1;  // MAS partitions
+};
+
+__device__ __forceinline__ Chunk chunk_of(const BatchDev &B, int c)
+{
+    Chunk k;
+    k.sys = B.chunk_sys[c];
+    k.p0 = B.chunk_p0[c];
+    k.p1 = B.chunk_p0[c + 1];
+    k.r0 = B.part_off[k.p0];
+    k.r1 = B.part_off[k.p1];
+    return k;
+}
+
+// Per-lane totals of NV values over the chunks of one system.  part[v] holds
+// the CTA's sum of value v for right-hand side threadIdx.x (threads < BK).
+// Returns true in the threads < BK of the last CTA of the system to arrive,
+// where tot[v] is the system's sum in chunk order; the counter is reset.
+template <int NV>
+__device__ bool sys_finish(const BatchDev &B, int c, int sys, const double (&part)[NV], double (&tot)[NV])
+{
+    __shared__ bool last;
+    const int t = threadIdx.x;
+    if (t < BK)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) B.partials[((int64_t)c * BK + t) * NV + v] = part[v];
+    __threadfence();
+    __syncthreads();
+    if (t == 0) {
+        const unsigned arrived = atomicAdd(B.counters + sys, 1u);
+        last = arrived == (unsigned)(B.sys_chunk0[sys + 1] - B.sys_chunk0[sys] - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    if (t < BK) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) tot[v] = 0.0;
+        for (int q = B.sys_chunk0[sys]; q < B.sys_chunk0[sys + 1]; ++q)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) tot[v] += __ldcg(B.partials + ((int64_t)q * BK + t) * NV + v);
+    }
+    if (t == 0) B.counters[sys] = 0u;
+    return t < BK;
+}
+
+// lanes of system s all stopped -> sys_done[s] (called by the finishing CTA)
+__device__ void mark_system(const BatchDev &B, int sys)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int all = 1;
+        for (int k = 0; k < BK; ++k) all &= B.lane[sys * BK + k].done != 0;
+        const_cast<int *>(B.sys_done)[sys] = all;
+    }
+}
+
+// ---------------------------------------------------------------- A p, p.Ap, alpha
+
+// One warp per block row: half-warp h takes the row's blocks l = h, h + 2, ...,
+// lane k of the half the right-hand side k; the 9 values of a block are
+// broadcast to the half-warp, p and A p move as 128-byte lines of 16 pairs.
+__global__ void __launch_bounds__(256) spmm_alpha_kernel(BatchDev B, const float2 *__restrict__ p,
+                                                         float2 *__restrict__ ap)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    if (B.sys_done[ch.sys]) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = lane >> 4, k = lane & 15;
+    float dh = 0.f, dl = 0.f;
+    for (int32_t I = ch.r0 + w; I < ch.r1; I += 8) {
+        const int32_t b = B.rows[I], len = B.rows[I + 1] - b;
+        const float2 *__restrict__ v = B.vals_df + (int64_t)b * 9;
+        float sh[BD] = {0.f, 0.f, 0.f}, sl[BD] = {0.f, 0.f, 0.f};
+        for (int32_t l = h; l < len; l += 2) {
+            const int32_t J = B.cols[b + l];
+            float2 x[BD];
+#pragma unroll
+            for (int c = 0; c < BD; ++c) x[c] = p[((int64_t)J * BD + c) * BK + k];
+#pragma unroll
+            for (int r = 0; r < BD; ++r)
+#pragma unroll
+                for (int c = 0; c < BD; ++c) {
+                    const float2 a = __ldg(v + (int64_t)(r * BD + c) * len + l);
+                    df_fma(sh[r], sl[r], a.x, a.y, x[c].x, x[c].y);
+                }
+        }
+#pragma unroll
+        for (int r = 0; r < BD; ++r) {
+            const float bh = __shfl_xor_sync(FULL, sh[r], 16), bl = __shfl_xor_sync(FULL, sl[r], 16);
+            df_add(sh[r], sl[r], bh, bl);
+        }
+        if (h == 0) {
+#pragma unroll
+            for (int r = 0; r < BD; ++r) {
+                const int64_t e = ((int64_t)I * BD + r) * BK + k;
+                const float s = __fadd_rn(sh[r], sl[r]);
+                ap[e] = make_float2(s, __fsub_rn(sl[r], __fsub_rn(s, sh[r])));
+                const float2 pk = p[e];
+                df_fma(dh, dl, pk.x, pk.y, sh[r], sl[r]);
+            }
+        }
+    }
+    __shared__ double red[8][BK];
+    if (h == 0) red[w][k] = (double)dh + (double)dl;
+    __syncthreads();
+    double part[1] = {0.0}, tot[1];
+    if (threadIdx.x < BK)
+        for (int q = 0; q < 8; ++q) part[0] += red[q][threadIdx.x];
+    if (sys_finish<1>(B, blockIdx.x, ch.sys, part, tot)) {
+        BatchLane &L = B.lane[ch.sys * BK + threadIdx.x];
+        if (!L.done) {
+            // GPUHybrid.cu:1458-1480 per lane
+            L.iter += 1;
+            const double pAp = tot[0];
+            L.pAp = pAp;
+            const double alpha = L.gamma / pAp;
+            if (pAp == 0.0) L.done = STOP_ZERO_PAP;
+            else if (!(alpha == alpha) || isinf(alpha)) L.done = STOP_NONFINITE;
+            else if (alpha <= 0.0) L.done = STOP_NEGATIVE_ALPHA;
+            else if (alpha < DBL_MIN) L.done = STOP_SUBNORMAL_ALPHA;
+            else L.alpha = alpha;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- x, r, rr, stopping tests
+
+__global__ void __launch_bounds__(256) update_xr_kernel(BatchDev B, float2 *__restrict__ x, float2 *__restrict__ r,
+                                                        const float2 *__restrict__ p, const float2 *__restrict__ ap)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    if (B.sys_done[ch.sys]) return;
+    const int k = threadIdx.x & (BK - 1);
+    const BatchLane &L = B.lane[ch.sys * BK + k];
+    const bool live = !L.done;
+    const double alpha = L.alpha;
+    const float ah = (float)alpha, al = (float)(alpha - (double)ah);
+    float rh = 0.f, rl = 0.f;
+    const int64_t e1 = (int64_t)ch.r1 * BD * BK;
+    for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x) {
+        if (!live) continue;
+        x[e] = df_sum(x[e], df_mul(p[e], ah, al));
+        const float2 d = df_mul(ap[e], ah, al);
+        const float2 ri = df_sum(r[e], make_float2(-d.x, -d.y));
+        r[e] = ri;
+        df_fma(rh, rl, ri.x, ri.y, ri.x, ri.y);
+    }
+    __shared__ double red[16][BK];
+    red[threadIdx.x >> 4][k] = (double)rh + (double)rl;
+    __syncthreads();
+    double part[1] = {0.0}, tot[1];
+    if (threadIdx.x < BK)
+        for (int q = 0; q < 16; ++q) part[0] += red[q][threadIdx.x];
+    const bool fin = sys_finish<1>(B, blockIdx.x, ch.sys, part, tot);
+    if (fin) {
+        BatchLane &M = B.lane[ch.sys * BK + threadIdx.x];
+        if (!M.done) {
+            // GPUHybrid.cu:1482-1496 per lane
+            const double rr = tot[0];
+            M.rr = rr;
+            if (!(rr == rr) || isinf(rr)) M.done = STOP_NONFINITE;
+            else if (M.rel_eps > 0 && rr / M.bb < M.rel_eps) M.done = STOP_CONVERGED_REL;
+            else if (M.abs_eps > 0 && rr < M.abs_eps) M.done = STOP_CONVERGED_ABS;
+            else if (M.iter >= M.max_iter) M.done = STOP_MAX_ITER;
+        }
+    }
+    // the finishing CTA (threads < BK returned true there) marks the system
+    __shared__ int fin_cta;
+    if (threadIdx.x == 0) fin_cta = 0;
+    __syncthreads();
+    if (fin && threadIdx.x == 0) fin_cta = 1;
+    __syncthreads();
+    if (fin_cta) mark_system(B, ch.sys);
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(256) update_p_kernel(BatchDev B, float2 *__restrict__ p, const float2 *__restrict__ z)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    if (B.sys_done[ch.sys]) return;
+    const int k = threadIdx.x & (BK - 1);
+    const BatchLane &L = B.lane[ch.sys * BK + k];
+    if (L.done) return;  // uniform per thread (k fixed): no barrier below
+    const double beta = L.beta;
+    const float bh = (float)beta, bl = (float)(beta - (double)bh);
+    const int64_t e1 = (int64_t)ch.r1 * BD * BK;
+    for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x)
+        p[e] = df_sum(z[e], df_mul(p[e], bh, bl));
+}
+
+// p = z (the first direction)
+__global__ void __launch_bounds__(256) copy_pairs_kernel(BatchDev B, float2 *__restrict__ dst,
+                                                         const float2 *__restrict__ src)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    const int64_t e1 = (int64_t)ch.r1 * BD * BK;
+    for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x) dst[e] = src[e];
+}
+
+// ---------------------------------------------------------------- true residual (FP64)
+
+// r = b - A x in FP64 (values FP64, x from its pairs), rr per lane; mode 0:
+// the start of a solve or a restart (r also replaces the recurrence residual,
+// bb recorded when first), mode 1: the final check (rr only, into L.rr)
+__global__ void __launch_bounds__(256) residual64_kernel(BatchDev B, const double *__restrict__ bvec,
+                                                         const float2 *__restrict__ x, float2 *__restrict__ r,
+                                                         int mode, double *__restrict__ out_rr)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = lane >> 4, k = lane & 15;
+    double acc_rr = 0.0;
+    for (int32_t I = ch.r0 + w; I < ch.r1; I += 8) {
+        const int32_t b = B.rows[I], len = B.rows[I + 1] - b;
+        const double *__restrict__ v = B.vals + (int64_t)b * 9;
+        double y[BD] = {0.0, 0.0, 0.0};
+        for (int32_t l = h; l < len; l += 2) {
+            const int32_t J = B.cols[b + l];
+            double xv[BD];
+#pragma unroll
+            for (int c = 0; c < BD; ++c) xv[c] = df_val(x[((int64_t)J * BD + c) * BK + k]);
+#pragma unroll
+            for (int rr = 0; rr < BD; ++rr)
+#pragma unroll
+                for (int c = 0; c < BD; ++c) y[rr] += __ldg(v + (int64_t)(rr * BD + c) * len + l) * xv[c];
+        }
+#pragma unroll
+        for (int rr = 0; rr < BD; ++rr) y[rr] += __shfl_xor_sync(FULL, y[rr], 16);
+        if (h == 0) {
+#pragma unroll
+            for (int rr = 0; rr < BD; ++rr) {
+                const int64_t e = ((int64_t)I * BD + rr) * BK + k;
+                const double ri = bvec[e] - y[rr];
+                if (mode == 0) r[e] = df_from(ri);
+                acc_rr += ri * ri;
+            }
+        }
+    }
+    __shared__ double red[8][BK];
+    if (h == 0) red[w][k] = acc_rr;
+    __syncthreads();
+    double part[1] = {0.0}, tot[1];
+    if (threadIdx.x < BK)
+        for (int q = 0; q < 8; ++q) part[0] += red[q][threadIdx.x];
+    if (sys_finish<1>(B, blockIdx.x, ch.sys, part, tot)) out_rr[ch.sys * BK + threadIdx.x] = tot[0];
+}
+
+// ---------------------------------------------------------------- MAS (FP32), BK right-hand sides
+
+// Level vectors: item-major, [(item * BD + c) * BK + k].
+
+// level 0 -> 1: per part, the sums of its nodes' entries per level-1 aggregate
+// (warp per part; lane k of half h takes the components c = h, h + 2)
+template <typename XT>
+__global__ void __launch_bounds__(256) restrict0_kernel(BatchDev B, MasDev m, const XT *__restrict__ xin,
+                                                        float *__restrict__ v)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    if (B.sys_done[ch.sys]) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = lane >> 4, k = lane & 15;
+    float *v1 = v + m.voff[1] * BK;
+    for (int32_t p = ch.p0 + w; p < ch.p1; p += 8) {
+        const int32_t lo = m.part_off[p], cnt = m.part_off[p + 1] - lo;
+        const int ncc = m.ccnt0[p];
+        const int32_t base = m.cbase0[p];
+        for (int a = 0; a < ncc; ++a)
+            for (int c = h; c < BD; c += 2) {
+                float acc = 0.f;
+                for (int j = 0; j < cnt; ++j)
+                    if (m.key0[lo + j] == a) {
+                        const XT xv = xin[((int64_t)(lo + j) * BD + c) * BK + k];
+                        if constexpr (sizeof(XT) == 8) acc += reinterpret_cast<const float2 &>(xv).x;
+                        else acc += (float)xv;
+                    }
+                v1[((int64_t)(base + a) * BD + c) * BK + k] = acc;
+            }
+    }
+}
+
+// level l -> l + 1 (warp per level-l bank)
+__global__ void __launch_bounds__(256) restrict_kernel(MasDev m, int l, float *__restrict__ v)
+{
+    const int lane = threadIdx.x & 31, h = lane >> 4, k = lane & 15;
+    const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (g >= m.nbanks[l]) return;
+    const float *vl = v + m.voff[l] * BK;
+    float *vn = v + m.voff[l + 1] * BK;
+    const int ncc = m.ccnt[l][g];
+    const int32_t base = m.cbase[l][g];
+    const uint8_t *key = m.key[l] + g * 32;
+    for (int a = 0; a < ncc; ++a)
+        for (int c = h; c < BD; c += 2) {
+            float acc = 0.f;
+            for (int j = 0; j < 32; ++j)
+                if (key[j] == a) acc += vl[((g * 32 + j) * BD + c) * BK + k];
+            vn[((int64_t)(base + a) * BD + c) * BK + k] = acc;
+        }
+}
+
+// Y (96 x BK) = Inv (96 x 96, circulant tiles) X (96 x BK) for one bank, one
+// warp: the bank's tiles are expanded into the full symmetric matrix in shared
+// memory (column j contiguous), X is staged there too, and lane (g, h)
+// accumulates rows 12g .. 12g + 11 for the right-hand sides 4h .. 4h + 3:
+// per column j one float4 of X and three float4 of Inv feed 48 FMAs.
+// Bank index = c * 32 + lane (component-major), as in the single-system MAS.
+constexpr int NB = 32 * BD;  // 96
+constexpr int MAS_SMEM_FLOATS = NB * NB + NB * BK;
+
+__device__ __forceinline__ void bank_gemm(const float *__restrict__ tiles, float *__restrict__ S,
+                                          const float *__restrict__ X, int lane, float (&y)[12][4])
+{
+    // expand: tile (c, c2 >= c), element [d][r] = Inv[c*32 + r][c2*32 + (r+d) % 32]
+    const float *t = tiles;
+    for (int c = 0; c < BD; ++c)
+        for (int c2 = c; c2 < BD; ++c2) {
+            const int nd = (c == c2) ? 17 : 32;
+            for (int d = 0; d < nd; ++d) {
+                const float a = __ldcs(t + d * 32 + lane);
+                const int i = c * 32 + lane, j = c2 * 32 + ((lane + d) & 31);
+                S[j * NB + i] = a;
+                S[i * NB + j] = a;
+            }
+            t += nd * 32;
+        }
+    __syncwarp();
+    const int g = lane >> 2, hq = lane & 3;
+#pragma unroll
+    for (int q = 0; q < 12; ++q)
+#pragma unroll
+        for (int s = 0; s < 4; ++s) y[q][s] = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < NB; ++j) {
+        const float4 xv = *reinterpret_cast<const float4 *>(X + j * BK + 4 * hq);
+        const float4 *col = reinterpret_cast<const float4 *>(S + j * NB + 12 * g);
+        float a[12];
+        const float4 a0 = col[0], a1 = col[1], a2 = col[2];
+        a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w;
+        a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
+        a[8] = a2.x; a[9] = a2.y; a[10] = a2.z; a[11] = a2.w;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) {
+            y[q][0] += a[q] * xv.x;
+            y[q][1] += a[q] * xv.y;
+            y[q][2] += a[q] * xv.z;
+            y[q][3] += a[q] * xv.w;
+        }
+    }
+}
+
+// coarse banks: u = Inv_l v (level by level, all levels in one launch)
+__global__ void __launch_bounds__(32) symv_coarse_kernel(MasDev m, const float *__restrict__ invc,
+                                                         const float *__restrict__ v, float *__restrict__ u)
+{
+    extern __shared__ float sm[];
+    float *S = sm, *X = sm + NB * NB;
+    const int lane = threadIdx.x;
+    for (int64_t gb = blockIdx.x; gb < m.ncoarse; gb += gridDim.x) {
+        int l = 1;
+        while (l + 1 < m.L && gb >= m.boff[l + 1]) ++l;
+        const int64_t b = gb - m.boff[l];
+        const float *vb = v + (m.voff[l] + b * 32 * BD) * BK;
+        // X[c*32 + r][k] = v[((b*32 + r) * BD + c) * BK + k]
+        for (int e = lane; e < NB * BK; e += 32) {
+            const int i = e / BK, kk = e % BK, c = i / 32, r = i % 32;
+            X[e] = vb[((int64_t)r * BD + c) * BK + kk];
+        }
+        __syncwarp();
+        float y[12][4];
+        bank_gemm(invc + gb * m.tile_elems, S, X, lane, y);
+        float *ub = u + (m.voff[l] + b * 32 * BD) * BK;
+        const int g = lane >> 2, hq = lane & 3;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) {
+            const int i = 12 * g + q, c = i / 32, r = i % 32;
+            *reinterpret_cast<float4 *>(ub + ((int64_t)r * BD + c) * BK + 4 * hq) =
+                make_float4(y[q][0], y[q][1], y[q][2], y[q][3]);
+        }
+        __syncwarp();
+    }
+}
+
+// u_1 += P (u_2 + P (u_3 + ...)) for every level-1 item, stopping where a
+// system has no coarser level (ccnt == 0)
+__global__ void __launch_bounds__(256) prolong_kernel(MasDev m, float *__restrict__ u)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)m.nitems[1] * BD * BK;
+    if (t >= total) return;
+    const int64_t item1 = t / (BD * BK);
+    const int rest = (int)(t % (BD * BK));
+    int64_t item[MAS_MAXL];
+    item[1] = item1;
+    int top = 1;
+    for (int l = 1; l + 1 < m.L; ++l) {
+        const int64_t bank = item[l] >> 5;
+        if (m.ccnt[l][bank] == 0) break;
+        item[l + 1] = m.cbase[l][bank] + m.key[l][item[l]];
+        top = l + 1;
+    }
+    float acc = u[(m.voff[top] + item[top] * BD) * BK + rest];
+    for (int l = top - 1; l >= 1; --l) acc = u[(m.voff[l] + item[l] * BD) * BK + rest] + acc;
+    u[(m.voff[1] + item1 * BD) * BK + rest] = acc;
+}
+
+// level 0: z = omega (Inv_0 x + u_1) (+ z with acc), as pairs; optional
+// gamma = r.z per lane (dot 1: initial gamma; dot 2: beta and the new gamma).
+// One warp per partition, four warps per CTA, one CTA per chunk.
+template <typename XT, bool ACC, int DOT>
+__global__ void __launch_bounds__(128) symv0_kernel(BatchDev B, MasDev m, const float *__restrict__ inv0,
+                                                    const float *__restrict__ u, const XT *__restrict__ xin,
+                                                    float2 *__restrict__ z, const float2 *__restrict__ rdot)
+{
+    extern __shared__ float sm[];
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    if (B.sys_done[ch.sys]) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float *S = sm + w * MAS_SMEM_FLOATS, *X = S + NB * NB;
+    const double om = B.omega[ch.sys];
+    const float oh = (float)om, ol = (float)(om - (double)oh);
+    const float *u1 = u + m.voff[1] * BK;
+    const int g = lane >> 2, hq = lane & 3;
+    float dh[4] = {0.f, 0.f, 0.f, 0.f}, dl[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int32_t p = ch.p0 + w; p < ch.p1; p += 4) {
+        const int32_t lo = m.part_off[p], cnt = m.part_off[p + 1] - lo;
+        for (int e = lane; e < NB * BK; e += 32) {
+            const int i = e / BK, kk = e % BK, c = i / 32, r = i % 32;
+            float xv = 0.f;
+            if (r < cnt) {
+                const XT v = xin[((int64_t)(lo + r) * BD + c) * BK + kk];
+                if constexpr (sizeof(XT) == 8) xv = reinterpret_cast<const float2 &>(v).x;
+                else xv = (float)v;
+            }
+            X[e] = xv;
+        }
+        __syncwarp();
+        float y[12][4];
+        bank_gemm(inv0 + (int64_t)p * m.tile_elems, S, X, lane, y);
+#pragma unroll
+        for (int q = 0; q < 12; ++q) {
+            const int i = 12 * g + q, c = i / 32, r = i % 32;
+            if (r >= cnt) continue;
+            const int32_t node = lo + r;
+            const int64_t e = ((int64_t)node * BD + c) * BK + 4 * hq;
+            float4 cu = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (m.L > 1 && m.ccnt0[p] > 0)
+                cu = *reinterpret_cast<const float4 *>(u1 + ((int64_t)(m.cbase0[p] + m.key0[node]) * BD + c) * BK +
+                                                       4 * hq);
+            const float s4[4] = {y[q][0] + cu.x, y[q][1] + cu.y, y[q][2] + cu.z, y[q][3] + cu.w};
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                float2 val = df_mul(make_float2(s4[s], 0.f), oh, ol);
+                if (ACC) val = df_sum(z[e + s], val);
+                z[e + s] = val;
+                if (DOT) {
+                    const float2 rv = rdot[e + s];
+                    df_fma(dh[s], dl[s], rv.x, rv.y, val.x, val.y);
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (DOT) {
+        __shared__ double red[4][8][BK];  // warp, row group g, rhs
+#pragma unroll
+        for (int s = 0; s < 4; ++s) red[w][g][4 * hq + s] = (double)dh[s] + (double)dl[s];
+        __syncthreads();
+        double part[1] = {0.0}, tot[1];
+        if (threadIdx.x < BK)
+            for (int q = 0; q < 4; ++q)
+                for (int gg = 0; gg < 8; ++gg) part[0] += red[q][gg][threadIdx.x];
+        if (sys_finish<1>(B, blockIdx.x, ch.sys, part, tot)) {
+            BatchLane &L = B.lane[ch.sys * BK + threadIdx.x];
+            if (!L.done) {
+                if (DOT == 2) L.beta = tot[0] / L.gamma;  // GPUHybrid.cu:1501-1504
+                L.gamma = tot[0];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- preconditioner residual
+
+// w = r - A z in FP32 (values FP32, r and z by their high words), except block
+// rows flagged precise: double-float (values as pairs, r and z as pairs)
+__global__ void __launch_bounds__(256) residual32_kernel(BatchDev B, const float2 *__restrict__ r,
+                                                         const float2 *__restrict__ z, float *__restrict__ wout)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    if (B.sys_done[ch.sys]) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = lane >> 4, k = lane & 15;
+    for (int32_t I = ch.r0 + w; I < ch.r1; I += 8) {
+        const int32_t b = B.rows[I], len = B.rows[I + 1] - b;
+        const bool precise = B.precise && B.precise[I];
+        if (!precise) {
+            const float *__restrict__ v = B.vals32 + (int64_t)b * 9;
+            float y[BD] = {0.f, 0.f, 0.f};
+            for (int32_t l = h; l < len; l += 2) {
+                const int32_t J = B.cols[b + l];
+                float xv[BD];
+#pragma unroll
+                for (int c = 0; c < BD; ++c) xv[c] = z[((int64_t)J * BD + c) * BK + k].x;
+#pragma unroll
+                for (int rr = 0; rr < BD; ++rr)
+#pragma unroll
+                    for (int c = 0; c < BD; ++c) y[rr] += __ldg(v + (int64_t)(rr * BD + c) * len + l) * xv[c];
+            }
+#pragma unroll
+            for (int rr = 0; rr < BD; ++rr) y[rr] += __shfl_xor_sync(FULL, y[rr], 16);
+            if (h == 0)
+#pragma unroll
+                for (int rr = 0; rr < BD; ++rr) {
+                    const int64_t e = ((int64_t)I * BD + rr) * BK + k;
+                    wout[e] = r[e].x - y[rr];
+                }
+        } else {
+            const float2 *__restrict__ v = B.vals_df + (int64_t)b * 9;
+            float sh[BD] = {0.f, 0.f, 0.f}, sl[BD] = {0.f, 0.f, 0.f};
+            for (int32_t l = h; l < len; l += 2) {
+                const int32_t J = B.cols[b + l];
+                float2 xv[BD];
+#pragma unroll
+                for (int c = 0; c < BD; ++c) xv[c] = z[((int64_t)J * BD + c) * BK + k];
+#pragma unroll
+                for (int rr = 0; rr < BD; ++rr)
+#pragma unroll
+                    for (int c = 0; c < BD; ++c) {
+                        const float2 a = __ldg(v + (int64_t)(rr * BD + c) * len + l);
+                        df_fma(sh[rr], sl[rr], a.x, a.y, xv[c].x, xv[c].y);
+                    }
+            }
+#pragma unroll
+            for (int rr = 0; rr < BD; ++rr) {
+                const float bh = __shfl_xor_sync(FULL, sh[rr], 16), bl = __shfl_xor_sync(FULL, sl[rr], 16);
+                df_add(sh[rr], sl[rr], bh, bl);
+            }
+            if (h == 0)
+#pragma unroll
+                for (int rr = 0; rr < BD; ++rr) {
+                    const int64_t e = ((int64_t)I * BD + rr) * BK + k;
+                    float th = r[e].x, tl = r[e].y;
+                    df_add(th, tl, -sh[rr], -sl[rr]);
+                    wout[e] = __fadd_rn(th, tl);
+                }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- stiff blocks
+
+// t[j][k] = r_d - (A z)_d for the stiff DOFs d = dofs[j]: one warp per DOF,
+// lane k of half h over the row's blocks, double-float
+__global__ void __launch_bounds__(256) stiff_gather_kernel(BatchDev B, StiffDev S, const float2 *__restrict__ r,
+                                                           const float2 *__restrict__ z, double *__restrict__ t)
+{
+    const int lane = threadIdx.x & 31, h = lane >> 4, k = lane & 15;
+    const int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= S.ndof) return;
+    const int32_t d = S.dofs[j], I = d / BD, comp = d % BD;
+    const int32_t b = B.rows[I], len = B.rows[I + 1] - b;
+    const float2 *__restrict__ v = B.vals_df + (int64_t)b * 9;
+    float sh = 0.f, sl = 0.f;
+    for (int32_t l = h; l < len; l += 2) {
+        const int32_t J = B.cols[b + l];
+#pragma unroll
+        for (int c = 0; c < BD; ++c) {
+            const float2 a = __ldg(v + (int64_t)(comp * BD + c) * len + l);
+            const float2 xv = z[((int64_t)J * BD + c) * BK + k];
+            df_fma(sh, sl, a.x, a.y, xv.x, xv.y);
+        }
+    }
+    const float bh = __shfl_xor_sync(FULL, sh, 16), bl = __shfl_xor_sync(FULL, sl, 16);
+    df_add(sh, sl, bh, bl);
+    if (h == 0) t[j * BK + k] = df_val(r[(int64_t)d * BK + k]) - ((double)sh + (double)sl);
+}
+
+// z_S += Inv t over the dense subdomains: one warp per stiff DOF row, lane k
+// of half h over the columns of its subdomain; FP64 products
+__global__ void __launch_bounds__(256) stiff_apply_kernel(StiffDev S, const double *__restrict__ t,
+                                                          float2 *__restrict__ z)
+{
+    const int lane = threadIdx.x & 31, h = lane >> 4, k = lane & 15;
+    const int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= S.ndof_dense) return;
+    const int32_t s = S.sub_of[j], o = S.off[s], m = S.off[s + 1] - o;
+    const double *row = S.inv + S.inv_off[s] + (int64_t)(j - o) * m;
+    double acc = 0.0;
+    for (int32_t q = h; q < m; q += 2) acc += row[q] * t[(int64_t)(o + q) * BK + k];
+    acc += __shfl_xor_sync(FULL, acc, 16);
+    if (h == 0) {
+        const int64_t e = (int64_t)S.dofs[j] * BK + k;
+        z[e] = df_from(df_val(z[e]) + acc);
+    }
+}
+
+// ---------------------------------------------------------------- layout changes
+
+// dst[(perm[i] * BD + c) * BK + k] = src_s[k * n_s + i * BD + c] for every system
+
+__global__ void to_batch_kernel(const ScatterSys *__restrict__ sys, int nsys, const int64_t *__restrict__ prefix,
+                                double *__restrict__ bvec, float2 *__restrict__ xpair)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= prefix[nsys]) return;
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const ScatterSys &S = sys[lo];
+    const int64_t e = t - prefix[lo];  // e = k * n_s + q
+    const int64_t n = (int64_t)S.nb * BD;
+    const int k = (int)(e / n);
+    const int64_t q = e % n;
+    const int64_t blk = q / BD, c = q % BD;
+    const int64_t dst = (((int64_t)S.row0 + S.perm[blk]) * BD + c) * BK + k;
+    if (bvec) bvec[dst] = S.src[e];
+    else xpair[dst] = df_from(S.src[e]);
+}
+
+__global__ void from_batch_kernel(const ScatterSys *__restrict__ sys, int nsys, const int64_t *__restrict__ prefix,
+                                  const float2 *__restrict__ xpair)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= prefix[nsys]) return;
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const ScatterSys &S = sys[lo];
+    const int64_t e = t - prefix[lo];
+    const int64_t n = (int64_t)S.nb * BD;
+    const int k = (int)(e / n);
+    const int64_t q = e % n;
+    const int64_t blk = q / BD, c = q % BD;
+    S.dst[e] = df_val(xpair[(((int64_t)S.row0 + S.perm[blk]) * BD + c) * BK + k]);
+}
+
+// bb per lane
+__global__ void __launch_bounds__(256) lane_norms_kernel(BatchDev B, const double *__restrict__ b,
+                                                         double *__restrict__ out)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    const int k = threadIdx.x & (BK - 1);
+    double s2 = 0.0;
+    const int64_t e1 = (int64_t)ch.r1 * BD * BK;
+    for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x) s2 += b[e] * b[e];
+    __shared__ double red[16][BK];
+    red[threadIdx.x >> 4][k] = s2;
+    __syncthreads();
+    double part[1] = {0.0}, tot[1];
+    if (threadIdx.x < BK)
+        for (int q = 0; q < 16; ++q) part[0] += red[q][threadIdx.x];
+    if (sys_finish<1>(B, blockIdx.x, ch.sys, part, tot)) out[ch.sys * BK + threadIdx.x] = tot[0];
+}
+
+__global__ void __launch_bounds__(256) zero_done_lanes_kernel(BatchDev B, float2 *__restrict__ x)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    const int k = threadIdx.x & (BK - 1);
+    const BatchLane &L = B.lane[ch.sys * BK + k];
+    if (L.bb > 0.0) return;
+    const int64_t e1 = (int64_t)ch.r1 * BD * BK;
+    for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x) x[e] = make_float2(0.f, 0.f);
+}
+
+}  // namespace bk
+
+namespace bk {
+
+void launch_spmm_alpha(const BatchDev &B, const float2 *p, float2 *ap, cudaStream_t s)
+{
+    spmm_alpha_kernel<<<B.nchunk, 256, 0, s>>>(B, p, ap);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_update_xr(const BatchDev &B, float2 *x, float2 *r, const float2 *p, const float2 *ap, cudaStream_t s)
+{
+    update_xr_kernel<<<B.nchunk, 256, 0, s>>>(B, x, r, p, ap);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_update_p(const BatchDev &B, float2 *p, const float2 *z, cudaStream_t s)
+{
+    update_p_kernel<<<B.nchunk, 256, 0, s>>>(B, p, z);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_copy_pairs(const BatchDev &B, float2 *dst, const float2 *src, cudaStream_t s)
+{
+    copy_pairs_kernel<<<B.nchunk, 256, 0, s>>>(B, dst, src);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_residual64(const BatchDev &B, const double *b, const float2 *x, float2 *r, int mode, double *rr,
+                       cudaStream_t s)
+{
+    residual64_kernel<<<B.nchunk, 256, 0, s>>>(B, b, x, r, mode, rr);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_lane_norms(const BatchDev &B, const double *b, double *bb, cudaStream_t s)
+{
+    lane_norms_kernel<<<B.nchunk, 256, 0, s>>>(B, b, bb);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_mas(const BatchDev &B, const BatchMas &M, const float2 *xin_pair, const float *xin32, float2 *z, bool acc,
+                int dot, const float2 *rdot, cudaStream_t s)
+{
+    const MasDev &m = M.m;
+    if (m.L > 1) {
+        if (xin_pair) restrict0_kernel<float2><<<B.nchunk, 256, 0, s>>>(B, m, xin_pair, M.v);
+        else restrict0_kernel<float><<<B.nchunk, 256, 0, s>>>(B, m, xin32, M.v);
+        for (int l = 1; l + 1 < m.L; ++l)
+            if (m.nbanks[l] > 0)
+                restrict_kernel<<<(unsigned)(((int64_t)m.nbanks[l] * 32 + 255) / 256), 256, 0, s>>>(m, l, M.v);
+        const size_t smem = (size_t)MAS_SMEM_FLOATS * sizeof(float);
+        raise_smem_limit((const void *)symv_coarse_kernel, smem);
+        if (m.ncoarse > 0)
+            symv_coarse_kernel<<<(unsigned)std::min<int64_t>(m.ncoarse, sm_grid(5)), 32, smem, s>>>(m, M.invc, M.v,
+                                                                                                   M.u);
+        if (m.L > 2 && m.nitems[1] > 0)
+            prolong_kernel<<<(unsigned)(((int64_t)m.nitems[1] * BD * BK + 255) / 256), 256, 0, s>>>(m, M.u);
+    }
+    const size_t smem = (size_t)4 * MAS_SMEM_FLOATS * sizeof(float);
+#define LSS_B0(XT_, X_, A_, D_)                                                                          \
+    do {                                                                                                 \
+        raise_smem_limit((const void *)symv0_kernel<XT_, A_, D_>, smem);                                 \
+        symv0_kernel<XT_, A_, D_><<<B.nchunk, 128, smem, s>>>(B, m, M.inv0, M.u, X_, z, rdot);           \
+    } while (0)
+    if (xin_pair) {
+        if (acc) {
+            if (dot == 1) LSS_B0(float2, xin_pair, true, 1);
+            else if (dot == 2) LSS_B0(float2, xin_pair, true, 2);
+            else LSS_B0(float2, xin_pair, true, 0);
+        } else {
+            if (dot == 1) LSS_B0(float2, xin_pair, false, 1);
+            else if (dot == 2) LSS_B0(float2, xin_pair, false, 2);
+            else LSS_B0(float2, xin_pair, false, 0);
+        }
+    } else {
+        if (acc) {
+            if (dot == 1) LSS_B0(float, xin32, true, 1);
+            else if (dot == 2) LSS_B0(float, xin32, true, 2);
+            else LSS_B0(float, xin32, true, 0);
+        } else {
+            if (dot == 1) LSS_B0(float, xin32, false, 1);
+            else if (dot == 2) LSS_B0(float, xin32, false, 2);
+            else LSS_B0(float, xin32, false, 0);
+        }
+    }
+#undef LSS_B0
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_residual32(const BatchDev &B, const float2 *r, const float2 *z, float *w, cudaStream_t s)
+{
+    residual32_kernel<<<B.nchunk, 256, 0, s>>>(B, r, z, w);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_stiff(const BatchDev &B, const StiffDev &S, const float2 *r, const float2 *z_in, double *t, float2 *z,
+                  cudaStream_t s)
+{
+    if (S.ndof == 0) return;
+    stiff_gather_kernel<<<(unsigned)(((int64_t)S.ndof * 32 + 255) / 256), 256, 0, s>>>(B, S, r, z_in, t);
+    if (S.ndof_dense > 0)
+        stiff_apply_kernel<<<(unsigned)(((int64_t)S.ndof_dense * 32 + 255) / 256), 256, 0, s>>>(S, t, z);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_to_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, double *bvec,
+                     float2 *xpair, cudaStream_t s)
+{
+    if (total == 0) return;
+    to_batch_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sys, nsys, prefix, bvec, xpair);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_from_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, const float2 *xpair,
+                       const BatchLane *lanes, cudaStream_t s)
+{
+    (void)lanes;
+    if (total == 0) return;
+    from_batch_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sys, nsys, prefix, xpair);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_zero_done_lanes(const BatchDev &B, float2 *x, cudaStream_t s)
+{
+    zero_done_lanes_kernel<<<B.nchunk, 256, 0, s>>>(B, x);
+    LSS_LAUNCH_CHECK();
+}
+
+}  // namespace bk
+}  // namespace lss

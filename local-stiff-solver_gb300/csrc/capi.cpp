@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "baddof.hpp"
+#include "batch.hpp"
 #include "noalloc.hpp"
 #include "solver.hpp"
 
@@ -71,6 +72,11 @@ int sm_grid(int per_sm)
 
 struct lss_solver {
     lss::HybridSolver *impl = nullptr;
+};
+
+struct lss_batch {
+    lss::BatchSolver *impl = nullptr;
+    std::string last_error;
 };
 
 namespace {
@@ -538,3 +544,86 @@ lss_status lss_op_select_bad_dofs(int32_t strategy, int32_t n, const double *sco
     });
 }
 
+// ---- batched PCG (batch.hpp)
+
+namespace {
+template <typename F>
+lss_status batch_guarded(lss_batch *b, F f)
+{
+    try {
+        f();
+        b->last_error.clear();
+        return LSS_OK;
+    } catch (const lss::Error &e) {
+        b->last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        b->last_error = "host allocation failed";
+        return LSS_ERR_OOM;
+    } catch (const std::exception &e) {
+        b->last_error = e.what();
+        return LSS_ERR_INTERNAL;
+    }
+}
+}  // namespace
+
+lss_status lss_batch_create(lss_solver *const *solvers, int32_t count, lss_batch **out)
+{
+    if (!out) return LSS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (count <= 0 || !solvers) {
+        g_create_error = "a batch needs at least one solver";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<lss::HybridSolver *> sys(count);
+    for (int32_t s = 0; s < count; ++s) {
+        if (!valid(solvers[s])) {
+            g_create_error = "invalid solver of system " + std::to_string(s);
+            return LSS_ERR_INVALID_ARGUMENT;
+        }
+        sys[s] = solvers[s]->impl;
+    }
+    lss::BatchSolver *impl = nullptr;
+    const lss_status st = guarded(nullptr, [&]() { impl = new lss::BatchSolver(sys, sys[0]->device()); });
+    if (st != LSS_OK) return st;
+    *out = new lss_batch{impl, std::string()};
+    return LSS_OK;
+}
+
+lss_status lss_batch_destroy(lss_batch *b)
+{
+    if (!b) return LSS_OK;
+    delete b->impl;
+    delete b;
+    return LSS_OK;
+}
+
+const char *lss_batch_last_error(const lss_batch *b)
+{
+    if (!b) return g_create_error.c_str();
+    return b->last_error.c_str();
+}
+
+lss_status lss_batch_factorize_device(lss_batch *b, const double *const *d_values, int32_t threads)
+{
+    if (!b || !b->impl || !d_values) return LSS_ERR_INVALID_ARGUMENT;
+    return batch_guarded(b, [&]() {
+        lss::CudaDeviceGuard guard(b->impl->device());
+        b->impl->factorize_device(d_values, threads);
+    });
+}
+
+lss_status lss_batch_solve_device(lss_batch *b, const double *const *d_b, double *const *d_x, int32_t *iterations)
+{
+    if (!b || !b->impl || !d_b || !d_x) return LSS_ERR_INVALID_ARGUMENT;
+    return batch_guarded(b, [&]() {
+        lss::CudaDeviceGuard guard(b->impl->device());
+        b->impl->solve_device(d_b, d_x, iterations);
+    });
+}
+
+lss_status lss_batch_get_info(const lss_batch *b, char *buf, size_t cap, size_t *len)
+{
+    if (!b || !b->impl) return LSS_ERR_INVALID_ARGUMENT;
+    return copy_out(b->impl->info_json(), buf, cap, len);
+}

@@ -47,6 +47,23 @@ std::atomic<unsigned long long> &launch_count();
 #define LSS_LAUNCH_CHECK() \
     (::lss::launch_count()++, ::lss::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__))
 
+// Makes `dev` current for a scope and restores the caller's device after.
+struct CudaDeviceGuard {
+    int saved = -1;
+    explicit CudaDeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&saved) != cudaSuccess) {
+            cudaGetLastError();
+            saved = -1;
+        }
+        if (saved != dev) cuda_check(cudaSetDevice(dev), "cudaSetDevice", __FILE__, __LINE__);
+    }
+    ~CudaDeviceGuard()
+    {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
+
 // Optional allocation cap for fault testing of the OOM path: at most
 // alloc_cap_bytes() more bytes than were live when the cap was set
 // (alloc_cap_base()); 0 = no cap.  Atomic: the batched entry points allocate

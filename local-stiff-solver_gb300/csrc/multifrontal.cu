@@ -418,6 +418,98 @@ __global__ void mf_scatter_kernel(MfView v, const StiffDev S, const double *__re
     }
 }
 
+// ---- solve with NR right-hand sides at once (the batched PCG): t, w and x
+// hold NR values per entry, [entry][NR]; z is a double-float pair vector.
+
+template <int NR>
+__global__ void __launch_bounds__(256) mf_forward_nr_kernel(MfView v, MfWork w, const double *__restrict__ T,
+                                                            const double *__restrict__ F, double *__restrict__ W,
+                                                            const int *sys_done, const int32_t *front_sys)
+{
+    extern __shared__ double sm[];
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    if (sys_done && sys_done[front_sys[N]]) return;
+    const int s = v.s[N], u = v.u[N], f = s + u;
+    const int chunk = (int)(blockIdx.x - w.prefix[i]);
+    double *wown = sm, *wb = sm + (int64_t)s * NR;
+    const int r0 = s + chunk * PW;
+    for (int e = threadIdx.x; e < s * NR; e += blockDim.x)
+        wown[e] = T[(int64_t)v.pos2j[v.p0[N] + e / NR] * NR + e % NR];
+    for (int e = threadIdx.x; e < PW * NR; e += blockDim.x) wb[e] = 0.0;
+    __syncthreads();
+    for (int32_t ci = v.child_off[N]; ci < v.child_off[N + 1]; ++ci) {
+        const int32_t c = v.child[ci], uc = v.u[c];
+        const double *cw = W + ((int64_t)v.woff[c] + v.s[c]) * NR;
+        const int32_t *map = v.ea_map + v.bnd_off[c];
+        for (int e = threadIdx.x; e < uc * NR; e += blockDim.x) {
+            const int m = map[e / NR], k = e % NR;
+            if (m < s) wown[m * NR + k] += cw[e];
+            else if (m >= r0 && m < r0 + PW) wb[(m - r0) * NR + k] += cw[e];
+        }
+        __syncthreads();
+    }
+    double *Wn = W + (int64_t)v.woff[N] * NR;
+    if (chunk == 0)
+        for (int e = threadIdx.x; e < s * NR; e += blockDim.x) Wn[e] = wown[e];
+    if (u == 0) return;
+    // thread (lane = output column, warp = right-hand sides warp, warp + 8, ...)
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    const int col = r0 + lane;
+    if (col >= f) return;
+    const double *Fn = F + v.foff[N];
+    for (int k = wq; k < NR; k += 8) {
+        double acc = 0.0;
+        for (int q = 0; q < s; ++q) acc += Fn[(int64_t)q * f + col] * wown[q * NR + k];
+        Wn[(int64_t)col * NR + k] = wb[lane * NR + k] - acc;
+    }
+}
+
+template <int NR>
+__global__ void __launch_bounds__(256) mf_backward_nr_kernel(MfView v, MfWork w, const double *__restrict__ F,
+                                                             const double *__restrict__ W, double *__restrict__ X,
+                                                             const int *sys_done, const int32_t *front_sys)
+{
+    extern __shared__ double sm[];
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    if (sys_done && sys_done[front_sys[N]]) return;
+    const int s = v.s[N], u = v.u[N], f = s + u;
+    const int chunk = (int)(blockIdx.x - w.prefix[i]);
+    double *vec = sm;
+    const double *Wn = W + (int64_t)v.woff[N] * NR;
+    const int32_t *bp = v.bnd_pos + v.bnd_off[N];
+    for (int e = threadIdx.x; e < f * NR; e += blockDim.x) {
+        const int q = e / NR, k = e % NR;
+        vec[e] = q < s ? Wn[e] : X[(int64_t)bp[q - s] * NR + k];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    const int c = chunk * PW + lane;
+    if (c >= s) return;
+    const double *Fn = F + v.foff[N];
+    for (int k = wq; k < NR; k += 8) {
+        double acc = 0.0;
+        for (int q = 0; q < f; ++q) acc += Fn[(int64_t)q * f + c] * vec[q * NR + k];
+        X[((int64_t)v.p0[N] + c) * NR + k] = -acc;
+    }
+}
+
+template <int NR>
+__global__ void mf_scatter_nr_kernel(MfView v, const StiffDev S, const double *__restrict__ X,
+                                     float2 *__restrict__ z)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)v.npos * NR) return;
+    const int64_t p = t / NR;
+    const int k = (int)(t % NR);
+    const int64_t e = (int64_t)S.dofs[v.pos2j[p]] * NR + k;
+    const float2 zo = z[e];
+    const double nz = (double)zo.x + (double)zo.y + X[t];
+    const float h = (float)nz;
+    z[e] = make_float2(h, (float)(nz - (double)h));
+}
+
 }  // namespace
 
 int64_t MfFactor::bytes() const
@@ -616,6 +708,37 @@ void MfFactor::solve(const StiffDev &S, double *z, float *z32, float *z_lo, cons
         LSS_LAUNCH_CHECK();
     }
     mf_scatter_kernel<<<(unsigned)((sym_.npos + 255) / 256), 256, 0, st>>>(v, S, d_x_.data(), z, z32, z_lo, done);
+    LSS_LAUNCH_CHECK();
+}
+
+void MfFactor::solve_batch(const StiffDev &S, const double *t, float2 *z, const int *sys_done,
+                           const int32_t *front_sys, cudaStream_t st)
+{
+    if (sym_.nfront == 0) return;
+    constexpr int NR = 16;
+    const MfView v = make_view(p0_, s_, u_, woff_, bnd_off_, bnd_pos_, child_off_, child_, ea_map_, front_of_pos_,
+                               pos2j_, j2pos_, poff_, foff_, sym_.j_base, sym_.npos);
+    const size_t fsmem = (size_t)(sym_.max_s + PW) * NR * sizeof(double);
+    const size_t bsmem = (size_t)sym_.max_f * NR * sizeof(double);
+    if (fsmem > 227 * 1024 || bsmem > 227 * 1024)
+        fail(LSS_ERR_UNSUPPORTED, "a stiff subdomain front (" + std::to_string(sym_.max_f) +
+                                      " variables) is too large for the batched multifrontal solve");
+    raise_smem_limit((const void *)mf_forward_nr_kernel<NR>, fsmem);
+    raise_smem_limit((const void *)mf_backward_nr_kernel<NR>, bsmem);
+    if (d_wb_.size() < (size_t)std::max<int64_t>(sym_.welems, 1) * NR) d_wb_.resize(std::max<int64_t>(sym_.welems, 1) * NR);
+    if (d_xb_.size() < (size_t)std::max<int32_t>(sym_.npos, 1) * NR) d_xb_.resize(std::max<int32_t>(sym_.npos, 1) * NR);
+    for (const Level &L : levels_) {
+        mf_forward_nr_kernel<NR><<<(unsigned)L.fwd.ctas, 256, fsmem, st>>>(v, L.fwd, t, d_F_.data(), d_wb_.data(),
+                                                                         sys_done, front_sys);
+        LSS_LAUNCH_CHECK();
+    }
+    for (int h = (int)levels_.size() - 1; h >= 0; --h) {
+        const Level &L = levels_[h];
+        mf_backward_nr_kernel<NR><<<(unsigned)L.bwd.ctas, 256, bsmem, st>>>(v, L.bwd, d_F_.data(), d_wb_.data(),
+                                                                          d_xb_.data(), sys_done, front_sys);
+        LSS_LAUNCH_CHECK();
+    }
+    mf_scatter_nr_kernel<NR><<<(unsigned)(((int64_t)sym_.npos * NR + 255) / 256), 256, 0, st>>>(v, S, d_xb_.data(), z);
     LSS_LAUNCH_CHECK();
 }
 

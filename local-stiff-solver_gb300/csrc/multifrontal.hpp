@@ -80,7 +80,15 @@ public:
     void factorize(const BsrDev &A, const StiffDev &S, int *bad, cudaStream_t s);
     // z[d] += (A_SS^-1 t)_d over the large subdomains, t = S.t
     void solve(const StiffDev &S, double *z, float *z32, float *z_lo, const int *done, cudaStream_t s);
+    // z[d][k] += (A_SS^-1 t)[d][k] for 16 right-hand sides at once: t is
+    // [stiff DOF][16] (FP64), z a [row][16] double-float pair vector.  Fronts
+    // of a system with sys_done[front_sys[N]] set are skipped.
+    void solve_batch(const StiffDev &S, const double *t, float2 *z, const int *sys_done, const int32_t *front_sys,
+                     cudaStream_t s);
     const MfSymbolic &symbolic() const { return sym_; }
+    // device front storage (f x f per front, foff offsets), for merging factors
+    const double *fronts() const { return d_F_.data(); }
+    double *fronts_mut() { return d_F_.data(); }
     int64_t bytes() const;
 
 private:
@@ -93,6 +101,7 @@ private:
     DBuf<int32_t> d_i32_;  // symbolic arrays and work-list fronts
     DBuf<int64_t> d_i64_;  // front offsets and work-list prefixes
     DBuf<double> d_F_, d_w_, d_x_, d_P_, d_D_;
+    DBuf<double> d_wb_, d_xb_;  // solve vectors of the batched solve
     const int32_t *p0_ = nullptr, *s_ = nullptr, *u_ = nullptr, *woff_ = nullptr, *bnd_off_ = nullptr,
                   *bnd_pos_ = nullptr, *child_off_ = nullptr, *child_ = nullptr, *ea_map_ = nullptr,
                   *front_of_pos_ = nullptr, *pos2j_ = nullptr, *j2pos_ = nullptr, *poff_ = nullptr;

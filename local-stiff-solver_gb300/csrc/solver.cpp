@@ -497,6 +497,11 @@ void HybridSolver::setup_stiff()
     d_sinv32_.release();
     d_st_.release();
     mf_ = std::make_unique<MfFactor>();
+    h_sdofs_.clear();
+    h_soff_.assign(1, 0);
+    h_sinvoff_.clear();
+    ndense_ = 0;
+    inv_total_ = 0;
     if (subs_.empty()) return;
     const int bd = pat_.bd;
     // subdomains with a dense inverse first, then those of the multifrontal factor
@@ -570,6 +575,11 @@ void HybridSolver::setup_stiff()
     for (const auto &sub : subs_) maxm = std::max<int64_t>(maxm, (int64_t)sub.size());
     stats_["max_subdomain_dofs"] = (double)maxm;
     stats_["dense_subdomains"] = ndense;
+    h_sdofs_ = std::move(dofs);
+    h_soff_ = std::move(off);
+    h_sinvoff_ = std::move(inv_off);
+    ndense_ = ndense;
+    inv_total_ = inv_total;
     stats_["multifrontal_subdomains"] = stiff_.nsub - ndense;
 }
 
@@ -587,6 +597,7 @@ void HybridSolver::stiff_correct(double *z, const int *done, float *z32, float *
 void HybridSolver::setup_precise_rows()
 {
     precise_rows_ = false;
+    h_precise_.clear();
     if (!p_.mixed || p_.precond_residual == 1) {
         d_precise_.release();
         return;
@@ -608,6 +619,7 @@ void HybridSolver::setup_precise_rows()
             for (int32_t d : s) mark(d);
     }
     stats_["precise_residual_block_rows"] = (double)count;
+    h_precise_ = flag;
     if (count == 0) {
         d_precise_.release();
         return;

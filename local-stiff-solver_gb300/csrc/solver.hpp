@@ -58,6 +58,7 @@ public:
     std::string last_error;
 
 private:
+    friend class BatchSolver;  // merges factorized solvers into one batched image
     // Runs a device-pointer call on the caller's stream (a non-null stream);
     // the internal stream otherwise.  Graphs captured on either replay on both.
     struct StreamScope {
@@ -128,6 +129,12 @@ private:
     DBuf<double> d_sinv_, d_st_;
     DBuf<float> d_sinv32_;
     std::unique_ptr<MfFactor> mf_;  // subdomains above STIFF_DENSE_MAX DOFs
+    // host copies of the stiff layout (batched solves merge them)
+    std::vector<int32_t> h_sdofs_, h_soff_;
+    std::vector<int64_t> h_sinvoff_;
+    int32_t ndense_ = 0;
+    int64_t inv_total_ = 0;
+    std::vector<uint8_t> h_precise_;  // block rows of the double-float preconditioner residual
     void stiff_correct(double *z, const int *done, float *z32 = nullptr, float *z_lo = nullptr);
     // PCG
     DBuf<double> d_x_, d_b_, d_r_, d_p_, d_z_, d_ap_, d_w_, d_tmp_;

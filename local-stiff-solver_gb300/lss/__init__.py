@@ -5,8 +5,8 @@ library + the C ABI of include/lss.h); this package loads it, mirrors the
 reference's linear-solver interface (``lss.Solver``), builds it in-tree
 (``lss.build``) and generates the synthetic workloads (``lss.gen``).
 """
-from .solver import (LssError, Solver, factorize_batched_device, load, partition_pattern, row_l1_norms,  # noqa: F401
-                     select_bad_dofs, solve_batched_device)
+from .solver import (BATCH_RHS, Batch, LssError, Solver, factorize_batched_device, load,  # noqa: F401
+                     partition_pattern, row_l1_norms, select_bad_dofs, solve_batched_device)
 
 __all__ = ["Solver", "LssError", "load", "row_l1_norms", "solve_batched_device", "factorize_batched_device",
-           "select_bad_dofs", "partition_pattern"]
+           "select_bad_dofs", "partition_pattern", "Batch", "BATCH_RHS"]

@@ -18,8 +18,9 @@ from . import _paths
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unknown-pragmas"]
-LIB_SOURCES = ["select.cu", "pcg.cu", "mas.cu", "stiff.cu", "multifrontal.cu", "noalloc.cu", "solver.cpp", "capi.cpp",
-               "params.cpp", "postproc.cpp", "partition.cpp", "pattern.cpp", "baddof.cpp", "mf_symbolic.cpp"]
+LIB_SOURCES = ["select.cu", "pcg.cu", "mas.cu", "stiff.cu", "multifrontal.cu", "batch.cu", "noalloc.cu", "solver.cpp",
+               "batch.cpp", "capi.cpp", "params.cpp", "postproc.cpp", "partition.cpp", "pattern.cpp", "baddof.cpp",
+               "mf_symbolic.cpp"]
 
 
 def _nvcc():

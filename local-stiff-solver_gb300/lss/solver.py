@@ -39,7 +39,11 @@ EXPORTS = [
     "lss_partition", "lss_op_row_l1_norms", "lss_op_spmv", "lss_op_spmv_outer", "lss_op_mas_apply", "lss_op_precond",
     "lss_op_time", "lss_set_memory_cap", "lss_gmm_select_device_noalloc", "lss_solve_batched_device",
     "lss_factorize_batched_device", "lss_op_row_scores", "lss_op_select_bad_dofs", "lss_partition_pattern",
+    "lss_batch_create", "lss_batch_destroy", "lss_batch_last_error", "lss_batch_factorize_device",
+    "lss_batch_solve_device", "lss_batch_get_info",
 ]
+
+BATCH_RHS = 16
 
 
 class LssError(RuntimeError):
@@ -102,10 +106,17 @@ def load(path: str | None = None):
                                          C.c_int32, _i32p, _i32p]
     L.lss_gmm_select_device_noalloc.argtypes = [C.c_int32, C.c_int64, vp, vp, C.c_double, C.c_double, C.c_int32,
                                                 vp, vp, vp]
+    L.lss_batch_create.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(vp)]
+    L.lss_batch_destroy.argtypes = [vp]
+    L.lss_batch_last_error.argtypes = [vp]
+    L.lss_batch_last_error.restype = C.c_char_p
+    L.lss_batch_factorize_device.argtypes = [vp, C.POINTER(vp), C.c_int32]
+    L.lss_batch_solve_device.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), _i32p]
+    L.lss_batch_get_info.argtypes = [vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]
     for name in EXPORTS:
         fn = getattr(L, name)
         if fn.restype is C.c_int or fn.restype is None:
-            if name not in ("lss_status_string", "lss_last_error"):
+            if name not in ("lss_status_string", "lss_last_error", "lss_batch_last_error"):
                 fn.restype = C.c_int
     if path == _paths.lib_path():
         _lib = L
@@ -190,6 +201,57 @@ def factorize_batched_device(solvers, d_values, threads: int = 0) -> None:
     st = L.lss_factorize_batched_device(S, count, V, threads)
     if st:
         raise LssError(st, L.lss_last_error(None).decode())
+
+
+class Batch:
+    """Batched PCG over factorized solvers (lss_batch_*): every step is one
+    launch per kernel over all systems and BATCH_RHS right-hand sides each."""
+
+    def __init__(self, solvers):
+        self._L = load()
+        self._h = C.c_void_p()
+        self._solvers = list(solvers)  # the batch reads their factorizations
+        S = (C.c_void_p * len(self._solvers))(*[s._h.value for s in self._solvers])
+        st = self._L.lss_batch_create(S, len(self._solvers), C.byref(self._h))
+        if st:
+            raise LssError(st, self._L.lss_batch_last_error(None).decode())
+
+    def _check(self, st):
+        if st:
+            raise LssError(st, self._L.lss_batch_last_error(self._h).decode())
+
+    def factorize_device(self, d_values, threads: int = 0):
+        V = (C.c_void_p * len(self._solvers))(*[int(p) for p in d_values])
+        self._check(self._L.lss_batch_factorize_device(self._h, V, threads))
+
+    def solve_device(self, d_b, d_x) -> np.ndarray:
+        """d_b[s], d_x[s]: device pointers to n_s x BATCH_RHS column-major
+        arrays (x: initial guess in, solution out).  Returns the iterations,
+        shape (count, BATCH_RHS)."""
+        n = len(self._solvers)
+        B = (C.c_void_p * n)(*[int(p) for p in d_b])
+        X = (C.c_void_p * n)(*[int(p) for p in d_x])
+        its = np.zeros(n * BATCH_RHS, np.int32)
+        self._check(self._L.lss_batch_solve_device(self._h, B, X, _p(its, _i32p)))
+        return its.reshape(n, BATCH_RHS)
+
+    def get_info(self) -> dict:
+        n = C.c_size_t(0)
+        self._L.lss_batch_get_info(self._h, None, 0, C.byref(n))
+        buf = C.create_string_buffer(n.value + 1)
+        self._check(self._L.lss_batch_get_info(self._h, buf, n.value + 1, C.byref(n)))
+        return json.loads(buf.value.decode())
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.lss_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 BAD_DOF_STRATEGIES = {"elbow": 1, "kmean": 2, "gmm": 3}

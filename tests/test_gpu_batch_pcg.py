@@ -1,0 +1,101 @@
+"""The batched PCG (lss_batch_*) through the C ABI: several elasticity systems
+of uneven size with stiff inclusions (E ratios 1e3 .. 1e7, some above the
+dense stiff-block size, so the merged multifrontal factor is exercised), 16
+right-hand sides each, advanced by one PCG whose every launch covers all
+systems and right-hand sides.
+
+* every (system, right-hand side) lane reaches a true relative residual of
+  max(1e-8, 2 x its FP64 rounding floor eps ||A||x|| / ||b||) and agrees with
+  scipy's FP64 sparse direct solve to 1e-6;
+* the lanes' iteration counts stay close to those of the single-system solver
+  (the same PCG per lane, vectors in double-float instead of FP64);
+* a zero right-hand side gives x = 0 after 0 iterations (GPUHybrid.cu:1428-1439);
+* a second solve reproduces the first bit for bit (fixed-order reductions);
+* a solver outside the batched form (plain FP64) is rejected.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = {"block_size": 3, "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4,
+          "max_iter": 20000}
+
+
+def _systems():
+    from lss import gen
+    out = []
+    for A, B, info in gen.workload_batched(seed=5, count=6, dof_lo=3_000, dof_hi=40_000, nrhs=16, radius=0.25):
+        A = A.tocsc()
+        A.sum_duplicates()
+        out.append((A, np.asfortranarray(B)))
+    return out
+
+
+def test_batch_pcg_matches_direct_and_single_solves(built):
+    import torch
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    import lss
+    dev = torch.device("cuda", 0)
+    systems = _systems()
+    solvers, vals, bs, xs = [], [], [], []
+    for A, B in systems:
+        s = lss.Solver.create({"solver": "GPUHybrid", "GPUHybrid": PARAMS, "gb300": {"precision": "mixed"}})
+        s.analyze_pattern(A)
+        solvers.append(s)
+        vals.append(torch.tensor(A.data, dtype=torch.float64, device=dev))
+        Bz = B.copy()
+        Bz[:, 5] = 0.0  # one zero right-hand side per system
+        bs.append(torch.tensor(Bz.T.copy(), dtype=torch.float64, device=dev))  # row k = right-hand side k
+        xs.append(torch.zeros_like(bs[-1]))
+    batch = lss.Batch(solvers)
+    batch.factorize_device([v.data_ptr() for v in vals])
+    assert any(s.get_info().get("multifrontal_subdomains", 0) > 0 for s in solvers)
+    its = batch.solve_device([b.data_ptr() for b in bs], [x.data_ptr() for x in xs])
+    torch.cuda.synchronize()
+    info = batch.get_info()
+    assert its.shape == (len(systems), lss.BATCH_RHS)
+    X1 = [x.cpu().numpy().copy() for x in xs]
+    eps = np.finfo(np.float64).eps
+    for si, ((A, B), s) in enumerate(zip(systems, solvers)):
+        Ar = sp.csr_matrix((A.data, A.indices, A.indptr), shape=A.shape)
+        lu = spla.splu(Ar.tocsc())
+        single_its = []
+        for k in range(lss.BATCH_RHS):
+            x = X1[si][k]
+            if k == 5:
+                assert its[si, k] == 0 and np.all(x == 0.0), (si, its[si, k])
+                continue
+            b = B[:, k]
+            bn = np.linalg.norm(b)
+            rel = np.linalg.norm(b - Ar @ x) / bn
+            floor = eps * np.linalg.norm(abs(Ar) @ abs(x)) / bn
+            assert rel <= max(1e-8, 2 * floor), (si, k, rel, floor)
+            xd = lu.solve(b)
+            assert np.linalg.norm(x - xd) <= 1e-6 * np.linalg.norm(xd), (si, k)
+            if k < 3:  # the same lane through the single-system solver
+                x1 = torch.zeros(A.shape[0], dtype=torch.float64, device=dev)
+                s.solve_device(torch.tensor(b, dtype=torch.float64, device=dev).data_ptr(), x1.data_ptr())
+                torch.cuda.synchronize()
+                single_its.append(s.get_info()["num_iterations"])
+                assert its[si, k] <= 1.25 * single_its[-1] + 10, (si, k, its[si, k], single_its[-1])
+    # deterministic: a second solve from the same start gives the same bits
+    for x in xs:
+        x.zero_()
+    its2 = batch.solve_device([b.data_ptr() for b in bs], [x.data_ptr() for x in xs])
+    torch.cuda.synchronize()
+    assert np.array_equal(its, its2)
+    for si in range(len(systems)):
+        np.testing.assert_array_equal(xs[si].cpu().numpy(), X1[si])
+    assert info["kernels_per_chunk"] > 0 and info["max_iterations"] == int(its.max())
+
+
+def test_batch_pcg_rejects_other_forms(built):
+    import lss
+    A, B = _systems()[0]
+    s = lss.Solver.create({"solver": "GPUHybrid", "GPUHybrid": PARAMS, "gb300": {"precision": "fp64"}})
+    s.factorize(A)
+    with pytest.raises(lss.LssError) as e:
+        lss.Batch([s])
+    assert "mixed precision" in str(e.value)
