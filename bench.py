@@ -856,6 +856,7 @@ def main():
     ap.add_argument("--fd-budget", type=float, default=240.0, help="seconds of the adjoint FD check (alone)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="the headline configuration only")
+    ap.add_argument("--no-sequential", action="store_true", help="batched workload without the sequential baselines")
     ap.add_argument("--profile", action="store_true",
                     help="one factorize + solve of the mixed solver only (for the ncu launch list)")
     args = ap.parse_args()
@@ -870,7 +871,8 @@ def main():
         return run_reference(args)
     if args.workload == "batched":
         return run_single_extra(args, lambda a, loc: batched_measure(a.seed, loc, a.batch_count, a.batch_rhs,
-                                                                       a.steps, a.warmup))
+                                                                       a.steps, a.warmup,
+                                                                       sequential=not a.no_sequential))
     if args.workload == "adjoint_500k":
         return run_single_extra(args, lambda a, loc: adjoint_measure(a.seed, loc, a.steps, a.warmup,
                                                                        a.fd_budget))

@@ -134,6 +134,14 @@ lss_status lss_grad_params_device(lss_solver *s, const double *d_lambda, const d
                                   const int64_t *d_mt_rowptr, const int32_t *d_mt_cols,
                                   const double *d_mt_vals, double *d_dtheta, void *stream);
 
+/* Forward of the same linear parameterisation (no counterpart in the
+ * reference): d_values[v] = sum_e M[v][e] theta[e] + c[v] for the n_values
+ * stored entries of A, with M in CSR (d_m_rowptr[n_values + 1], column = the
+ * parameter e); d_c may be NULL.  Device pointers, ordered on `stream`. */
+lss_status lss_assemble_values_device(int64_t n_values, const int64_t *d_m_rowptr, const int32_t *d_m_cols,
+                                      const double *d_m_vals, const double *d_theta, const double *d_c,
+                                      double *d_values, void *stream);
+
 /* The selected stiff DOF set after post-processing (the union of the stiff
  * subdomains, ascending; GPUHybrid.cu:240-262 d_all_bad_dofs).  With
  * out == NULL only *count is written. */

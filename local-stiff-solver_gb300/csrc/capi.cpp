@@ -261,6 +261,20 @@ lss_status lss_grad_params_device(lss_solver *s, const double *d_lambda, const d
     });
 }
 
+lss_status lss_assemble_values_device(int64_t n_values, const int64_t *d_m_rowptr, const int32_t *d_m_cols,
+                                      const double *d_m_vals, const double *d_theta, const double *d_c,
+                                      double *d_values, void *stream)
+{
+    if (n_values < 0 || (n_values > 0 && (!d_m_rowptr || !d_m_cols || !d_m_vals || !d_theta || !d_values))) {
+        g_create_error = "invalid parameter-map arguments";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    return guarded(nullptr, [&]() {
+        lss::launch_assemble_values(n_values, d_m_rowptr, d_m_cols, d_m_vals, d_theta, d_c, d_values,
+                                    (cudaStream_t)stream);
+    });
+}
+
 lss_status lss_selected_dofs(const lss_solver *s, int32_t *out, int32_t cap, int32_t *count)
 {
     if (!valid(s) || !count) return LSS_ERR_INVALID_ARGUMENT;

@@ -148,6 +148,9 @@ void launch_grad_params(int32_t nparams, const int64_t *mt_rowptr, const int32_t
                         const int32_t *row_of, const int32_t *inner, const double *lambda, const double *x,
                         double *dtheta, cudaStream_t s);
 void launch_row_of(int32_t n, const int32_t *outer, int32_t *row_of, cudaStream_t s);
+// out[v] = sum_k mvals[k] theta[mcols[k]] over CSR row v (+ c[v], c optional)
+void launch_assemble_values(int64_t nvals, const int64_t *rowptr, const int32_t *mcols, const double *mvals,
+                            const double *theta, const double *c, double *out, cudaStream_t s);
 
 // ---------------------------------------------------------------- MAS
 constexpr int MAS_MAXL = 7;

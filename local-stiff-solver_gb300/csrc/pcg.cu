@@ -370,6 +370,21 @@ __global__ void __launch_bounds__(256) grad_params_kernel(int32_t nparams, const
     }
 }
 
+// values[v] = sum_k mvals[k] theta[mcols[k]] over the CSR row v of M, + c[v]:
+// one thread per stored entry of A (rows of a few dozen parameters)
+__global__ void __launch_bounds__(256) assemble_values_kernel(int64_t nvals, const int64_t *__restrict__ rowptr,
+                                                              const int32_t *__restrict__ mcols,
+                                                              const double *__restrict__ mvals,
+                                                              const double *__restrict__ theta,
+                                                              const double *__restrict__ c, double *__restrict__ out)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvals; v += (int64_t)gridDim.x * blockDim.x) {
+        double acc = c ? c[v] : 0.0;
+        for (int64_t k = rowptr[v]; k < rowptr[v + 1]; ++k) acc += mvals[k] * theta[mcols[k]];
+        out[v] = acc;
+    }
+}
+
 __global__ void row_of_kernel(int32_t n, const int32_t *__restrict__ outer, int32_t *__restrict__ row_of)
 {
     const int lane = threadIdx.x & 31;
@@ -613,6 +628,15 @@ void launch_grad_params(int32_t nparams, const int64_t *mt_rowptr, const int32_t
     if (nparams <= 0) return;
     grad_params_kernel<<<grid_for((int64_t)nparams * 32, 256, sm_grid(16)), 256, 0, s>>>(
         nparams, mt_rowptr, mt_cols, mt_vals, row_of, inner, lambda, x, dtheta);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_assemble_values(int64_t nvals, const int64_t *rowptr, const int32_t *mcols, const double *mvals,
+                            const double *theta, const double *c, double *out, cudaStream_t s)
+{
+    if (nvals <= 0) return;
+    assemble_values_kernel<<<grid_for(nvals, 256, sm_grid(16)), 256, 0, s>>>(nvals, rowptr, mcols, mvals, theta, c,
+                                                                            out);
     LSS_LAUNCH_CHECK();
 }
 

@@ -2,7 +2,7 @@
 
 A(theta) is linear in the parameters: A.values = M @ theta + c on a fixed
 pattern (one Young's modulus per element, say).  Forward: assemble the values
-on the GPU, factorize with them in device memory, solve.  Backward: the
+on the GPU (the library's kernel), factorize with them in device memory, solve.  Backward: the
 adjoint reuses the same factorized hybrid preconditioner and PCG to solve
 A^T lambda = dL/dx (A is SPD), then dL/db = lambda and
 dL/dtheta_e = -sum_{ij in e} M_(ij),e lambda_i x_j, formed by the library's
@@ -35,9 +35,11 @@ class LinearSystem:
         self.solver.analyze_pattern(self.pattern)
         M = sp.csr_matrix(M)
         self.n_params = M.shape[1]
-        Mc = M.tocoo()
-        self.M = torch.sparse_coo_tensor(np.vstack([Mc.row, Mc.col]), Mc.data, M.shape,
-                                         dtype=torch.float64, device=self.device).coalesce()
+        self.n_values = M.shape[0]
+        # M in CSR (rows = stored entries of A): the forward's values = M theta + c
+        self.m_rowptr = torch.from_numpy(M.indptr.astype(np.int64)).to(self.device)
+        self.m_cols = torch.from_numpy(M.indices.astype(np.int32)).to(self.device)
+        self.m_vals = torch.from_numpy(M.data.astype(np.float64)).to(self.device)
         Mt = M.T.tocsr()
         self.mt_rowptr = torch.from_numpy(Mt.indptr.astype(np.int64)).to(self.device)
         self.mt_cols = torch.from_numpy(Mt.indices.astype(np.int32)).to(self.device)
@@ -45,7 +47,17 @@ class LinearSystem:
         self.c = torch.from_numpy(np.asarray(c, np.float64)).to(self.device)
 
     def values(self, theta):
-        return torch.sparse.mm(self.M, theta.reshape(-1, 1)).reshape(-1) + self.c
+        """A.values = M theta + c, by the library's kernel (lss_assemble_values_device)."""
+        from .solver import LssError, load
+        th = theta.contiguous()
+        out = torch.empty(self.n_values, dtype=torch.float64, device=self.device)
+        L = load()
+        st = L.lss_assemble_values_device(self.n_values, self.m_rowptr.data_ptr(), self.m_cols.data_ptr(),
+                                          self.m_vals.data_ptr(), th.data_ptr(), self.c.data_ptr(), out.data_ptr(),
+                                          _stream_handle())
+        if st:
+            raise LssError(st, L.lss_last_error(None).decode())
+        return out
 
 
 class LinearSolve(torch.autograd.Function):

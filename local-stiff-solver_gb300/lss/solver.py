@@ -40,7 +40,7 @@ EXPORTS = [
     "lss_op_time", "lss_set_memory_cap", "lss_gmm_select_device_noalloc", "lss_solve_batched_device",
     "lss_factorize_batched_device", "lss_op_row_scores", "lss_op_select_bad_dofs", "lss_partition_pattern",
     "lss_batch_create", "lss_batch_destroy", "lss_batch_last_error", "lss_batch_factorize_device",
-    "lss_batch_solve_device", "lss_batch_get_info",
+    "lss_batch_solve_device", "lss_batch_get_info", "lss_assemble_values_device",
 ]
 
 BATCH_RHS = 16
@@ -106,6 +106,7 @@ def load(path: str | None = None):
                                          C.c_int32, _i32p, _i32p]
     L.lss_gmm_select_device_noalloc.argtypes = [C.c_int32, C.c_int64, vp, vp, C.c_double, C.c_double, C.c_int32,
                                                 vp, vp, vp]
+    L.lss_assemble_values_device.argtypes = [C.c_int64, vp, vp, vp, vp, vp, vp, vp]
     L.lss_batch_create.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(vp)]
     L.lss_batch_destroy.argtypes = [vp]
     L.lss_batch_last_error.argtypes = [vp]

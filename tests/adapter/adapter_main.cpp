@@ -1,9 +1,10 @@
 // Drives include/lss_polysolve.hpp the way polysolve's callers do
 // (Solver::create -> set_parameters -> analyze_pattern -> factorize -> solve
 // -> get_info; tests/linear_solve.cpp:433-475 of the reference): a 2D
-// five-point Laplacian with a stiff square (x1e6), solved to 1e-10.
-// Prints one line: "ok <name> <iterations> <relative residual>", or
-// "error <message>" (exit 2) when the library refuses, e.g. without a GPU.
+// five-point Laplacian with a stiff square (x1e6), solved to 1e-8.
+// Prints one line: "ok <name> <iterations> <relative residual> <FP64 floor
+// eps || |A| |x| || / ||b||>", or "error <message>" (exit 2) when the library
+// refuses, e.g. without a GPU.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -49,21 +50,26 @@ int main()
     try {
         std::unique_ptr<linear::Solver> s = std::make_unique<linear::LssGPUHybrid>();
         s->set_parameters(json::parse(R"({"solver": "GPUHybrid", "GPUHybrid": {"block_size": 1,
-            "relative_tolerance": 1e-10, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4}})"));
+            "relative_tolerance": 1e-8, "gmm_jump_threshold": 10.0, "min_subdomain_size": 4}})"));
         s->analyze_pattern(A, 1);
         s->factorize(A);
         const Eigen::VectorXd &cb = b;
         s->solve(linear::Solver::Ref<const Eigen::VectorXd>(cb), linear::Solver::Ref<Eigen::VectorXd>(x));
         json info;
         s->get_info(info);
-        double rr = 0.0, bb = 0.0;
+        double rr = 0.0, bb = 0.0, ff = 0.0;
         for (int r = 0; r < n; ++r) {
-            double ax = 0.0;
-            for (int k = outer[r]; k < outer[r + 1]; ++k) ax += vals[k] * x[inner[k]];
+            double ax = 0.0, aax = 0.0;
+            for (int k = outer[r]; k < outer[r + 1]; ++k) {
+                ax += vals[k] * x[inner[k]];
+                aax += std::fabs(vals[k] * x[inner[k]]);
+            }
             rr += (b[r] - ax) * (b[r] - ax);
             bb += b[r] * b[r];
+            ff += aax * aax;
         }
-        std::printf("ok %s %s %.3e\n", s->name().c_str(), info["num_iterations"].dump().c_str(), std::sqrt(rr / bb));
+        std::printf("ok %s %s %.3e %.3e\n", s->name().c_str(), info["num_iterations"].dump().c_str(),
+                    std::sqrt(rr / bb), 2.220446049250313e-16 * std::sqrt(ff / bb));
         return 0;
     } catch (const std::exception &e) {
         std::printf("error %s\n", e.what());
