@@ -54,7 +54,7 @@ struct BatchSolver::Impl {
     DBuf<int64_t> sinvoff;
     DBuf<double> sinv, t;
     // vectors [n][BK]
-    DBuf<double> b, rr;
+    DBuf<double> b, rr, xt;  // right-hand sides, lane sums, the solution (FP64)
     DBuf<float2> x, r, p, z, ap;
     DBuf<float> w;
     // host
@@ -449,6 +449,7 @@ void BatchSolver::merge()
     // ---- vectors and the device view
     const int64_t nvec = (int64_t)nb * BDIM * BK;
     D.b.resize(nvec);
+    D.xt.resize(nvec);
     for (DBuf<float2> *v : {&D.x, &D.r, &D.p, &D.z, &D.ap}) v->resize(nvec);
     D.w.resize(nvec);
     BatchDev &B = D.B;
@@ -546,10 +547,11 @@ void BatchSolver::solve_device(const double *const *d_b, double *const *d_x, int
     }
     D.scat.upload(tab, stream_);
     D.scat_prefix.upload(prefix, stream_);
-    bk::launch_to_batch(D.scat.data(), ns, D.scat_prefix.data(), prefix[ns], D.b.data(), nullptr, stream_);
+    bk::launch_to_batch(D.scat.data(), ns, D.scat_prefix.data(), prefix[ns], D.b.data(), stream_);
     for (int32_t s = 0; s < ns; ++s) tab[s].src = d_x[s];
     D.scat.upload(tab, stream_);
-    bk::launch_to_batch(D.scat.data(), ns, D.scat_prefix.data(), prefix[ns], nullptr, D.x.data(), stream_);
+    bk::launch_to_batch(D.scat.data(), ns, D.scat_prefix.data(), prefix[ns], D.xt.data(), stream_);
+    D.x.zero(stream_);
     // lane states
     bk::launch_lane_norms(D.B, D.b.data(), D.rr.data(), stream_);
     D.h_rr.resize((size_t)ns * BK);
@@ -586,8 +588,9 @@ void BatchSolver::solve_device(const double *const *d_b, double *const *d_x, int
     std::vector<double> prev_res(D.h_lane.size(), INFINITY);
     last_refinements_ = 0;
     for (int attempt = 0;; ++attempt) {
-        // r = b - A x (FP64); z = M r; p = z; gamma = r.z
-        bk::launch_residual64(D.B, D.b.data(), D.x.data(), D.r.data(), 0, D.rr.data(), stream_);
+        // r = b - A x (FP64); z = M r; p = z; gamma = r.z; the PCG runs on the
+        // correction (x = 0), folded into the FP64 solution after the attempt
+        bk::launch_residual64(D.B, D.b.data(), D.xt.data(), D.r.data(), 0, D.rr.data(), stream_);
         precond(1);
         bk::launch_copy_pairs(D.B, D.p.data(), D.z.data(), stream_);
         while (launched < max_iter) {
@@ -600,7 +603,8 @@ void BatchSolver::solve_device(const double *const *d_b, double *const *d_x, int
             if (std::all_of(D.h_done.begin(), D.h_done.end(), [](int v) { return v != 0; })) break;
         }
         // true residuals (FP64), per lane
-        bk::launch_residual64(D.B, D.b.data(), D.x.data(), nullptr, 1, D.rr.data(), stream_);
+        bk::launch_fold(D.B, D.xt.data(), D.x.data(), stream_);
+        bk::launch_residual64(D.B, D.b.data(), D.xt.data(), nullptr, 1, D.rr.data(), stream_);
         LSS_CUDA(cudaMemcpyAsync(D.h_rr.data(), D.rr.data(), D.h_rr.size() * 8, cudaMemcpyDeviceToHost, stream_));
         LSS_CUDA(cudaMemcpyAsync(D.h_lane.data(), D.lane.data(), D.h_lane.size() * sizeof(BatchLane),
                                  cudaMemcpyDeviceToHost, stream_));
@@ -639,10 +643,10 @@ void BatchSolver::solve_device(const double *const *d_b, double *const *d_x, int
                                  stream_));
     }
     // x -> user vectors (x = 0 where b = 0)
-    bk::launch_zero_done_lanes(D.B, D.x.data(), stream_);
+    bk::launch_zero_done_lanes(D.B, D.xt.data(), stream_);
     for (int32_t s = 0; s < ns; ++s) tab[s].dst = d_x[s];
     D.scat.upload(tab, stream_);
-    bk::launch_from_batch(D.scat.data(), ns, D.scat_prefix.data(), prefix[ns], D.x.data(), D.lane.data(), stream_);
+    bk::launch_from_batch(D.scat.data(), ns, D.scat_prefix.data(), prefix[ns], D.xt.data(), stream_);
     LSS_CUDA(cudaStreamSynchronize(stream_));
     last_iters_.assign((size_t)ns * BK, 0);
     for (size_t q = 0; q < last_iters_.size(); ++q) last_iters_[q] = D.h_lane[q].iter;

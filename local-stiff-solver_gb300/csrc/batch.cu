@@ -257,11 +257,11 @@ __global__ void __launch_bounds__(256) copy_pairs_kernel(BatchDev B, float2 *__r
 
 // ---------------------------------------------------------------- true residual (FP64)
 
-// r = b - A x in FP64 (values FP64, x from its pairs), rr per lane; mode 0:
-// the start of a solve or a restart (r also replaces the recurrence residual,
-// bb recorded when first), mode 1: the final check (rr only, into L.rr)
+// r = b - A x in FP64 (values and x FP64), rr per lane; mode 0: the start of
+// a solve or a restart (r also replaces the recurrence residual), mode 1: the
+// final check (rr only)
 __global__ void __launch_bounds__(256) residual64_kernel(BatchDev B, const double *__restrict__ bvec,
-                                                         const float2 *__restrict__ x, float2 *__restrict__ r,
+                                                         const double *__restrict__ x, float2 *__restrict__ r,
                                                          int mode, double *__restrict__ out_rr)
 {
     const Chunk ch = chunk_of(B, blockIdx.x);
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(256) residual64_kernel(BatchDev B, const doubl
             const int32_t J = B.cols[b + l];
             double xv[BD];
 #pragma unroll
-            for (int c = 0; c < BD; ++c) xv[c] = df_val(x[((int64_t)J * BD + c) * BK + k]);
+            for (int c = 0; c < BD; ++c) xv[c] = x[((int64_t)J * BD + c) * BK + k];
 #pragma unroll
             for (int rr = 0; rr < BD; ++rr)
 #pragma unroll
@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(256) stiff_apply_kernel(StiffDev S, const doub
 // dst[(perm[i] * BD + c) * BK + k] = src_s[k * n_s + i * BD + c] for every system
 
 __global__ void to_batch_kernel(const ScatterSys *__restrict__ sys, int nsys, const int64_t *__restrict__ prefix,
-                                double *__restrict__ bvec, float2 *__restrict__ xpair)
+                                double *__restrict__ bvec)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= prefix[nsys]) return;
@@ -671,12 +671,11 @@ __global__ void to_batch_kernel(const ScatterSys *__restrict__ sys, int nsys, co
     const int64_t q = e % n;
     const int64_t blk = q / BD, c = q % BD;
     const int64_t dst = (((int64_t)S.row0 + S.perm[blk]) * BD + c) * BK + k;
-    if (bvec) bvec[dst] = S.src[e];
-    else xpair[dst] = df_from(S.src[e]);
+    bvec[dst] = S.src[e];
 }
 
 __global__ void from_batch_kernel(const ScatterSys *__restrict__ sys, int nsys, const int64_t *__restrict__ prefix,
-                                  const float2 *__restrict__ xpair)
+                                  const double *__restrict__ xv)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= prefix[nsys]) return;
@@ -692,7 +691,7 @@ __global__ void from_batch_kernel(const ScatterSys *__restrict__ sys, int nsys, 
     const int k = (int)(e / n);
     const int64_t q = e % n;
     const int64_t blk = q / BD, c = q % BD;
-    S.dst[e] = df_val(xpair[(((int64_t)S.row0 + S.perm[blk]) * BD + c) * BK + k]);
+    S.dst[e] = xv[(((int64_t)S.row0 + S.perm[blk]) * BD + c) * BK + k];
 }
 
 // bb per lane
@@ -713,14 +712,25 @@ __global__ void __launch_bounds__(256) lane_norms_kernel(BatchDev B, const doubl
     if (sys_finish<1>(B, blockIdx.x, ch.sys, part, tot)) out[ch.sys * BK + threadIdx.x] = tot[0];
 }
 
-__global__ void __launch_bounds__(256) zero_done_lanes_kernel(BatchDev B, float2 *__restrict__ x)
+__global__ void __launch_bounds__(256) zero_done_lanes_kernel(BatchDev B, double *__restrict__ x)
 {
     const Chunk ch = chunk_of(B, blockIdx.x);
     const int k = threadIdx.x & (BK - 1);
     const BatchLane &L = B.lane[ch.sys * BK + k];
     if (L.bb > 0.0) return;
     const int64_t e1 = (int64_t)ch.r1 * BD * BK;
-    for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x) x[e] = make_float2(0.f, 0.f);
+    for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x) x[e] = 0.0;
+}
+
+// xt += x (the pair correction of the attempt, in FP64); x = 0
+__global__ void __launch_bounds__(256) fold_kernel(BatchDev B, double *__restrict__ xt, float2 *__restrict__ x)
+{
+    const Chunk ch = chunk_of(B, blockIdx.x);
+    const int64_t e1 = (int64_t)ch.r1 * BD * BK;
+    for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x) {
+        xt[e] += df_val(x[e]);
+        x[e] = make_float2(0.f, 0.f);
+    }
 }
 
 }  // namespace bk
@@ -751,7 +761,7 @@ void launch_copy_pairs(const BatchDev &B, float2 *dst, const float2 *src, cudaSt
     LSS_LAUNCH_CHECK();
 }
 
-void launch_residual64(const BatchDev &B, const double *b, const float2 *x, float2 *r, int mode, double *rr,
+void launch_residual64(const BatchDev &B, const double *b, const double *x, float2 *r, int mode, double *rr,
                        cudaStream_t s)
 {
     residual64_kernel<<<B.nchunk, 256, 0, s>>>(B, b, x, r, mode, rr);
@@ -829,26 +839,31 @@ void launch_stiff(const BatchDev &B, const StiffDev &S, const float2 *r, const f
     LSS_LAUNCH_CHECK();
 }
 
-void launch_to_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, double *bvec,
-                     float2 *xpair, cudaStream_t s)
+void launch_to_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, double *dst,
+                     cudaStream_t s)
 {
     if (total == 0) return;
-    to_batch_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sys, nsys, prefix, bvec, xpair);
+    to_batch_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sys, nsys, prefix, dst);
     LSS_LAUNCH_CHECK();
 }
 
-void launch_from_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, const float2 *xpair,
-                       const BatchLane *lanes, cudaStream_t s)
+void launch_from_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, const double *src,
+                       cudaStream_t s)
 {
-    (void)lanes;
     if (total == 0) return;
-    from_batch_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sys, nsys, prefix, xpair);
+    from_batch_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sys, nsys, prefix, src);
     LSS_LAUNCH_CHECK();
 }
 
-void launch_zero_done_lanes(const BatchDev &B, float2 *x, cudaStream_t s)
+void launch_zero_done_lanes(const BatchDev &B, double *x, cudaStream_t s)
 {
     zero_done_lanes_kernel<<<B.nchunk, 256, 0, s>>>(B, x);
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_fold(const BatchDev &B, double *xt, float2 *x, cudaStream_t s)
+{
+    fold_kernel<<<B.nchunk, 256, 0, s>>>(B, xt, x);
     LSS_LAUNCH_CHECK();
 }
 

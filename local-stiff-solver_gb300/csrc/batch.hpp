@@ -6,7 +6,10 @@
 // GPUHybrid.cu:342-399, PCG :1413-1512); a batch runs exactly that PCG for
 // every (system, right-hand side) lane -- its own alpha, beta, gamma and
 // stopping test -- but the operator, the MAS inverses and the stiff factors
-// of a system are read once per iteration for all BK right-hand sides.
+// of a system are read once per iteration for all BK right-hand sides.  The
+// iterations run on a correction in double-float; the solution accumulates in
+// FP64 at every restart, where the residual b - A x is recomputed in FP64
+// (iterative refinement), so the attainable accuracy is FP64's.
 //
 // The systems are factorized one by one (each keeps its own selection,
 // partition, MAS hierarchy, damping and stiff factor) and then merged into one
@@ -87,9 +90,11 @@ void launch_spmm_alpha(const BatchDev &B, const float2 *p, float2 *ap, cudaStrea
 void launch_update_xr(const BatchDev &B, float2 *x, float2 *r, const float2 *p, const float2 *ap, cudaStream_t s);
 void launch_update_p(const BatchDev &B, float2 *p, const float2 *z, cudaStream_t s);
 void launch_copy_pairs(const BatchDev &B, float2 *dst, const float2 *src, cudaStream_t s);
-// mode 0: r = b - A x (and rr); mode 1: rr only
-void launch_residual64(const BatchDev &B, const double *b, const float2 *x, float2 *r, int mode, double *rr,
+// mode 0: r = b - A x (and rr); mode 1: rr only; x in FP64
+void launch_residual64(const BatchDev &B, const double *b, const double *x, float2 *r, int mode, double *rr,
                        cudaStream_t s);
+// xt += x (pairs), x = 0
+void launch_fold(const BatchDev &B, double *xt, float2 *x, cudaStream_t s);
 void launch_lane_norms(const BatchDev &B, const double *b, double *bb, cudaStream_t s);
 // z = omega M x (acc: z += ...); x as pairs (xin_pair) or FP32 (xin32); dot 1 / 2: gamma (and beta) = r.z
 void launch_mas(const BatchDev &B, const BatchMas &M, const float2 *xin_pair, const float *xin32, float2 *z, bool acc,
@@ -98,12 +103,13 @@ void launch_residual32(const BatchDev &B, const float2 *r, const float2 *z, floa
 // t = r_S - (A z)_S over every stiff DOF; z_S += Inv t over the dense subdomains
 void launch_stiff(const BatchDev &B, const StiffDev &S, const float2 *r, const float2 *z_in, double *t, float2 *z,
                   cudaStream_t s);
-void launch_to_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, double *bvec,
-                     float2 *xpair, cudaStream_t s);
-void launch_from_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, const float2 *xpair,
-                       const BatchLane *lanes, cudaStream_t s);
+// user column-major vectors (src) -> [row][BK] FP64 (dst), and back (dst of the table)
+void launch_to_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, double *dst,
+                     cudaStream_t s);
+void launch_from_batch(const ScatterSys *sys, int nsys, const int64_t *prefix, int64_t total, const double *src,
+                       cudaStream_t s);
 // x = 0 for the lanes with a zero right-hand side (GPUHybrid.cu:1428-1439)
-void launch_zero_done_lanes(const BatchDev &B, float2 *x, cudaStream_t s);
+void launch_zero_done_lanes(const BatchDev &B, double *x, cudaStream_t s);
 }  // namespace bk
 
 class BatchSolver {
