@@ -740,7 +740,7 @@ def batched_measure(seed, local, count, nrhs, steps, warmup, sequential=True):
         batch.factorize_device(vptr)
         return batch.solve_device(bptr, xptr)
 
-    def sequential(solvers):
+    def run_sequential(solvers):
         its = []
         for si, s in enumerate(solvers):
             s.factorize_device(vptr[si])
@@ -788,18 +788,18 @@ def batched_measure(seed, local, count, nrhs, steps, warmup, sequential=True):
            "gpu_launches": int(launches) if launches > 0 else None,
            "dtype": "f64 lane scalars and final residual, df32 vectors and A.p, f32 MAS, f64 stiff factor"}
     if sequential:
-        sequential(s_mixed)  # warm-up of the single-system graphs
+        run_sequential(s_mixed)  # warm-up of the single-system graphs
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        its_sm = sequential(s_mixed)
+        its_sm = run_sequential(s_mixed)
         torch.cuda.synchronize()
         wall_sm = time.perf_counter() - t2
         del batch
         s_plain = make("fp64")
-        sequential(s_plain[:1])
+        run_sequential(s_plain[:1])
         torch.cuda.synchronize()
         t3 = time.perf_counter()
-        its_p = sequential(s_plain)
+        its_p = run_sequential(s_plain)
         torch.cuda.synchronize()
         wall_p = time.perf_counter() - t3
         out.update({"sequential_mixed_ms": 1e3 * wall_sm, "batched_speedup_vs_sequential_mixed": wall_sm / wall_m,
