@@ -221,7 +221,7 @@ void BatchSolver::merge()
     D.counters.resize(ns);
     D.counters.zero(st);
     D.lane.resize((size_t)ns * BK);
-    D.sys_done.resize(ns);
+    D.sys_done.resize((size_t)ns + 1);  // + the kernels' error status
     D.rr.resize((size_t)ns * BK);
 
     // ---- MAS: levels padded to whole banks per system
@@ -471,6 +471,7 @@ void BatchSolver::merge()
     B.omega = D.omega.data();
     B.lane = D.lane.data();
     B.sys_done = D.sys_done.data();
+    B.err = D.sys_done.data() + ns;
     B.partials = D.partials.data();
     B.counters = D.counters.data();
     // scatter table of the user vectors
@@ -558,7 +559,7 @@ void BatchSolver::solve_device(const double *const *d_b, double *const *d_x, int
     LSS_CUDA(cudaMemcpyAsync(D.h_rr.data(), D.rr.data(), D.h_rr.size() * 8, cudaMemcpyDeviceToHost, stream_));
     LSS_CUDA(cudaStreamSynchronize(stream_));
     D.h_lane.assign((size_t)ns * BK, BatchLane{});
-    D.h_done.assign(ns, 0);
+    D.h_done.assign((size_t)ns + 1, 0);  // [ns]: error status
     for (int32_t s = 0; s < ns; ++s) {
         const Params &P = sys_[s]->p_;
         int all = 1;
@@ -576,7 +577,9 @@ void BatchSolver::solve_device(const double *const *d_b, double *const *d_x, int
     }
     LSS_CUDA(cudaMemcpyAsync(D.lane.data(), D.h_lane.data(), D.h_lane.size() * sizeof(BatchLane),
                              cudaMemcpyHostToDevice, stream_));
-    LSS_CUDA(cudaMemcpyAsync(D.sys_done.data(), D.h_done.data(), ns * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    LSS_CUDA(cudaMemcpyAsync(D.sys_done.data(), D.h_done.data(), (ns + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                             stream_));
+    D.counters.zero(stream_);
     std::vector<double> target(D.h_lane.size());
     for (size_t q = 0; q < target.size(); ++q) target[q] = D.h_lane[q].rel_eps;
     int launched = 0;
@@ -597,10 +600,12 @@ void BatchSolver::solve_device(const double *const *d_b, double *const *d_x, int
             const int chunk = std::min(P0.check_every, max_iter - launched);
             launch_chunk(chunk);
             launched += chunk;
-            LSS_CUDA(cudaMemcpyAsync(D.h_done.data(), D.sys_done.data(), ns * sizeof(int), cudaMemcpyDeviceToHost,
-                                     stream_));
+            LSS_CUDA(cudaMemcpyAsync(D.h_done.data(), D.sys_done.data(), (ns + 1) * sizeof(int),
+                                     cudaMemcpyDeviceToHost, stream_));
             LSS_CUDA(cudaStreamSynchronize(stream_));
-            if (std::all_of(D.h_done.begin(), D.h_done.end(), [](int v) { return v != 0; })) break;
+            if (D.h_done[ns] != 0)
+                fail(LSS_ERR_INTERNAL, "batched MAS: a bulk copy into shared memory did not complete");
+            if (std::all_of(D.h_done.begin(), D.h_done.begin() + ns, [](int v) { return v != 0; })) break;
         }
         // true residuals (FP64), per lane
         bk::launch_fold(D.B, D.xt.data(), D.x.data(), stream_);

@@ -19,6 +19,7 @@
 #include <cfloat>
 
 #include "batch.hpp"
+#include "bulk.cuh"
 #include "device_common.cuh"
 #include "spmv.cuh"
 
@@ -306,134 +307,249 @@ __global__ void __launch_bounds__(256) residual64_kernel(BatchDev B, const doubl
 
 // Level vectors: item-major, [(item * BD + c) * BK + k].
 
+// Segment sums of one bank (cnt <= 32 items of BD x BK values each, item j
+// contributing to aggregate key[j] < ncc) into out[a * BD * BK ...], one warp:
+// lane e owns the values e and e + 32 of the BD * BK = 48 of an item; the
+// per-aggregate sums collect in the warp's shared rows acc[a][48].
+template <typename XT>
+__device__ __forceinline__ void bank_restrict(const XT *__restrict__ x, const uint8_t *__restrict__ key, int cnt,
+                                              int ncc, float *__restrict__ out, float *__restrict__ acc, int lane)
+{
+    constexpr int W = BD * BK;  // 48
+    for (int q = lane; q < ncc * W; q += 32) acc[q] = 0.f;
+    __syncwarp();
+    for (int j = 0; j < cnt; ++j) {
+        const int a = key[j];
+        const XT *xj = x + (int64_t)j * W;
+        float v0, v1 = 0.f;
+        if constexpr (sizeof(XT) == 8) {
+            v0 = reinterpret_cast<const float2 *>(xj)[lane].x;
+            if (lane < W - 32) v1 = reinterpret_cast<const float2 *>(xj)[lane + 32].x;
+        } else {
+            v0 = (float)xj[lane];
+            if (lane < W - 32) v1 = (float)xj[lane + 32];
+        }
+        acc[a * W + lane] += v0;
+        if (lane < W - 32) acc[a * W + lane + 32] += v1;
+    }
+    __syncwarp();
+    for (int q = lane; q < ncc * W; q += 32) out[q] = acc[q];
+    __syncwarp();
+}
+
 // level 0 -> 1: per part, the sums of its nodes' entries per level-1 aggregate
-// (warp per part; lane k of half h takes the components c = h, h + 2)
+// (warp per part, eight warps per CTA = the chunk's parts)
 template <typename XT>
 __global__ void __launch_bounds__(256) restrict0_kernel(BatchDev B, MasDev m, const XT *__restrict__ xin,
                                                         float *__restrict__ v)
 {
+    __shared__ float acc_all[8][32 * BD * BK];
     const Chunk ch = chunk_of(B, blockIdx.x);
     if (B.sys_done[ch.sys]) return;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = lane >> 4, k = lane & 15;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     float *v1 = v + m.voff[1] * BK;
-    for (int32_t p = ch.p0 + w; p < ch.p1; p += 8) {
-        const int32_t lo = m.part_off[p], cnt = m.part_off[p + 1] - lo;
-        const int ncc = m.ccnt0[p];
-        const int32_t base = m.cbase0[p];
-        for (int a = 0; a < ncc; ++a)
-            for (int c = h; c < BD; c += 2) {
-                float acc = 0.f;
-                for (int j = 0; j < cnt; ++j)
-                    if (m.key0[lo + j] == a) {
-                        const XT xv = xin[((int64_t)(lo + j) * BD + c) * BK + k];
-                        if constexpr (sizeof(XT) == 8) acc += reinterpret_cast<const float2 &>(xv).x;
-                        else acc += (float)xv;
-                    }
-                v1[((int64_t)(base + a) * BD + c) * BK + k] = acc;
-            }
-    }
+    const int32_t p = ch.p0 + w;
+    if (p >= ch.p1) return;
+    const int ncc = m.ccnt0[p];
+    if (ncc == 0) return;
+    const int32_t lo = m.part_off[p], cnt = m.part_off[p + 1] - lo;
+    bank_restrict<XT>(xin + (int64_t)lo * BD * BK, m.key0 + lo, cnt, ncc, v1 + (int64_t)m.cbase0[p] * BD * BK,
+                      acc_all[w], lane);
 }
 
 // level l -> l + 1 (warp per level-l bank)
 __global__ void __launch_bounds__(256) restrict_kernel(MasDev m, int l, float *__restrict__ v)
 {
-    const int lane = threadIdx.x & 31, h = lane >> 4, k = lane & 15;
-    const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    __shared__ float acc_all[8][32 * BD * BK];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t g = (int64_t)blockIdx.x * 8 + w;
     if (g >= m.nbanks[l]) return;
-    const float *vl = v + m.voff[l] * BK;
-    float *vn = v + m.voff[l + 1] * BK;
     const int ncc = m.ccnt[l][g];
-    const int32_t base = m.cbase[l][g];
-    const uint8_t *key = m.key[l] + g * 32;
-    for (int a = 0; a < ncc; ++a)
-        for (int c = h; c < BD; c += 2) {
-            float acc = 0.f;
-            for (int j = 0; j < 32; ++j)
-                if (key[j] == a) acc += vl[((g * 32 + j) * BD + c) * BK + k];
-            vn[((int64_t)(base + a) * BD + c) * BK + k] = acc;
-        }
+    if (ncc == 0) return;
+    bank_restrict<float>(v + (m.voff[l] + g * 32 * BD) * BK, m.key[l] + g * 32, 32, ncc,
+                         v + (m.voff[l + 1] + (int64_t)m.cbase[l][g] * BD) * BK, acc_all[w], lane);
 }
 
-// Y (96 x BK) = Inv (96 x 96, circulant tiles) X (96 x BK) for one bank, one
-// warp: the bank's tiles are expanded into the full symmetric matrix in shared
-// memory (column j contiguous), X is staged there too, and lane (g, h)
-// accumulates rows 12g .. 12g + 11 for the right-hand sides 4h .. 4h + 3:
-// per column j one float4 of X and three float4 of Inv feed 48 FMAs.
-// Bank index = c * 32 + lane (component-major), as in the single-system MAS.
-constexpr int NB = 32 * BD;  // 96
-constexpr int MAS_SMEM_FLOATS = NB * NB + NB * BK;
+// Y (96 x BK) = Inv (96 x 96) X (96 x BK) for a sequence of banks, one CTA of
+// four warps per sequence.  Per bank, the copy engine brings the inverse's
+// 147 stored diagonals (the tiles (c, c2 >= c) of mas_tile_elems, 18,816
+// bytes) and the bank's X block into shared memory (cp.async.bulk, double
+// buffered: bank i + 1 arrives while bank i computes); the CTA expands the
+// diagonals into the full 96 x 96 matrix S (column-major, rows and columns in
+// node-major order q = 3 node + component, the order of X) and multiplies:
+// warp w takes the right-hand sides 8 (w & 1) .. + 7 and the columns
+// 48 (w >> 1) .. + 47, lane (g, h) the rows 12 g .. 12 g + 11 and the
+// right-hand sides 8 (w & 1) + 2 h, + 1 -- per column three float4 of S, one
+// vector load of X, 24 FMAs.  The two column halves meet in shared memory.
+constexpr int NB = 32 * BD;                          // 96
+constexpr int TILE_FLOATS = 3 * 17 * 32 + 3 * 32 * 32;  // 4704 (mas_tile_elems(3))
+constexpr int TILE_BYTES = TILE_FLOATS * 4;          // 18,816
+constexpr int RSTRIDE = NB * BK + 64;                // partial sums of one column half (+ skew)
+constexpr int XBUF_BYTES = 2 * RSTRIDE * 4;          // >= 32 x 48 pairs (12,288) and both halves (12,800)
+constexpr int BANK_SMEM = NB * NB * 4 + 2 * TILE_BYTES + 2 * XBUF_BYTES + 16;
+static_assert(XBUF_BYTES >= 32 * BD * BK * 8, "X staging holds 32 nodes of pairs");
 
-__device__ __forceinline__ void bank_gemm(const float *__restrict__ tiles, float *__restrict__ S,
-                                          const float *__restrict__ X, int lane, float (&y)[12][4])
+struct BankSmem {
+    float *S, *T, *X;  // S: 96 x 96; T: 2 tile buffers; X: 2 X / partial-sum buffers (bytes XBUF_BYTES each)
+    uint64_t *bar;
+};
+
+__device__ __forceinline__ BankSmem bank_smem(unsigned char *raw)
 {
-    // expand: tile (c, c2 >= c), element [d][r] = Inv[c*32 + r][c2*32 + (r+d) % 32]
-    const float *t = tiles;
-    for (int c = 0; c < BD; ++c)
-        for (int c2 = c; c2 < BD; ++c2) {
-            const int nd = (c == c2) ? 17 : 32;
-            for (int d = 0; d < nd; ++d) {
-                const float a = __ldcs(t + d * 32 + lane);
-                const int i = c * 32 + lane, j = c2 * 32 + ((lane + d) & 31);
-                S[j * NB + i] = a;
-                S[i * NB + j] = a;
-            }
-            t += nd * 32;
-        }
-    __syncwarp();
-    const int g = lane >> 2, hq = lane & 3;
+    BankSmem b;
+    b.S = reinterpret_cast<float *>(raw);
+    b.T = b.S + NB * NB;
+    b.X = b.T + 2 * TILE_FLOATS;
+    b.bar = reinterpret_cast<uint64_t *>(reinterpret_cast<unsigned char *>(b.X) + 2 * XBUF_BYTES);
+    return b;
+}
+
+// stored diagonal D (0..146) -> tile (c, c2) and diagonal d
+__device__ __forceinline__ void diag_of(int D, int &c, int &c2, int &d)
+{
+    if (D < 81) {
+        c = 0;
+        if (D < 17) { c2 = 0; d = D; }
+        else { c2 = 1 + (D - 17) / 32; d = (D - 17) % 32; }
+    } else if (D < 130) {
+        c = 1;
+        if (D < 98) { c2 = 1; d = D - 81; }
+        else { c2 = 2; d = D - 98; }
+    } else {
+        c = 2; c2 = 2; d = D - 130;
+    }
+}
+
+// tile diagonals (shared) -> S[col * 96 + row]; warp w takes diagonals w, w + 4, ...
+// Diagonal tile, d = 16: entry [r][r + 16] belongs to row r only (row r + 16
+// has its own stored value), as in the single-system MAS.
+__device__ __forceinline__ void expand_tile(const float *__restrict__ T, float *__restrict__ S, int w, int lane)
+{
+    for (int D = w; D < 147; D += 4) {
+        int c, c2, d;
+        diag_of(D, c, c2, d);
+        const float a = T[D * 32 + lane];
+        const int qi = 3 * lane + c, qj = 3 * ((lane + d) & 31) + c2;
+        S[qj * NB + qi] = a;
+        if (c != c2 || (d != 0 && d != 16)) S[qi * NB + qj] = a;
+    }
+}
+
+template <typename XT>
+__device__ __forceinline__ void bank_mma(const float *__restrict__ S, const float *__restrict__ X, int ncol, int w,
+                                         int lane, float (&acc)[12][2])
+{
+    const int rh = w & 1, kh = w >> 1, g = lane >> 2, h = lane & 3;
 #pragma unroll
-    for (int q = 0; q < 12; ++q)
-#pragma unroll
-        for (int s = 0; s < 4; ++s) y[q][s] = 0.f;
+    for (int j = 0; j < 12; ++j) acc[j][0] = acc[j][1] = 0.f;
+    const int q0 = 48 * kh, q1 = min(q0 + 48, ncol);
+    const int xo = 8 * rh + 2 * h;
 #pragma unroll 4
-    for (int j = 0; j < NB; ++j) {
-        const float4 xv = *reinterpret_cast<const float4 *>(X + j * BK + 4 * hq);
-        const float4 *col = reinterpret_cast<const float4 *>(S + j * NB + 12 * g);
-        float a[12];
+    for (int q = q0; q < q1; ++q) {
+        const float4 *col = reinterpret_cast<const float4 *>(S + q * NB + 12 * g);
         const float4 a0 = col[0], a1 = col[1], a2 = col[2];
-        a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w;
-        a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
-        a[8] = a2.x; a[9] = a2.y; a[10] = a2.z; a[11] = a2.w;
+        float x0, x1;
+        if constexpr (sizeof(XT) == 8) {
+            const float4 xv = *reinterpret_cast<const float4 *>(X + 2 * (q * BK + xo));
+            x0 = xv.x;
+            x1 = xv.z;
+        } else {
+            const float2 xv = *reinterpret_cast<const float2 *>(X + q * BK + xo);
+            x0 = xv.x;
+            x1 = xv.y;
+        }
+        const float a[12] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
 #pragma unroll
-        for (int q = 0; q < 12; ++q) {
-            y[q][0] += a[q] * xv.x;
-            y[q][1] += a[q] * xv.y;
-            y[q][2] += a[q] * xv.z;
-            y[q][3] += a[q] * xv.w;
+        for (int j = 0; j < 12; ++j) {
+            acc[j][0] = fmaf(a[j], x0, acc[j][0]);
+            acc[j][1] = fmaf(a[j], x1, acc[j][1]);
         }
     }
 }
 
-// coarse banks: u = Inv_l v (level by level, all levels in one launch)
-__global__ void __launch_bounds__(32) symv_coarse_kernel(MasDev m, const float *__restrict__ invc,
-                                                         const float *__restrict__ v, float *__restrict__ u)
+// partial sums -> R[kh][row][k] (skewed by 8 per row group of 12), R in the X buffer
+__device__ __forceinline__ void bank_store_partials(float *__restrict__ R, int w, int lane, const float (&acc)[12][2])
 {
-    extern __shared__ float sm[];
-    float *S = sm, *X = sm + NB * NB;
-    const int lane = threadIdx.x;
-    for (int64_t gb = blockIdx.x; gb < m.ncoarse; gb += gridDim.x) {
-        int l = 1;
-        while (l + 1 < m.L && gb >= m.boff[l + 1]) ++l;
-        const int64_t b = gb - m.boff[l];
-        const float *vb = v + (m.voff[l] + b * 32 * BD) * BK;
-        // X[c*32 + r][k] = v[((b*32 + r) * BD + c) * BK + k]
-        for (int e = lane; e < NB * BK; e += 32) {
-            const int i = e / BK, kk = e % BK, c = i / 32, r = i % 32;
-            X[e] = vb[((int64_t)r * BD + c) * BK + kk];
-        }
-        __syncwarp();
-        float y[12][4];
-        bank_gemm(invc + gb * m.tile_elems, S, X, lane, y);
-        float *ub = u + (m.voff[l] + b * 32 * BD) * BK;
-        const int g = lane >> 2, hq = lane & 3;
+    const int rh = w & 1, kh = w >> 1, g = lane >> 2, h = lane & 3;
 #pragma unroll
-        for (int q = 0; q < 12; ++q) {
-            const int i = 12 * g + q, c = i / 32, r = i % 32;
-            *reinterpret_cast<float4 *>(ub + ((int64_t)r * BD + c) * BK + 4 * hq) =
-                make_float4(y[q][0], y[q][1], y[q][2], y[q][3]);
-        }
-        __syncwarp();
+    for (int j = 0; j < 12; ++j) {
+        const int row = 12 * g + j;
+        *reinterpret_cast<float2 *>(R + kh * RSTRIDE + row * BK + 8 * g + 8 * rh + 2 * h) =
+            make_float2(acc[j][0], acc[j][1]);
     }
+}
+
+__device__ __forceinline__ float bank_result(const float *__restrict__ R, int row, int k)
+{
+    const int o = row * BK + 8 * (row / 12) + k;
+    return R[o] + R[RSTRIDE + o];
+}
+
+// The bank pipeline of one CTA: jobs 0 .. nj - 1, job(i, tile, x, xbytes, cnt)
+// names the bank's inverse, its X block and item count, epi(i, R, cnt) consumes
+// the result rows 0 .. 3 cnt - 1 (R as bank_result reads it).  Returns false,
+// with *err set, when a copy did not arrive within the poll limit.
+template <typename XT, typename Job, typename Epi>
+__device__ bool bank_pipeline(unsigned char *raw, int nj, Job job, Epi epi, int *err)
+{
+    const BankSmem sm = bank_smem(raw);
+    __shared__ int s_fail;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    auto issue = [&](int i, int b) {
+        const float *tile;
+        const XT *x;
+        int cnt;
+        job(i, tile, x, cnt);
+        const uint32_t xbytes = (uint32_t)cnt * BD * BK * sizeof(XT);
+        mbar_arrive_expect_tx(sm.bar + b, TILE_BYTES + xbytes);
+        bulk_load(sm.T + b * TILE_FLOATS, tile, TILE_BYTES, sm.bar + b);
+        bulk_load(reinterpret_cast<unsigned char *>(sm.X) + b * XBUF_BYTES, x, xbytes, sm.bar + b);
+    };
+    if (t == 0) {
+        mbar_init(sm.bar, 1);
+        mbar_init(sm.bar + 1, 1);
+        mbar_init_fence();
+        s_fail = 0;
+    }
+    __syncthreads();
+    if (t == 0) {
+        issue(0, 0);
+        if (nj > 1) issue(1, 1);
+    }
+    for (int i = 0; i < nj; ++i) {
+        const int b = i & 1;
+        if (t == 0 && !mbar_wait_bounded(sm.bar + b, (i >> 1) & 1)) s_fail = 1;
+        __syncthreads();
+        if (s_fail) {
+            if (t == 0) {
+                atomicExch(err, 1);
+                // let the copies in flight land before the CTA's shared memory goes
+                mbar_wait_bounded(sm.bar + b, (i >> 1) & 1);
+                if (i + 1 < nj) mbar_wait_bounded(sm.bar + (b ^ 1), ((i + 1) >> 1) & 1);
+            }
+            return false;
+        }
+        if (t != 0) (void)mbar_test(sm.bar + b, (i >> 1) & 1);  // acquire the completed phase in every thread
+        const float *tile;
+        const XT *xsrc;
+        int cnt;
+        job(i, tile, xsrc, cnt);
+        float *X = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(sm.X) + b * XBUF_BYTES);
+        expand_tile(sm.T + b * TILE_FLOATS, sm.S, w, lane);
+        __syncthreads();
+        float acc[12][2];
+        bank_mma<XT>(sm.S, X, 3 * cnt, w, lane, acc);
+        __syncthreads();
+        bank_store_partials(X, w, lane, acc);
+        __syncthreads();
+        epi(i, X, cnt);
+        __syncthreads();
+        if (t == 0 && i + 2 < nj) {
+            proxy_async_fence();
+            issue(i + 2, b);
+        }
+    }
+    return true;
 }
 
 // u_1 += P (u_2 + P (u_3 + ...)) for every level-1 item, stopping where a
@@ -459,72 +575,85 @@ __global__ void __launch_bounds__(256) prolong_kernel(MasDev m, float *__restric
     u[(m.voff[1] + item1 * BD) * BK + rest] = acc;
 }
 
+// coarse banks: u = Inv_l v, all levels in one launch (banks grid-strided)
+__global__ void __launch_bounds__(128) symv_coarse_kernel(MasDev m, const float *__restrict__ invc,
+                                                          const float *__restrict__ v, float *__restrict__ u,
+                                                          int *err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int nj = (int)((m.ncoarse - blockIdx.x + gridDim.x - 1) / gridDim.x);
+    if (nj <= 0) return;
+    auto locate = [&](int i, int64_t &gb, int64_t &at) {
+        gb = blockIdx.x + (int64_t)i * gridDim.x;
+        int l = 1;
+        while (l + 1 < m.L && gb >= m.boff[l + 1]) ++l;
+        at = (m.voff[l] + (gb - m.boff[l]) * 32 * BD) * BK;
+    };
+    auto job = [&](int i, const float *&tile, const float *&x, int &cnt) {
+        int64_t gb, at;
+        locate(i, gb, at);
+        tile = invc + gb * TILE_FLOATS;
+        x = v + at;
+        cnt = 32;
+    };
+    auto epi = [&](int i, const float *R, int) {
+        int64_t gb, at;
+        locate(i, gb, at);
+        const int k = threadIdx.x & (BK - 1);
+#pragma unroll 4
+        for (int row = threadIdx.x >> 4; row < NB; row += 8) u[at + row * BK + k] = bank_result(R, row, k);
+    };
+    bank_pipeline<float>(smem_raw, nj, job, epi, err);
+}
+
 // level 0: z = omega (Inv_0 x + u_1) (+ z with acc), as pairs; optional
 // gamma = r.z per lane (dot 1: initial gamma; dot 2: beta and the new gamma).
-// One warp per partition, four warps per CTA, one CTA per chunk.
+// One CTA per chunk, its parts in sequence through the bank pipeline.
 template <typename XT, bool ACC, int DOT>
 __global__ void __launch_bounds__(128) symv0_kernel(BatchDev B, MasDev m, const float *__restrict__ inv0,
                                                     const float *__restrict__ u, const XT *__restrict__ xin,
                                                     float2 *__restrict__ z, const float2 *__restrict__ rdot)
 {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const Chunk ch = chunk_of(B, blockIdx.x);
     if (B.sys_done[ch.sys]) return;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    float *S = sm + w * MAS_SMEM_FLOATS, *X = S + NB * NB;
     const double om = B.omega[ch.sys];
     const float oh = (float)om, ol = (float)(om - (double)oh);
     const float *u1 = u + m.voff[1] * BK;
-    const int g = lane >> 2, hq = lane & 3;
-    float dh[4] = {0.f, 0.f, 0.f, 0.f}, dl[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int32_t p = ch.p0 + w; p < ch.p1; p += 4) {
-        const int32_t lo = m.part_off[p], cnt = m.part_off[p + 1] - lo;
-        for (int e = lane; e < NB * BK; e += 32) {
-            const int i = e / BK, kk = e % BK, c = i / 32, r = i % 32;
-            float xv = 0.f;
-            if (r < cnt) {
-                const XT v = xin[((int64_t)(lo + r) * BD + c) * BK + kk];
-                if constexpr (sizeof(XT) == 8) xv = reinterpret_cast<const float2 &>(v).x;
-                else xv = (float)v;
-            }
-            X[e] = xv;
-        }
-        __syncwarp();
-        float y[12][4];
-        bank_gemm(inv0 + (int64_t)p * m.tile_elems, S, X, lane, y);
-#pragma unroll
-        for (int q = 0; q < 12; ++q) {
-            const int i = 12 * g + q, c = i / 32, r = i % 32;
-            if (r >= cnt) continue;
-            const int32_t node = lo + r;
-            const int64_t e = ((int64_t)node * BD + c) * BK + 4 * hq;
-            float4 cu = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (m.L > 1 && m.ccnt0[p] > 0)
-                cu = *reinterpret_cast<const float4 *>(u1 + ((int64_t)(m.cbase0[p] + m.key0[node]) * BD + c) * BK +
-                                                       4 * hq);
-            const float s4[4] = {y[q][0] + cu.x, y[q][1] + cu.y, y[q][2] + cu.z, y[q][3] + cu.w};
-#pragma unroll
-            for (int s = 0; s < 4; ++s) {
-                float2 val = df_mul(make_float2(s4[s], 0.f), oh, ol);
-                if (ACC) val = df_sum(z[e + s], val);
-                z[e + s] = val;
-                if (DOT) {
-                    const float2 rv = rdot[e + s];
-                    df_fma(dh[s], dl[s], rv.x, rv.y, val.x, val.y);
-                }
+    const int k = threadIdx.x & (BK - 1);
+    float dh = 0.f, dl = 0.f;
+    auto job = [&](int i, const float *&tile, const XT *&x, int &cnt) {
+        const int32_t p = ch.p0 + i, lo = m.part_off[p];
+        tile = inv0 + (int64_t)p * TILE_FLOATS;
+        x = xin + (int64_t)lo * BD * BK;
+        cnt = m.part_off[p + 1] - lo;
+    };
+    auto epi = [&](int i, const float *R, int cnt) {
+        const int32_t p = ch.p0 + i, lo = m.part_off[p];
+        const bool coarse = m.L > 1 && m.ccnt0[p] > 0;
+        const int32_t cb = coarse ? m.cbase0[p] : 0;
+        for (int row = threadIdx.x >> 4; row < 3 * cnt; row += 8) {
+            const int node = row / 3, c = row - 3 * node;
+            float y = bank_result(R, row, k);
+            if (coarse) y += u1[((int64_t)(cb + m.key0[lo + node]) * BD + c) * BK + k];
+            const int64_t e = ((int64_t)lo * BD + row) * BK + k;
+            float2 val = df_mul(make_float2(y, 0.f), oh, ol);
+            if (ACC) val = df_sum(z[e], val);
+            z[e] = val;
+            if (DOT) {
+                const float2 rv = rdot[e];
+                df_fma(dh, dl, rv.x, rv.y, val.x, val.y);
             }
         }
-        __syncwarp();
-    }
+    };
+    if (!bank_pipeline<XT>(smem_raw, ch.p1 - ch.p0, job, epi, B.err)) return;
     if (DOT) {
-        __shared__ double red[4][8][BK];  // warp, row group g, rhs
-#pragma unroll
-        for (int s = 0; s < 4; ++s) red[w][g][4 * hq + s] = (double)dh[s] + (double)dl[s];
+        __shared__ double red[8][BK];
+        red[threadIdx.x >> 4][k] = (double)dh + (double)dl;
         __syncthreads();
         double part[1] = {0.0}, tot[1];
         if (threadIdx.x < BK)
-            for (int q = 0; q < 4; ++q)
-                for (int gg = 0; gg < 8; ++gg) part[0] += red[q][gg][threadIdx.x];
+            for (int q = 0; q < 8; ++q) part[0] += red[q][threadIdx.x];
         if (sys_finish<1>(B, blockIdx.x, ch.sys, part, tot)) {
             BatchLane &L = B.lane[ch.sys * BK + threadIdx.x];
             if (!L.done) {
@@ -778,21 +907,20 @@ void launch_mas(const BatchDev &B, const BatchMas &M, const float2 *xin_pair, co
                 int dot, const float2 *rdot, cudaStream_t s)
 {
     const MasDev &m = M.m;
+    if (m.tile_elems != TILE_FLOATS) fail(LSS_ERR_INTERNAL, "batched MAS: unexpected bank tile size");
+    const size_t smem = (size_t)BANK_SMEM;
     if (m.L > 1) {
         if (xin_pair) restrict0_kernel<float2><<<B.nchunk, 256, 0, s>>>(B, m, xin_pair, M.v);
         else restrict0_kernel<float><<<B.nchunk, 256, 0, s>>>(B, m, xin32, M.v);
         for (int l = 1; l + 1 < m.L; ++l)
-            if (m.nbanks[l] > 0)
-                restrict_kernel<<<(unsigned)(((int64_t)m.nbanks[l] * 32 + 255) / 256), 256, 0, s>>>(m, l, M.v);
-        const size_t smem = (size_t)MAS_SMEM_FLOATS * sizeof(float);
+            if (m.nbanks[l] > 0) restrict_kernel<<<(unsigned)((m.nbanks[l] + 7) / 8), 256, 0, s>>>(m, l, M.v);
         raise_smem_limit((const void *)symv_coarse_kernel, smem);
         if (m.ncoarse > 0)
-            symv_coarse_kernel<<<(unsigned)std::min<int64_t>(m.ncoarse, sm_grid(5)), 32, smem, s>>>(m, M.invc, M.v,
-                                                                                                   M.u);
+            symv_coarse_kernel<<<(unsigned)std::min<int64_t>(m.ncoarse, sm_grid(2)), 128, smem, s>>>(m, M.invc, M.v,
+                                                                                                    M.u, B.err);
         if (m.L > 2 && m.nitems[1] > 0)
             prolong_kernel<<<(unsigned)(((int64_t)m.nitems[1] * BD * BK + 255) / 256), 256, 0, s>>>(m, M.u);
     }
-    const size_t smem = (size_t)4 * MAS_SMEM_FLOATS * sizeof(float);
 #define LSS_B0(XT_, X_, A_, D_)                                                                          \
     do {                                                                                                 \
         raise_smem_limit((const void *)symv0_kernel<XT_, A_, D_>, smem);                                 \

@@ -60,6 +60,7 @@ struct BatchDev {
     const double *omega = nullptr;        // per system: damping of MAS in the multiplicative form
     BatchLane *lane = nullptr;            // nsys * BK
     const int *sys_done = nullptr;        // per system: every lane stopped
+    int *err = nullptr;                   // != 0: a bulk copy did not arrive (sys_done[nsys])
     double *partials = nullptr;           // nchunk * BK * 2
     unsigned *counters = nullptr;         // nsys
 };
