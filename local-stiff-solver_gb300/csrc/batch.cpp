@@ -444,6 +444,7 @@ void BatchSolver::merge()
             at += Q.elems;
         }
         D.front_sys.upload(front_sys, st);
+        D.mf.make_pairs(st);
     }
 
     // ---- vectors and the device view

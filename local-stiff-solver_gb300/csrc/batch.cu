@@ -119,9 +119,34 @@ __device__ void mark_system(const BatchDev &B, int sys)
 // One warp per block row: half-warp h takes the row's blocks l = h, h + 2, ...,
 // lane k of the half the right-hand side k; the 9 values of a block are
 // broadcast to the half-warp, p and A p move as 128-byte lines of 16 pairs.
+// The row's column indices are loaded once (lane l: block l) and handed out
+// by shuffles, U blocks per half-warp at a time, so that their loads are in
+// flight together.
+template <int U, typename Blk>
+__device__ __forceinline__ void row_blocks(const BatchDev &B, int32_t b, int32_t len, int lane, Blk blk)
+{
+    const int h = lane >> 4;
+    for (int32_t l0 = 0; l0 < len; l0 += 32) {
+        const int n = min(32, len - l0);
+        const int32_t cj = lane < n ? B.cols[b + l0 + lane] : 0;
+        for (int j0 = 0; j0 < n; j0 += 2 * U) {
+            int32_t J[U];
+            bool ok[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int l = j0 + 2 * u + h;
+                ok[u] = l < n;
+                J[u] = __shfl_sync(FULL, cj, l & 31);
+            }
+            blk(l0 + j0 + h, J, ok);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) spmm_alpha_kernel(BatchDev B, const float2 *__restrict__ p,
                                                          float2 *__restrict__ ap)
 {
+    constexpr int U = 2;
     const Chunk ch = chunk_of(B, blockIdx.x);
     if (B.sys_done[ch.sys]) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = lane >> 4, k = lane & 15;
@@ -130,19 +155,25 @@ __global__ void __launch_bounds__(256) spmm_alpha_kernel(BatchDev B, const float
         const int32_t b = B.rows[I], len = B.rows[I + 1] - b;
         const float2 *__restrict__ v = B.vals_df + (int64_t)b * 9;
         float sh[BD] = {0.f, 0.f, 0.f}, sl[BD] = {0.f, 0.f, 0.f};
-        for (int32_t l = h; l < len; l += 2) {
-            const int32_t J = B.cols[b + l];
-            float2 x[BD];
+        row_blocks<U>(B, b, len, lane, [&](int l, const int32_t (&J)[U], const bool (&ok)[U]) {
+            float2 x[U][BD], a[U][BD * BD];
 #pragma unroll
-            for (int c = 0; c < BD; ++c) x[c] = p[((int64_t)J * BD + c) * BK + k];
+            for (int u = 0; u < U; ++u) {
 #pragma unroll
-            for (int r = 0; r < BD; ++r)
+                for (int c = 0; c < BD; ++c)
+                    x[u][c] = ok[u] ? p[((int64_t)J[u] * BD + c) * BK + k] : make_float2(0.f, 0.f);
 #pragma unroll
-                for (int c = 0; c < BD; ++c) {
-                    const float2 a = __ldg(v + (int64_t)(r * BD + c) * len + l);
-                    df_fma(sh[r], sl[r], a.x, a.y, x[c].x, x[c].y);
-                }
-        }
+                for (int e = 0; e < BD * BD; ++e)
+                    a[u][e] = ok[u] ? __ldg(v + (int64_t)e * len + l + 2 * u) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int r = 0; r < BD; ++r)
+#pragma unroll
+                    for (int c = 0; c < BD; ++c)
+                        df_fma(sh[r], sl[r], a[u][r * BD + c].x, a[u][r * BD + c].y, x[u][c].x, x[u][c].y);
+        });
 #pragma unroll
         for (int r = 0; r < BD; ++r) {
             const float bh = __shfl_xor_sync(FULL, sh[r], 16), bl = __shfl_xor_sync(FULL, sl[r], 16);
@@ -272,16 +303,22 @@ __global__ void __launch_bounds__(256) residual64_kernel(BatchDev B, const doubl
         const int32_t b = B.rows[I], len = B.rows[I + 1] - b;
         const double *__restrict__ v = B.vals + (int64_t)b * 9;
         double y[BD] = {0.0, 0.0, 0.0};
-        for (int32_t l = h; l < len; l += 2) {
-            const int32_t J = B.cols[b + l];
-            double xv[BD];
+        row_blocks<2>(B, b, len, lane, [&](int l, const int32_t (&J)[2], const bool (&ok)[2]) {
+            double xv[2][BD], a[2][BD * BD];
 #pragma unroll
-            for (int c = 0; c < BD; ++c) xv[c] = x[((int64_t)J * BD + c) * BK + k];
+            for (int u = 0; u < 2; ++u) {
 #pragma unroll
-            for (int rr = 0; rr < BD; ++rr)
+                for (int c = 0; c < BD; ++c) xv[u][c] = ok[u] ? x[((int64_t)J[u] * BD + c) * BK + k] : 0.0;
 #pragma unroll
-                for (int c = 0; c < BD; ++c) y[rr] += __ldg(v + (int64_t)(rr * BD + c) * len + l) * xv[c];
-        }
+                for (int e = 0; e < BD * BD; ++e) a[u][e] = ok[u] ? __ldg(v + (int64_t)e * len + l + 2 * u) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+                for (int rr = 0; rr < BD; ++rr)
+#pragma unroll
+                    for (int c = 0; c < BD; ++c) y[rr] += a[u][rr * BD + c] * xv[u][c];
+        });
 #pragma unroll
         for (int rr = 0; rr < BD; ++rr) y[rr] += __shfl_xor_sync(FULL, y[rr], 16);
         if (h == 0) {
@@ -371,26 +408,31 @@ __global__ void __launch_bounds__(256) restrict_kernel(MasDev m, int l, float *_
 }
 
 // Y (96 x BK) = Inv (96 x 96) X (96 x BK) for a sequence of banks, one CTA of
-// four warps per sequence.  Per bank, the copy engine brings the inverse's
+// eight warps per sequence.  Per bank, the copy engine brings the inverse's
 // 147 stored diagonals (the tiles (c, c2 >= c) of mas_tile_elems, 18,816
-// bytes) and the bank's X block into shared memory (cp.async.bulk, double
-// buffered: bank i + 1 arrives while bank i computes); the CTA expands the
+// bytes) and the bank's X block into a shared-memory stage (cp.async.bulk,
+// two stages: bank i + 1 arrives while bank i computes); the CTA expands the
 // diagonals into the full 96 x 96 matrix S (column-major, rows and columns in
 // node-major order q = 3 node + component, the order of X) and multiplies:
 // warp w takes the right-hand sides 8 (w & 1) .. + 7 and the columns
-// 48 (w >> 1) .. + 47, lane (g, h) the rows 12 g .. 12 g + 11 and the
+// 24 (w >> 1) .. + 23, lane (g, h) the rows 12 g .. 12 g + 11 and the
 // right-hand sides 8 (w & 1) + 2 h, + 1 -- per column three float4 of S, one
-// vector load of X, 24 FMAs.  The two column halves meet in shared memory.
-constexpr int NB = 32 * BD;                          // 96
+// vector load of X, 24 FMAs.  The four column quarters meet in shared memory
+// (in the stage just consumed), summed in quarter order.
+constexpr int BANK_THREADS = 256;
+constexpr int NB = 32 * BD;                             // 96
 constexpr int TILE_FLOATS = 3 * 17 * 32 + 3 * 32 * 32;  // 4704 (mas_tile_elems(3))
-constexpr int TILE_BYTES = TILE_FLOATS * 4;          // 18,816
-constexpr int RSTRIDE = NB * BK + 64;                // partial sums of one column half (+ skew)
-constexpr int XBUF_BYTES = 2 * RSTRIDE * 4;          // >= 32 x 48 pairs (12,288) and both halves (12,800)
-constexpr int BANK_SMEM = NB * NB * 4 + 2 * TILE_BYTES + 2 * XBUF_BYTES + 16;
-static_assert(XBUF_BYTES >= 32 * BD * BK * 8, "X staging holds 32 nodes of pairs");
+constexpr int TILE_BYTES = TILE_FLOATS * 4;             // 18,816
+constexpr int XBUF_BYTES = 32 * BD * BK * 8;            // 32 nodes of pairs: 12,288
+constexpr int STAGE_BYTES = TILE_BYTES + XBUF_BYTES + 512;  // + pad: the partial sums need 25,600
+constexpr int RSTRIDE = NB * BK + 64;                   // partial sums of one column quarter (+ skew)
+constexpr int BANK_SMEM = NB * NB * 4 + 2 * STAGE_BYTES + 16;
+static_assert(4 * RSTRIDE * 4 <= STAGE_BYTES, "the partial sums fit in a stage");
+static_assert(STAGE_BYTES % 16 == 0 && TILE_BYTES % 16 == 0, "bulk copies need 16-byte alignment");
 
 struct BankSmem {
-    float *S, *T, *X;  // S: 96 x 96; T: 2 tile buffers; X: 2 X / partial-sum buffers (bytes XBUF_BYTES each)
+    float *S;            // 96 x 96
+    unsigned char *st;   // 2 stages: tile (TILE_BYTES), then X (XBUF_BYTES)
     uint64_t *bar;
 };
 
@@ -398,9 +440,8 @@ __device__ __forceinline__ BankSmem bank_smem(unsigned char *raw)
 {
     BankSmem b;
     b.S = reinterpret_cast<float *>(raw);
-    b.T = b.S + NB * NB;
-    b.X = b.T + 2 * TILE_FLOATS;
-    b.bar = reinterpret_cast<uint64_t *>(reinterpret_cast<unsigned char *>(b.X) + 2 * XBUF_BYTES);
+    b.st = raw + NB * NB * 4;
+    b.bar = reinterpret_cast<uint64_t *>(b.st + 2 * STAGE_BYTES);
     return b;
 }
 
@@ -420,12 +461,12 @@ __device__ __forceinline__ void diag_of(int D, int &c, int &c2, int &d)
     }
 }
 
-// tile diagonals (shared) -> S[col * 96 + row]; warp w takes diagonals w, w + 4, ...
+// tile diagonals (shared) -> S[col * 96 + row]; warp w takes diagonals w, w + 8, ...
 // Diagonal tile, d = 16: entry [r][r + 16] belongs to row r only (row r + 16
 // has its own stored value), as in the single-system MAS.
 __device__ __forceinline__ void expand_tile(const float *__restrict__ T, float *__restrict__ S, int w, int lane)
 {
-    for (int D = w; D < 147; D += 4) {
+    for (int D = w; D < 147; D += BANK_THREADS / 32) {
         int c, c2, d;
         diag_of(D, c, c2, d);
         const float a = T[D * 32 + lane];
@@ -439,10 +480,10 @@ template <typename XT>
 __device__ __forceinline__ void bank_mma(const float *__restrict__ S, const float *__restrict__ X, int ncol, int w,
                                          int lane, float (&acc)[12][2])
 {
-    const int rh = w & 1, kh = w >> 1, g = lane >> 2, h = lane & 3;
+    const int rh = w & 1, kq = w >> 1, g = lane >> 2, h = lane & 3;
 #pragma unroll
     for (int j = 0; j < 12; ++j) acc[j][0] = acc[j][1] = 0.f;
-    const int q0 = 48 * kh, q1 = min(q0 + 48, ncol);
+    const int q0 = 24 * kq, q1 = min(q0 + 24, ncol);
     const int xo = 8 * rh + 2 * h;
 #pragma unroll 4
     for (int q = q0; q < q1; ++q) {
@@ -467,14 +508,14 @@ __device__ __forceinline__ void bank_mma(const float *__restrict__ S, const floa
     }
 }
 
-// partial sums -> R[kh][row][k] (skewed by 8 per row group of 12), R in the X buffer
+// partial sums -> R[kq][row][k] (skewed by 8 per row group of 12)
 __device__ __forceinline__ void bank_store_partials(float *__restrict__ R, int w, int lane, const float (&acc)[12][2])
 {
-    const int rh = w & 1, kh = w >> 1, g = lane >> 2, h = lane & 3;
+    const int rh = w & 1, kq = w >> 1, g = lane >> 2, h = lane & 3;
 #pragma unroll
     for (int j = 0; j < 12; ++j) {
         const int row = 12 * g + j;
-        *reinterpret_cast<float2 *>(R + kh * RSTRIDE + row * BK + 8 * g + 8 * rh + 2 * h) =
+        *reinterpret_cast<float2 *>(R + kq * RSTRIDE + row * BK + 8 * g + 8 * rh + 2 * h) =
             make_float2(acc[j][0], acc[j][1]);
     }
 }
@@ -482,13 +523,15 @@ __device__ __forceinline__ void bank_store_partials(float *__restrict__ R, int w
 __device__ __forceinline__ float bank_result(const float *__restrict__ R, int row, int k)
 {
     const int o = row * BK + 8 * (row / 12) + k;
-    return R[o] + R[RSTRIDE + o];
+    return ((R[o] + R[RSTRIDE + o]) + R[2 * RSTRIDE + o]) + R[3 * RSTRIDE + o];
 }
 
-// The bank pipeline of one CTA: jobs 0 .. nj - 1, job(i, tile, x, xbytes, cnt)
-// names the bank's inverse, its X block and item count, epi(i, R, cnt) consumes
-// the result rows 0 .. 3 cnt - 1 (R as bank_result reads it).  Returns false,
-// with *err set, when a copy did not arrive within the poll limit.
+// The bank pipeline of one CTA (BANK_THREADS threads): jobs 0 .. nj - 1,
+// job(i, tile, x, cnt) names the bank's inverse, its X block and item count,
+// epi(i, R, cnt) consumes the result rows 0 .. 3 cnt - 1 (R as bank_result
+// reads it; thread t takes rows t / 16 + 16 j, right-hand side t % 16).
+// Returns false, with *err set, when a copy did not arrive within the poll
+// limit.
 template <typename XT, typename Job, typename Epi>
 __device__ bool bank_pipeline(unsigned char *raw, int nj, Job job, Epi epi, int *err)
 {
@@ -501,9 +544,10 @@ __device__ bool bank_pipeline(unsigned char *raw, int nj, Job job, Epi epi, int 
         int cnt;
         job(i, tile, x, cnt);
         const uint32_t xbytes = (uint32_t)cnt * BD * BK * sizeof(XT);
+        unsigned char *stage = sm.st + b * STAGE_BYTES;
         mbar_arrive_expect_tx(sm.bar + b, TILE_BYTES + xbytes);
-        bulk_load(sm.T + b * TILE_FLOATS, tile, TILE_BYTES, sm.bar + b);
-        bulk_load(reinterpret_cast<unsigned char *>(sm.X) + b * XBUF_BYTES, x, xbytes, sm.bar + b);
+        bulk_load(stage, tile, TILE_BYTES, sm.bar + b);
+        bulk_load(stage + TILE_BYTES, x, xbytes, sm.bar + b);
     };
     if (t == 0) {
         mbar_init(sm.bar, 1);
@@ -534,15 +578,16 @@ __device__ bool bank_pipeline(unsigned char *raw, int nj, Job job, Epi epi, int 
         const XT *xsrc;
         int cnt;
         job(i, tile, xsrc, cnt);
-        float *X = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(sm.X) + b * XBUF_BYTES);
-        expand_tile(sm.T + b * TILE_FLOATS, sm.S, w, lane);
+        unsigned char *stage = sm.st + b * STAGE_BYTES;
+        expand_tile(reinterpret_cast<const float *>(stage), sm.S, w, lane);
         __syncthreads();
         float acc[12][2];
-        bank_mma<XT>(sm.S, X, 3 * cnt, w, lane, acc);
+        bank_mma<XT>(sm.S, reinterpret_cast<const float *>(stage + TILE_BYTES), 3 * cnt, w, lane, acc);
         __syncthreads();
-        bank_store_partials(X, w, lane, acc);
+        float *R = reinterpret_cast<float *>(stage);  // the stage is consumed: partial sums
+        bank_store_partials(R, w, lane, acc);
         __syncthreads();
-        epi(i, X, cnt);
+        epi(i, R, cnt);
         __syncthreads();
         if (t == 0 && i + 2 < nj) {
             proxy_async_fence();
@@ -576,7 +621,7 @@ __global__ void __launch_bounds__(256) prolong_kernel(MasDev m, float *__restric
 }
 
 // coarse banks: u = Inv_l v, all levels in one launch (banks grid-strided)
-__global__ void __launch_bounds__(128) symv_coarse_kernel(MasDev m, const float *__restrict__ invc,
+__global__ void __launch_bounds__(BANK_THREADS) symv_coarse_kernel(MasDev m, const float *__restrict__ invc,
                                                           const float *__restrict__ v, float *__restrict__ u,
                                                           int *err)
 {
@@ -601,7 +646,7 @@ __global__ void __launch_bounds__(128) symv_coarse_kernel(MasDev m, const float 
         locate(i, gb, at);
         const int k = threadIdx.x & (BK - 1);
 #pragma unroll 4
-        for (int row = threadIdx.x >> 4; row < NB; row += 8) u[at + row * BK + k] = bank_result(R, row, k);
+        for (int row = threadIdx.x >> 4; row < NB; row += BANK_THREADS / BK) u[at + row * BK + k] = bank_result(R, row, k);
     };
     bank_pipeline<float>(smem_raw, nj, job, epi, err);
 }
@@ -610,7 +655,7 @@ __global__ void __launch_bounds__(128) symv_coarse_kernel(MasDev m, const float 
 // gamma = r.z per lane (dot 1: initial gamma; dot 2: beta and the new gamma).
 // One CTA per chunk, its parts in sequence through the bank pipeline.
 template <typename XT, bool ACC, int DOT>
-__global__ void __launch_bounds__(128) symv0_kernel(BatchDev B, MasDev m, const float *__restrict__ inv0,
+__global__ void __launch_bounds__(BANK_THREADS) symv0_kernel(BatchDev B, MasDev m, const float *__restrict__ inv0,
                                                     const float *__restrict__ u, const XT *__restrict__ xin,
                                                     float2 *__restrict__ z, const float2 *__restrict__ rdot)
 {
@@ -632,7 +677,7 @@ __global__ void __launch_bounds__(128) symv0_kernel(BatchDev B, MasDev m, const 
         const int32_t p = ch.p0 + i, lo = m.part_off[p];
         const bool coarse = m.L > 1 && m.ccnt0[p] > 0;
         const int32_t cb = coarse ? m.cbase0[p] : 0;
-        for (int row = threadIdx.x >> 4; row < 3 * cnt; row += 8) {
+        for (int row = threadIdx.x >> 4; row < 3 * cnt; row += BANK_THREADS / BK) {
             const int node = row / 3, c = row - 3 * node;
             float y = bank_result(R, row, k);
             if (coarse) y += u1[((int64_t)(cb + m.key0[lo + node]) * BD + c) * BK + k];
@@ -648,12 +693,12 @@ __global__ void __launch_bounds__(128) symv0_kernel(BatchDev B, MasDev m, const 
     };
     if (!bank_pipeline<XT>(smem_raw, ch.p1 - ch.p0, job, epi, B.err)) return;
     if (DOT) {
-        __shared__ double red[8][BK];
+        __shared__ double red[BANK_THREADS / BK][BK];
         red[threadIdx.x >> 4][k] = (double)dh + (double)dl;
         __syncthreads();
         double part[1] = {0.0}, tot[1];
         if (threadIdx.x < BK)
-            for (int q = 0; q < 8; ++q) part[0] += red[q][threadIdx.x];
+            for (int q = 0; q < BANK_THREADS / BK; ++q) part[0] += red[q][threadIdx.x];
         if (sys_finish<1>(B, blockIdx.x, ch.sys, part, tot)) {
             BatchLane &L = B.lane[ch.sys * BK + threadIdx.x];
             if (!L.done) {
@@ -678,18 +723,25 @@ __global__ void __launch_bounds__(256) residual32_kernel(BatchDev B, const float
         const int32_t b = B.rows[I], len = B.rows[I + 1] - b;
         const bool precise = B.precise && B.precise[I];
         if (!precise) {
+            constexpr int U = 4;
             const float *__restrict__ v = B.vals32 + (int64_t)b * 9;
             float y[BD] = {0.f, 0.f, 0.f};
-            for (int32_t l = h; l < len; l += 2) {
-                const int32_t J = B.cols[b + l];
-                float xv[BD];
+            row_blocks<U>(B, b, len, lane, [&](int l, const int32_t (&J)[U], const bool (&ok)[U]) {
+                float xv[U][BD], a[U][BD * BD];
 #pragma unroll
-                for (int c = 0; c < BD; ++c) xv[c] = z[((int64_t)J * BD + c) * BK + k].x;
+                for (int u = 0; u < U; ++u) {
 #pragma unroll
-                for (int rr = 0; rr < BD; ++rr)
+                    for (int c = 0; c < BD; ++c) xv[u][c] = ok[u] ? z[((int64_t)J[u] * BD + c) * BK + k].x : 0.f;
 #pragma unroll
-                    for (int c = 0; c < BD; ++c) y[rr] += __ldg(v + (int64_t)(rr * BD + c) * len + l) * xv[c];
-            }
+                    for (int e = 0; e < BD * BD; ++e) a[u][e] = ok[u] ? __ldg(v + (int64_t)e * len + l + 2 * u) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int rr = 0; rr < BD; ++rr)
+#pragma unroll
+                        for (int c = 0; c < BD; ++c) y[rr] += a[u][rr * BD + c] * xv[u][c];
+            });
 #pragma unroll
             for (int rr = 0; rr < BD; ++rr) y[rr] += __shfl_xor_sync(FULL, y[rr], 16);
             if (h == 0)
@@ -699,21 +751,28 @@ __global__ void __launch_bounds__(256) residual32_kernel(BatchDev B, const float
                     wout[e] = r[e].x - y[rr];
                 }
         } else {
+            constexpr int U = 2;
             const float2 *__restrict__ v = B.vals_df + (int64_t)b * 9;
             float sh[BD] = {0.f, 0.f, 0.f}, sl[BD] = {0.f, 0.f, 0.f};
-            for (int32_t l = h; l < len; l += 2) {
-                const int32_t J = B.cols[b + l];
-                float2 xv[BD];
+            row_blocks<U>(B, b, len, lane, [&](int l, const int32_t (&J)[U], const bool (&ok)[U]) {
+                float2 xv[U][BD], a[U][BD * BD];
 #pragma unroll
-                for (int c = 0; c < BD; ++c) xv[c] = z[((int64_t)J * BD + c) * BK + k];
+                for (int u = 0; u < U; ++u) {
 #pragma unroll
-                for (int rr = 0; rr < BD; ++rr)
+                    for (int c = 0; c < BD; ++c)
+                        xv[u][c] = ok[u] ? z[((int64_t)J[u] * BD + c) * BK + k] : make_float2(0.f, 0.f);
 #pragma unroll
-                    for (int c = 0; c < BD; ++c) {
-                        const float2 a = __ldg(v + (int64_t)(rr * BD + c) * len + l);
-                        df_fma(sh[rr], sl[rr], a.x, a.y, xv[c].x, xv[c].y);
-                    }
-            }
+                    for (int e = 0; e < BD * BD; ++e)
+                        a[u][e] = ok[u] ? __ldg(v + (int64_t)e * len + l + 2 * u) : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int rr = 0; rr < BD; ++rr)
+#pragma unroll
+                        for (int c = 0; c < BD; ++c)
+                            df_fma(sh[rr], sl[rr], a[u][rr * BD + c].x, a[u][rr * BD + c].y, xv[u][c].x, xv[u][c].y);
+            });
 #pragma unroll
             for (int rr = 0; rr < BD; ++rr) {
                 const float bh = __shfl_xor_sync(FULL, sh[rr], 16), bl = __shfl_xor_sync(FULL, sl[rr], 16);
@@ -916,7 +975,7 @@ void launch_mas(const BatchDev &B, const BatchMas &M, const float2 *xin_pair, co
             if (m.nbanks[l] > 0) restrict_kernel<<<(unsigned)((m.nbanks[l] + 7) / 8), 256, 0, s>>>(m, l, M.v);
         raise_smem_limit((const void *)symv_coarse_kernel, smem);
         if (m.ncoarse > 0)
-            symv_coarse_kernel<<<(unsigned)std::min<int64_t>(m.ncoarse, sm_grid(2)), 128, smem, s>>>(m, M.invc, M.v,
+            symv_coarse_kernel<<<(unsigned)std::min<int64_t>(m.ncoarse, sm_grid(2)), BANK_THREADS, smem, s>>>(m, M.invc, M.v,
                                                                                                     M.u, B.err);
         if (m.L > 2 && m.nitems[1] > 0)
             prolong_kernel<<<(unsigned)(((int64_t)m.nitems[1] * BD * BK + 255) / 256), 256, 0, s>>>(m, M.u);
@@ -924,7 +983,7 @@ void launch_mas(const BatchDev &B, const BatchMas &M, const float2 *xin_pair, co
 #define LSS_B0(XT_, X_, A_, D_)                                                                          \
     do {                                                                                                 \
         raise_smem_limit((const void *)symv0_kernel<XT_, A_, D_>, smem);                                 \
-        symv0_kernel<XT_, A_, D_><<<B.nchunk, 128, smem, s>>>(B, m, M.inv0, M.u, X_, z, rdot);           \
+        symv0_kernel<XT_, A_, D_><<<B.nchunk, BANK_THREADS, smem, s>>>(B, m, M.inv0, M.u, X_, z, rdot);  \
     } while (0)
     if (xin_pair) {
         if (acc) {

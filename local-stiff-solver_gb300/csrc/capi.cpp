@@ -46,6 +46,9 @@ void raise_smem_limit(const void *kernel, size_t bytes)
     size_t &cur = set[{dev, kernel}];
     if (bytes <= cur) return;
     LSS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    // the largest shared-memory carveout, so that as many CTAs as fit are resident
+    LSS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared));
     cur = bytes;
 }
 int sm_grid(int per_sm)

@@ -176,7 +176,11 @@ template <int BD>
 __global__ void __launch_bounds__(256) assemble_coarse_chunk_kernel(BsrDev A, MasDev m, const int32_t *__restrict__ cmap,
                                                                     CoarseMembers mb, double *__restrict__ partial)
 {
+    __shared__ int8_t slot_all[8][32];  // per warp: column slot -> lane holding its group sum
     const int lane = threadIdx.x & 31;
+    int8_t *slot = slot_all[threadIdx.x >> 5];
+    slot[lane] = -1;
+    __syncwarp();
     const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (c >= mb.nchunk) return;
     // the chunk's item: last i with item_chunk[i] <= c
@@ -209,17 +213,39 @@ __global__ void __launch_bounds__(256) assemble_coarse_chunk_kernel(BsrDev A, Ma
 #pragma unroll
                 for (int k = 0; k < BD * BD; ++k) val[k] = 0.0;
             }
-            unsigned pending = __ballot_sync(0xffffffffu, cj >= 0 && (cj >> 5) == (ci >> 5));
-            while (pending) {
-                const int src = __ffs(pending) - 1;
-                pending &= pending - 1;
-                const int32_t cc = __shfl_sync(0xffffffffu, cj, src);
+            const bool mine = cj >= 0 && (cj >> 5) == (ci >> 5);
+            if (!__any_sync(0xffffffffu, mine)) continue;
+            // lanes holding the same column item form a group; its leader (lowest
+            // lane) sums the group in lane order, then hands the sum to the lane
+            // that owns the item's slot -- groups proceed in parallel
+            const unsigned grp = __match_any_sync(0xffffffffu, mine ? cj : (int32_t)(0x80000000u | (unsigned)lane));
+            const bool leader = mine && __ffs(grp) - 1 == lane;
+            unsigned rest = mine ? grp & (grp - 1) : 0u;
+            const int rounds = __reduce_max_sync(0xffffffffu, __popc(rest));
+            double gs[BD * BD];
+#pragma unroll
+            for (int k = 0; k < BD * BD; ++k) gs[k] = val[k];
+            for (int it = 0; it < rounds; ++it) {
+                const bool have = rest != 0u;
+                const int src = have ? __ffs(rest) - 1 : lane;
+                rest &= rest - 1u;
 #pragma unroll
                 for (int k = 0; k < BD * BD; ++k) {
                     const double x = __shfl_sync(0xffffffffu, val[k], src);
-                    if ((cc & 31) == lane) acc[k] += x;
+                    if (have) gs[k] += x;
                 }
             }
+            if (leader) slot[cj & 31] = (int8_t)lane;
+            __syncwarp();
+            const int from = slot[lane];
+            __syncwarp();
+            if (leader) slot[cj & 31] = -1;
+#pragma unroll
+            for (int k = 0; k < BD * BD; ++k) {
+                const double x = __shfl_sync(0xffffffffu, gs[k], from >= 0 ? from : lane);
+                if (from >= 0) acc[k] += x;
+            }
+            __syncwarp();
         }
     }
     double *out = partial + c * (BD * BD * 32);

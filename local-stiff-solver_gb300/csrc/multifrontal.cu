@@ -16,6 +16,7 @@
 
 #include "device_common.cuh"
 #include "multifrontal.hpp"
+#include "spmv.cuh"
 
 namespace lss {
 namespace {
@@ -420,54 +421,152 @@ __global__ void mf_scatter_kernel(MfView v, const StiffDev S, const double *__re
 
 // ---- solve with NR right-hand sides at once (the batched PCG): t, w and x
 // hold NR values per entry, [entry][NR]; z is a double-float pair vector.
+// The fronts are read as double-float pairs (Fp: the FP64 factor split into
+// FP32 (hi, lo), 8 bytes per entry like FP64) and every product runs on the
+// FP32 pipe with error-free products and compensated sums (about 2^-48
+// relative per term): GB300 issues 64 FP32 FMAs per FP64 FMA, and the NR
+// right-hand sides make the solve arithmetic-bound.
+//
+// Forward, per level: one CTA per front sums the right-hand side and the
+// children's contributions into the front's vector (extend-add, children in
+// order), then CTAs of COLS output columns apply c = w_bnd - P w_own.
+// Backward, per level: CTAs of COLS output columns apply
+// x_own = F11^-1 (w_own - F12 x_bnd).  A GEMV CTA's 256 threads are COLS
+// columns x (256 / COLS) row slices (thread t: column t % COLS, rows
+// q = t / COLS + (256 / COLS) j), each keeping all NR sums of its column; the
+// slices meet in shared memory in slice order.  COLS = 32 for fronts of up to
+// 256 rows, else 8 (more CTAs per large front).  The solve vector in shared
+// memory is pairs, the 16-byte slots of row q XOR-swizzled by q % 8 so that
+// the rows a warp reads at once fall into different banks.
 
+constexpr int NR_SMALL_ROWS = 256;  // fronts with at most this many GEMV rows use 32-column CTAs
+
+__host__ __device__ __forceinline__ int nr_cols(int rows) { return rows <= NR_SMALL_ROWS ? 32 : 8; }
+
+__device__ __forceinline__ float2 split_pair(double d)
+{
+    const float h = (float)d;
+    return make_float2(h, (float)(d - (double)h));
+}
+
+// pair index of right-hand side k in row q (swizzled 16-byte slots)
 template <int NR>
-__global__ void __launch_bounds__(256) mf_forward_nr_kernel(MfView v, MfWork w, const double *__restrict__ T,
-                                                            const double *__restrict__ F, double *__restrict__ W,
-                                                            const int *sys_done, const int32_t *front_sys)
+__device__ __forceinline__ int swz(int q, int k)
+{
+    return q * NR + ((((k >> 1) ^ (q & 7))) << 1) + (k & 1);
+}
+
+// out[c][k] = sum_q Fn[q][col0 + c] xs[q][k] for the CTA's COLS columns
+// (c < ncol), q < nrow; handed over as a pair by out(c, k, hi, lo)
+template <int NR, int COLS, typename Out>
+__device__ __forceinline__ void nr_gemv(const float2 *__restrict__ Fn, int f, int col0, int ncol, int nrow,
+                                        const float2 *__restrict__ xs, float2 *__restrict__ red, Out out)
+{
+    constexpr int SL = 256 / COLS;
+    const int cl = threadIdx.x % COLS, ks = threadIdx.x / COLS;
+    float ah[NR], al[NR];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) ah[k] = al[k] = 0.f;
+    if (cl < ncol) {
+        const float2 *Fc = Fn + col0 + cl;
+        auto step = [&](const float2 a, int q) {
+            const float4 *xv = reinterpret_cast<const float4 *>(xs + q * NR);
+            const int sw = q & 7;
+#pragma unroll
+            for (int kk = 0; kk < NR / 2; ++kk) {
+                const float4 x2 = xv[kk ^ sw];
+                df_fma(ah[2 * kk], al[2 * kk], a.x, a.y, x2.x, x2.y);
+                df_fma(ah[2 * kk + 1], al[2 * kk + 1], a.x, a.y, x2.z, x2.w);
+            }
+        };
+        // eight rows' loads in flight before their products
+        int q = ks;
+        for (; q + 7 * SL < nrow; q += 8 * SL) {
+            float2 a[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = __ldg(Fc + (int64_t)(q + u * SL) * f);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) step(a[u], q + u * SL);
+        }
+        for (; q < nrow; q += SL) step(__ldg(Fc + (int64_t)q * f), q);
+    }
+    // partials of (slice, column), slots swizzled by the column
+    float4 *dst = reinterpret_cast<float4 *>(red + (ks * COLS + cl) * NR);
+#pragma unroll
+    for (int kk = 0; kk < NR / 2; ++kk)
+        dst[kk ^ (cl & 7)] = make_float4(ah[2 * kk], al[2 * kk], ah[2 * kk + 1], al[2 * kk + 1]);
+    __syncthreads();
+    for (int o = threadIdx.x; o < COLS * NR; o += blockDim.x) {
+        const int c = o / NR, k = o % NR;
+        if (c >= ncol) continue;
+        const int slot = (((k >> 1) ^ (c & 7)) << 1) | (k & 1);
+        float h = 0.f, l = 0.f;
+#pragma unroll 8
+        for (int q = 0; q < SL; ++q) {
+            const float2 v = red[(q * COLS + c) * NR + slot];
+            df_add(h, l, v.x, v.y);
+        }
+        out(c, k, h, l);
+    }
+}
+
+// forward, step 1: W_N = [t_own ; 0] + the children's contributions, every
+// entry gathered from its contributors (gptr/gsrc: per entry of W, the child
+// entries that extend-add into it, children in ascending order); CTAs of 16
+// entries x NR right-hand sides
+template <int NR>
+__global__ void __launch_bounds__(256) mf_fassemble_nr_kernel(MfView v, MfWork w, const int32_t *__restrict__ gptr,
+                                                              const int32_t *__restrict__ gsrc,
+                                                              const double *__restrict__ T, float2 *__restrict__ W,
+                                                              const int *sys_done, const int32_t *front_sys)
+{
+    static_assert(NR == 16, "16 entries x 16 right-hand sides per CTA");
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    if (sys_done && sys_done[front_sys[N]]) return;
+    const int s = v.s[N], f = s + v.u[N];
+    const int q = (int)(blockIdx.x - w.prefix[i]) * 16 + (int)(threadIdx.x >> 4), k = threadIdx.x & 15;
+    if (q >= f) return;
+    const int64_t e = (int64_t)v.woff[N] + q;
+    float2 acc = q < s ? split_pair(T[(int64_t)v.pos2j[v.p0[N] + q] * NR + k]) : make_float2(0.f, 0.f);
+    for (int32_t g = gptr[e]; g < gptr[e + 1]; ++g) {
+        const float2 c = W[(int64_t)gsrc[g] * NR + k];
+        df_add(acc.x, acc.y, c.x, c.y);
+    }
+    W[e * NR + k] = acc;
+}
+
+// forward, step 2: W_N[bnd] -= P W_N[own] over the CTA's boundary columns
+template <int NR>
+__global__ void __launch_bounds__(256) mf_forward_nr_kernel(MfView v, MfWork w, const float2 *__restrict__ Fp,
+                                                            float2 *__restrict__ W, const int *sys_done,
+                                                            const int32_t *front_sys)
 {
     extern __shared__ double sm[];
     const int i = find_front(w, blockIdx.x);
     const int32_t N = w.front[i];
     if (sys_done && sys_done[front_sys[N]]) return;
     const int s = v.s[N], u = v.u[N], f = s + u;
-    const int chunk = (int)(blockIdx.x - w.prefix[i]);
-    double *wown = sm, *wb = sm + (int64_t)s * NR;
-    const int r0 = s + chunk * PW;
-    for (int e = threadIdx.x; e < s * NR; e += blockDim.x)
-        wown[e] = T[(int64_t)v.pos2j[v.p0[N] + e / NR] * NR + e % NR];
-    for (int e = threadIdx.x; e < PW * NR; e += blockDim.x) wb[e] = 0.0;
+    const int cols = nr_cols(s);
+    const int col0 = s + (int)(blockIdx.x - w.prefix[i]) * cols;
+    float2 *xs = reinterpret_cast<float2 *>(sm), *red = xs + (int64_t)s * NR;
+    float2 *Wn = W + (int64_t)v.woff[N] * NR;
+    for (int e = threadIdx.x; e < s * NR; e += blockDim.x) xs[swz<NR>(e / NR, e % NR)] = Wn[e];
     __syncthreads();
-    for (int32_t ci = v.child_off[N]; ci < v.child_off[N + 1]; ++ci) {
-        const int32_t c = v.child[ci], uc = v.u[c];
-        const double *cw = W + ((int64_t)v.woff[c] + v.s[c]) * NR;
-        const int32_t *map = v.ea_map + v.bnd_off[c];
-        for (int e = threadIdx.x; e < uc * NR; e += blockDim.x) {
-            const int m = map[e / NR], k = e % NR;
-            if (m < s) wown[m * NR + k] += cw[e];
-            else if (m >= r0 && m < r0 + PW) wb[(m - r0) * NR + k] += cw[e];
-        }
-        __syncthreads();
-    }
-    double *Wn = W + (int64_t)v.woff[N] * NR;
-    if (chunk == 0)
-        for (int e = threadIdx.x; e < s * NR; e += blockDim.x) Wn[e] = wown[e];
-    if (u == 0) return;
-    // thread (lane = output column, warp = right-hand sides warp, warp + 8, ...)
-    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-    const int col = r0 + lane;
-    if (col >= f) return;
-    const double *Fn = F + v.foff[N];
-    for (int k = wq; k < NR; k += 8) {
-        double acc = 0.0;
-        for (int q = 0; q < s; ++q) acc += Fn[(int64_t)q * f + col] * wown[q * NR + k];
-        Wn[(int64_t)col * NR + k] = wb[lane * NR + k] - acc;
-    }
+    auto out = [&](int c, int k, float h, float l) {
+        float2 &o = Wn[(int64_t)(col0 + c) * NR + k];
+        float oh = o.x, ol = o.y;
+        df_add(oh, ol, -h, -l);
+        o = make_float2(oh, ol);
+    };
+    const float2 *Fn = Fp + v.foff[N];
+    if (cols == 32) nr_gemv<NR, 32>(Fn, f, col0, min(32, f - col0), s, xs, red, out);
+    else nr_gemv<NR, 8>(Fn, f, col0, min(8, f - col0), s, xs, red, out);
 }
 
 template <int NR>
-__global__ void __launch_bounds__(256) mf_backward_nr_kernel(MfView v, MfWork w, const double *__restrict__ F,
-                                                             const double *__restrict__ W, double *__restrict__ X,
+__global__ void __launch_bounds__(256) mf_backward_nr_kernel(MfView v, MfWork w, const float2 *__restrict__ Fp,
+                                                             const float2 *__restrict__ W, float2 *__restrict__ X,
                                                              const int *sys_done, const int32_t *front_sys)
 {
     extern __shared__ double sm[];
@@ -475,28 +574,33 @@ __global__ void __launch_bounds__(256) mf_backward_nr_kernel(MfView v, MfWork w,
     const int32_t N = w.front[i];
     if (sys_done && sys_done[front_sys[N]]) return;
     const int s = v.s[N], u = v.u[N], f = s + u;
-    const int chunk = (int)(blockIdx.x - w.prefix[i]);
-    double *vec = sm;
-    const double *Wn = W + (int64_t)v.woff[N] * NR;
+    const int cols = nr_cols(f);
+    const int c0 = (int)(blockIdx.x - w.prefix[i]) * cols;
+    float2 *vec = reinterpret_cast<float2 *>(sm), *red = vec + (int64_t)f * NR;
+    const float2 *Wn = W + (int64_t)v.woff[N] * NR;
     const int32_t *bp = v.bnd_pos + v.bnd_off[N];
+#pragma unroll 4
     for (int e = threadIdx.x; e < f * NR; e += blockDim.x) {
         const int q = e / NR, k = e % NR;
-        vec[e] = q < s ? Wn[e] : X[(int64_t)bp[q - s] * NR + k];
+        vec[swz<NR>(q, k)] = q < s ? Wn[e] : X[(int64_t)bp[q - s] * NR + k];
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-    const int c = chunk * PW + lane;
-    if (c >= s) return;
-    const double *Fn = F + v.foff[N];
-    for (int k = wq; k < NR; k += 8) {
-        double acc = 0.0;
-        for (int q = 0; q < f; ++q) acc += Fn[(int64_t)q * f + c] * vec[q * NR + k];
-        X[((int64_t)v.p0[N] + c) * NR + k] = -acc;
-    }
+    // x_own = F11^-1 (w_own - F12 x_bnd) = -(column c of the swept front) . vec
+    const int64_t xo = (int64_t)v.p0[N] + c0;
+    auto out = [&](int c, int k, float h, float l) { X[(xo + c) * NR + k] = make_float2(-h, -l); };
+    const float2 *Fn = Fp + v.foff[N];
+    if (cols == 32) nr_gemv<NR, 32>(Fn, f, c0, min(32, s - c0), f, vec, red, out);
+    else nr_gemv<NR, 8>(Fn, f, c0, min(8, s - c0), f, vec, red, out);
+}
+
+__global__ void split_pairs_kernel(int64_t n, const double *__restrict__ src, float2 *__restrict__ dst)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = split_pair(src[t]);
 }
 
 template <int NR>
-__global__ void mf_scatter_nr_kernel(MfView v, const StiffDev S, const double *__restrict__ X,
+__global__ void mf_scatter_nr_kernel(MfView v, const StiffDev S, const float2 *__restrict__ X,
                                      float2 *__restrict__ z)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -504,10 +608,11 @@ __global__ void mf_scatter_nr_kernel(MfView v, const StiffDev S, const double *_
     const int64_t p = t / NR;
     const int k = (int)(t % NR);
     const int64_t e = (int64_t)S.dofs[v.pos2j[p]] * NR + k;
-    const float2 zo = z[e];
-    const double nz = (double)zo.x + (double)zo.y + X[t];
-    const float h = (float)nz;
-    z[e] = make_float2(h, (float)(nz - (double)h));
+    float h = z[e].x, l = z[e].y;
+    const float2 xv = X[t];
+    df_add(h, l, xv.x, xv.y);
+    const float r = __fadd_rn(h, l);
+    z[e] = make_float2(r, __fsub_rn(l, __fsub_rn(r, h)));
 }
 
 }  // namespace
@@ -599,11 +704,41 @@ void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
         make(L.mirror, lv_large[h], [&](int32_t id) { return (F_of(id) * M.s[id] + 255) / 256; });
         make(L.fwd, lv_all[h], [&](int32_t id) { return std::max<int64_t>(1, (M.u[id] + PW - 1) / PW); });
         make(L.bwd, lv_all[h], [&](int32_t id) { return (int64_t)(M.s[id] + PW - 1) / PW; });
+        make(L.fasm_nr, lv_all[h], [&](int32_t id) { return (F_of(id) + 15) / 16; });
+        make(L.fwd_nr, lv_all[h], [&](int32_t id) {
+            const int c = nr_cols(M.s[id]);
+            return (int64_t)(M.u[id] + c - 1) / c;
+        });
+        make(L.bwd_nr, lv_all[h], [&](int32_t id) {
+            const int c = nr_cols(M.s[id] + M.u[id]);
+            return (int64_t)(M.s[id] + c - 1) / c;
+        });
         for (int32_t id : lv_large[h]) L.max_s_large = std::max(L.max_s_large, M.s[id]);
     }
+    // extend-add as a gather: per entry of W, the child entries that add into it
+    std::vector<int32_t> gptr((size_t)M.welems + 1, 0), gsrc;
+    {
+        for (int32_t id = 0; id < nf; ++id)
+            for (int32_t ci = M.child_off[id]; ci < M.child_off[id + 1]; ++ci) {
+                const int32_t c = M.child[ci];
+                for (int32_t j = 0; j < M.u[c]; ++j) ++gptr[(size_t)M.woff[id] + M.ea_map[M.bnd_off[c] + j] + 1];
+            }
+        for (size_t e = 0; e < (size_t)M.welems; ++e) gptr[e + 1] += gptr[e];
+        gsrc.resize(gptr.back());
+        std::vector<int32_t> fill(gptr.begin(), gptr.end() - 1);
+        for (int32_t id = 0; id < nf; ++id)
+            for (int32_t ci = M.child_off[id]; ci < M.child_off[id + 1]; ++ci) {
+                const int32_t c = M.child[ci];
+                for (int32_t j = 0; j < M.u[c]; ++j)
+                    gsrc[fill[(size_t)M.woff[id] + M.ea_map[M.bnd_off[c] + j]]++] = M.woff[c] + M.s[c] + j;
+            }
+    }
+    const size_t a_gp = put32(gptr), a_gs = put32(gsrc);
     d_i32_.upload(i32, st);
     d_i64_.upload(i64, st);
     const int32_t *b32 = d_i32_.data();
+    gptr_ = b32 + a_gp;
+    gsrc_ = b32 + a_gs;
     const int64_t *b64 = d_i64_.data();
     for (const Pending &q : pend) {
         q.w->front = b32 + q.fat;
@@ -711,15 +846,26 @@ void MfFactor::solve(const StiffDev &S, double *z, float *z32, float *z_lo, cons
     LSS_LAUNCH_CHECK();
 }
 
+void MfFactor::make_pairs(cudaStream_t st)
+{
+    d_Fp_.resize(std::max<int64_t>(sym_.elems, 1));
+    if (sym_.elems > 0) {
+        split_pairs_kernel<<<(unsigned)((sym_.elems + 255) / 256), 256, 0, st>>>(sym_.elems, d_F_.data(), d_Fp_.data());
+        LSS_LAUNCH_CHECK();
+    }
+}
+
 void MfFactor::solve_batch(const StiffDev &S, const double *t, float2 *z, const int *sys_done,
                            const int32_t *front_sys, cudaStream_t st)
 {
     if (sym_.nfront == 0) return;
+    if (d_Fp_.size() < (size_t)sym_.elems) fail(LSS_ERR_INTERNAL, "batched multifrontal solve before make_pairs");
     constexpr int NR = 16;
     const MfView v = make_view(p0_, s_, u_, woff_, bnd_off_, bnd_pos_, child_off_, child_, ea_map_, front_of_pos_,
                                pos2j_, j2pos_, poff_, foff_, sym_.j_base, sym_.npos);
-    const size_t fsmem = (size_t)(sym_.max_s + PW) * NR * sizeof(double);
-    const size_t bsmem = (size_t)sym_.max_f * NR * sizeof(double);
+    const size_t red = (size_t)256 * NR * sizeof(float2);
+    const size_t fsmem = (size_t)sym_.max_s * NR * sizeof(float2) + red;
+    const size_t bsmem = (size_t)sym_.max_f * NR * sizeof(float2) + red;
     if (fsmem > 227 * 1024 || bsmem > 227 * 1024)
         fail(LSS_ERR_UNSUPPORTED, "a stiff subdomain front (" + std::to_string(sym_.max_f) +
                                       " variables) is too large for the batched multifrontal solve");
@@ -728,14 +874,17 @@ void MfFactor::solve_batch(const StiffDev &S, const double *t, float2 *z, const 
     if (d_wb_.size() < (size_t)std::max<int64_t>(sym_.welems, 1) * NR) d_wb_.resize(std::max<int64_t>(sym_.welems, 1) * NR);
     if (d_xb_.size() < (size_t)std::max<int32_t>(sym_.npos, 1) * NR) d_xb_.resize(std::max<int32_t>(sym_.npos, 1) * NR);
     for (const Level &L : levels_) {
-        mf_forward_nr_kernel<NR><<<(unsigned)L.fwd.ctas, 256, fsmem, st>>>(v, L.fwd, t, d_F_.data(), d_wb_.data(),
-                                                                         sys_done, front_sys);
+        mf_fassemble_nr_kernel<NR><<<(unsigned)L.fasm_nr.ctas, 256, 0, st>>>(v, L.fasm_nr, gptr_, gsrc_, t,
+                                                                           d_wb_.data(), sys_done, front_sys);
+        if (L.fwd_nr.ctas > 0)
+            mf_forward_nr_kernel<NR><<<(unsigned)L.fwd_nr.ctas, 256, fsmem, st>>>(v, L.fwd_nr, d_Fp_.data(),
+                                                                                d_wb_.data(), sys_done, front_sys);
         LSS_LAUNCH_CHECK();
     }
     for (int h = (int)levels_.size() - 1; h >= 0; --h) {
         const Level &L = levels_[h];
-        mf_backward_nr_kernel<NR><<<(unsigned)L.bwd.ctas, 256, bsmem, st>>>(v, L.bwd, d_F_.data(), d_wb_.data(),
-                                                                          d_xb_.data(), sys_done, front_sys);
+        mf_backward_nr_kernel<NR><<<(unsigned)L.bwd_nr.ctas, 256, bsmem, st>>>(v, L.bwd_nr, d_Fp_.data(), d_wb_.data(),
+                                                                             d_xb_.data(), sys_done, front_sys);
         LSS_LAUNCH_CHECK();
     }
     mf_scatter_nr_kernel<NR><<<(unsigned)(((int64_t)sym_.npos * NR + 255) / 256), 256, 0, st>>>(v, S, d_xb_.data(), z);

@@ -85,6 +85,8 @@ public:
     // of a system with sys_done[front_sys[N]] set are skipped.
     void solve_batch(const StiffDev &S, const double *t, float2 *z, const int *sys_done, const int32_t *front_sys,
                      cudaStream_t s);
+    // the fronts as double-float pairs for solve_batch (after the fronts are final)
+    void make_pairs(cudaStream_t s);
     const MfSymbolic &symbolic() const { return sym_; }
     // device front storage (f x f per front, foff offsets), for merging factors
     const double *fronts() const { return d_F_.data(); }
@@ -93,7 +95,7 @@ public:
 
 private:
     struct Level {
-        MfWork ea, small, diag, panel, update, write, mirror, fwd, bwd;
+        MfWork ea, small, diag, panel, update, write, mirror, fwd, bwd, fasm_nr, fwd_nr, bwd_nr;
         int32_t max_s_large = 0;
     };
     MfSymbolic sym_;
@@ -101,11 +103,13 @@ private:
     DBuf<int32_t> d_i32_;  // symbolic arrays and work-list fronts
     DBuf<int64_t> d_i64_;  // front offsets and work-list prefixes
     DBuf<double> d_F_, d_w_, d_x_, d_P_, d_D_;
-    DBuf<double> d_wb_, d_xb_;  // solve vectors of the batched solve
+    DBuf<float2> d_wb_, d_xb_;  // solve vectors of the batched solve (double-float pairs)
+    DBuf<float2> d_Fp_;         // fronts as (hi, lo) FP32 pairs, for the batched solve
     const int32_t *p0_ = nullptr, *s_ = nullptr, *u_ = nullptr, *woff_ = nullptr, *bnd_off_ = nullptr,
                   *bnd_pos_ = nullptr, *child_off_ = nullptr, *child_ = nullptr, *ea_map_ = nullptr,
                   *front_of_pos_ = nullptr, *pos2j_ = nullptr, *j2pos_ = nullptr, *poff_ = nullptr;
     const int64_t *foff_ = nullptr;
+    const int32_t *gptr_ = nullptr, *gsrc_ = nullptr;  // extend-add gather lists (batched solve)
 };
 
 }  // namespace lss
