@@ -786,7 +786,8 @@ def batched_measure(seed, local, count, nrhs, steps, warmup, sequential=True):
            "iterations_batched_mean": float(its_m.mean()), "iterations_batched_max": int(its_m.max()),
            "worst_rel_residual_batched": worst, "worst_rel_residual_over_max_1e-8_and_fp64_floor": worst_vs_floor,
            "gpu_launches": int(launches) if launches > 0 else None,
-           "dtype": "f64 lane scalars and final residual, df32 vectors and A.p, f32 MAS, f64 stiff factor"}
+           "dtype": "f64 lane scalars, solution and final residual; df32 correction vectors and A.p; f32 MAS; "
+                    "f64 stiff factors (dense inverses applied in f64, multifrontal fronts applied as df32 pairs)"}
     if sequential:
         run_sequential(s_mixed)  # warm-up of the single-system graphs
         torch.cuda.synchronize()

@@ -227,6 +227,7 @@ __global__ void __launch_bounds__(256) update_xr_kernel(BatchDev B, float2 *__re
     const float ah = (float)alpha, al = (float)(alpha - (double)ah);
     float rh = 0.f, rl = 0.f;
     const int64_t e1 = (int64_t)ch.r1 * BD * BK;
+#pragma unroll 4
     for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x) {
         if (!live) continue;
         x[e] = df_sum(x[e], df_mul(p[e], ah, al));
@@ -274,6 +275,7 @@ __global__ void __launch_bounds__(256) update_p_kernel(BatchDev B, float2 *__res
     const double beta = L.beta;
     const float bh = (float)beta, bl = (float)(beta - (double)bh);
     const int64_t e1 = (int64_t)ch.r1 * BD * BK;
+#pragma unroll 4
     for (int64_t e = (int64_t)ch.r0 * BD * BK + threadIdx.x; e < e1; e += blockDim.x)
         p[e] = df_sum(z[e], df_mul(p[e], bh, bl));
 }
@@ -674,21 +676,35 @@ __global__ void __launch_bounds__(BANK_THREADS) symv0_kernel(BatchDev B, MasDev 
         cnt = m.part_off[p + 1] - lo;
     };
     auto epi = [&](int i, const float *R, int cnt) {
+        constexpr int RPT = NB / (BANK_THREADS / BK);  // rows per thread: 6
         const int32_t p = ch.p0 + i, lo = m.part_off[p];
         const bool coarse = m.L > 1 && m.ccnt0[p] > 0;
         const int32_t cb = coarse ? m.cbase0[p] : 0;
-        for (int row = threadIdx.x >> 4; row < 3 * cnt; row += BANK_THREADS / BK) {
+        const int r0 = threadIdx.x >> 4, nrow = 3 * cnt;
+        // every gather of the thread's rows first, then the arithmetic
+        float cu[RPT];
+        float2 zo[RPT], rv[RPT];
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            const int row = r0 + j * (BANK_THREADS / BK);
+            cu[j] = 0.f;
+            zo[j] = rv[j] = make_float2(0.f, 0.f);
+            if (row >= nrow) continue;
             const int node = row / 3, c = row - 3 * node;
-            float y = bank_result(R, row, k);
-            if (coarse) y += u1[((int64_t)(cb + m.key0[lo + node]) * BD + c) * BK + k];
             const int64_t e = ((int64_t)lo * BD + row) * BK + k;
-            float2 val = df_mul(make_float2(y, 0.f), oh, ol);
-            if (ACC) val = df_sum(z[e], val);
+            if (coarse) cu[j] = u1[((int64_t)(cb + m.key0[lo + node]) * BD + c) * BK + k];
+            if (ACC) zo[j] = z[e];
+            if (DOT) rv[j] = rdot[e];
+        }
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            const int row = r0 + j * (BANK_THREADS / BK);
+            if (row >= nrow) continue;
+            const int64_t e = ((int64_t)lo * BD + row) * BK + k;
+            float2 val = df_mul(make_float2(bank_result(R, row, k) + cu[j], 0.f), oh, ol);
+            if (ACC) val = df_sum(zo[j], val);
             z[e] = val;
-            if (DOT) {
-                const float2 rv = rdot[e];
-                df_fma(dh, dl, rv.x, rv.y, val.x, val.y);
-            }
+            if (DOT) df_fma(dh, dl, rv[j].x, rv[j].y, val.x, val.y);
         }
     };
     if (!bank_pipeline<XT>(smem_raw, ch.p1 - ch.p0, job, epi, B.err)) return;

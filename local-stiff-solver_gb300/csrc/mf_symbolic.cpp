@@ -100,12 +100,24 @@ struct Nd {
         if (depth < 2) return {make(std::move(nodes), {})};
         std::vector<int32_t> count(depth + 1, 0);
         for (int32_t v : order) ++count[lvl[v]];
-        // median level, then the smallest level within two of it (not an end level)
+        // the separator level: the smallest level among those that leave at
+        // least 30% of the nodes on either side (balanced subtrees keep the
+        // tree shallow); the median level when no level does
+        const int64_t nn = (int64_t)nodes.size();
         int32_t med = 0, acc = 0;
-        while (med < depth && 2 * (acc + count[med]) < (int32_t)nodes.size()) acc += count[med++];
+        while (med < depth && 2 * (acc + count[med]) < (int32_t)nn) acc += count[med++];
         int32_t best = std::clamp(med, 1, depth - 1);
-        for (int32_t l = std::max(1, med - 2); l <= std::min(depth - 1, med + 2); ++l)
-            if (count[l] < count[best]) best = l;
+        int64_t below = 0;
+        int32_t best_cnt = -1;
+        for (int32_t l = 0; l <= depth; ++l) {
+            const int64_t above = nn - below - count[l];
+            if (l >= 1 && l <= depth - 1 && 10 * std::min(below, above) >= 3 * nn &&
+                (best_cnt < 0 || count[l] < best_cnt)) {
+                best = l;
+                best_cnt = count[l];
+            }
+            below += count[l];
+        }
         std::vector<int32_t> A, B, S;
         for (int32_t v : order) (lvl[v] < best ? A : (lvl[v] > best ? B : S)).push_back(v);
         // thin: a separator node without a neighbour in B joins A

@@ -32,6 +32,7 @@ struct MfView {
 
 __device__ __forceinline__ int find_front(const MfWork &w, int64_t cta)
 {
+    if (w.cta_item) return w.cta_item[cta];
     int lo = 0, hi = w.count - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -419,6 +420,11 @@ __global__ void mf_scatter_kernel(MfView v, const StiffDev S, const double *__re
     }
 }
 
+constexpr int NR_COLS = 32;    // output columns per GEMV CTA of the batched solve
+constexpr int NR_KROWS = 256;  // front rows per GEMV CTA of the batched solve
+
+__host__ __device__ __forceinline__ int nr_kchunks(int rows) { return (rows + NR_KROWS - 1) / NR_KROWS; }
+
 // ---- solve with NR right-hand sides at once (the batched PCG): t, w and x
 // hold NR values per entry, [entry][NR]; z is a double-float pair vector.
 // The fronts are read as double-float pairs (Fp: the FP64 factor split into
@@ -427,21 +433,19 @@ __global__ void mf_scatter_kernel(MfView v, const StiffDev S, const double *__re
 // relative per term): GB300 issues 64 FP32 FMAs per FP64 FMA, and the NR
 // right-hand sides make the solve arithmetic-bound.
 //
-// Forward, per level: one CTA per front sums the right-hand side and the
-// children's contributions into the front's vector (extend-add, children in
-// order), then CTAs of COLS output columns apply c = w_bnd - P w_own.
-// Backward, per level: CTAs of COLS output columns apply
-// x_own = F11^-1 (w_own - F12 x_bnd).  A GEMV CTA's 256 threads are COLS
-// columns x (256 / COLS) row slices (thread t: column t % COLS, rows
-// q = t / COLS + (256 / COLS) j), each keeping all NR sums of its column; the
-// slices meet in shared memory in slice order.  COLS = 32 for fronts of up to
-// 256 rows, else 8 (more CTAs per large front).  The solve vector in shared
-// memory is pairs, the 16-byte slots of row q XOR-swizzled by q % 8 so that
-// the rows a warp reads at once fall into different banks.
-
-constexpr int NR_SMALL_ROWS = 256;  // fronts with at most this many GEMV rows use 32-column CTAs
-
-__host__ __device__ __forceinline__ int nr_cols(int rows) { return rows <= NR_SMALL_ROWS ? 32 : 8; }
+// Forward, per level: CTAs of 16 entries sum the right-hand side and the
+// children's contributions into each front's vector (extend-add as a gather,
+// children in order), then GEMV CTAs apply c = w_bnd - P w_own.  Backward,
+// per level: GEMV CTAs apply x_own = F11^-1 (w_own - F12 x_bnd).  A GEMV CTA
+// takes 32 output columns and at most 256 of the front's rows: its 256
+// threads are 32 columns x 8 row slices (thread t: column t % 32, rows
+// t / 32 + 8 j), each keeping all NR sums of its column; the slices meet in
+// shared memory in slice order.  A front with more rows splits them over
+// several CTAs, whose partial sums meet in global memory: the last CTA of the
+// group to arrive adds them in row-chunk order (fixed-order, deterministic).
+// The solve vector in shared memory is pairs, the 16-byte slots of row q
+// XOR-swizzled by q % 8 so that the rows a warp reads at once fall into
+// different banks.
 
 __device__ __forceinline__ float2 split_pair(double d)
 {
@@ -456,19 +460,25 @@ __device__ __forceinline__ int swz(int q, int k)
     return q * NR + ((((k >> 1) ^ (q & 7))) << 1) + (k & 1);
 }
 
-// out[c][k] = sum_q Fn[q][col0 + c] xs[q][k] for the CTA's COLS columns
-// (c < ncol), q < nrow; handed over as a pair by out(c, k, hi, lo)
-template <int NR, int COLS, typename Out>
-__device__ __forceinline__ void nr_gemv(const float2 *__restrict__ Fn, int f, int col0, int ncol, int nrow,
-                                        const float2 *__restrict__ xs, float2 *__restrict__ red, Out out)
+struct NrScratch {
+    float2 *part;   // per CTA of a launch: NR_COLS x NR partial sums
+    unsigned *cnt;  // per group (first CTA of the group): arrivals
+};
+
+// res[c][k] = sum over the CTA's rows q0 .. q0 + nrow - 1 of Fn[q][col0 + c] xs[q - q0][k]
+// (c < ncol); res in shared memory, NR_COLS x NR pairs
+template <int NR>
+__device__ __forceinline__ void nr_gemv(const float2 *__restrict__ Fn, int f, int col0, int ncol, int q0, int nrow,
+                                        const float2 *__restrict__ xs, float2 *__restrict__ red,
+                                        float2 *__restrict__ res)
 {
-    constexpr int SL = 256 / COLS;
+    constexpr int COLS = NR_COLS, SL = 256 / NR_COLS;
     const int cl = threadIdx.x % COLS, ks = threadIdx.x / COLS;
     float ah[NR], al[NR];
 #pragma unroll
     for (int k = 0; k < NR; ++k) ah[k] = al[k] = 0.f;
     if (cl < ncol) {
-        const float2 *Fc = Fn + col0 + cl;
+        const float2 *Fc = Fn + (int64_t)q0 * f + col0 + cl;
         auto step = [&](const float2 a, int q) {
             const float4 *xv = reinterpret_cast<const float4 *>(xs + q * NR);
             const int sw = q & 7;
@@ -496,19 +506,50 @@ __device__ __forceinline__ void nr_gemv(const float2 *__restrict__ Fn, int f, in
     for (int kk = 0; kk < NR / 2; ++kk)
         dst[kk ^ (cl & 7)] = make_float4(ah[2 * kk], al[2 * kk], ah[2 * kk + 1], al[2 * kk + 1]);
     __syncthreads();
-    for (int o = threadIdx.x; o < COLS * NR; o += blockDim.x) {
+    for (int o = threadIdx.x; o < ncol * NR; o += blockDim.x) {
         const int c = o / NR, k = o % NR;
-        if (c >= ncol) continue;
         const int slot = (((k >> 1) ^ (c & 7)) << 1) | (k & 1);
         float h = 0.f, l = 0.f;
-#pragma unroll 8
+#pragma unroll
         for (int q = 0; q < SL; ++q) {
             const float2 v = red[(q * COLS + c) * NR + slot];
             df_add(h, l, v.x, v.y);
         }
-        out(c, k, h, l);
+        res[o] = make_float2(h, l);
     }
+    __syncthreads();
 }
+
+// Row-chunk kc of nkc: true in the CTA whose res then holds the group's total
+// (every CTA when nkc == 1, else the last of the group to arrive).
+template <int NR>
+__device__ __forceinline__ bool nr_combine(NrScratch sc, int kc, int nkc, float2 *__restrict__ res, int ncol)
+{
+    if (nkc == 1) return true;
+    __shared__ bool last;
+    float2 *mine = sc.part + (int64_t)blockIdx.x * NR_COLS * NR;
+    for (int o = threadIdx.x; o < ncol * NR; o += blockDim.x) mine[o] = res[o];
+    __threadfence();
+    __syncthreads();
+    const int64_t g = (int64_t)blockIdx.x - kc;  // the group's first CTA
+    if (threadIdx.x == 0) last = atomicAdd(sc.cnt + g, 1u) == (unsigned)(nkc - 1);
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    for (int o = threadIdx.x; o < ncol * NR; o += blockDim.x) {
+        float h = 0.f, l = 0.f;
+        for (int j = 0; j < nkc; ++j) {
+            const float2 v = __ldcg(sc.part + (g + j) * NR_COLS * NR + o);
+            df_add(h, l, v.x, v.y);
+        }
+        res[o] = make_float2(h, l);
+    }
+    if (threadIdx.x == 0) sc.cnt[g] = 0u;
+    __syncthreads();
+    return true;
+}
+
+constexpr size_t NR_SMEM = (size_t)(NR_KROWS * 16 + 256 * 16 + NR_COLS * 16) * sizeof(float2);  // NR = 16
 
 // forward, step 1: W_N = [t_own ; 0] + the children's contributions, every
 // entry gathered from its contributors (gptr/gsrc: per entry of W, the child
@@ -539,7 +580,7 @@ __global__ void __launch_bounds__(256) mf_fassemble_nr_kernel(MfView v, MfWork w
 // forward, step 2: W_N[bnd] -= P W_N[own] over the CTA's boundary columns
 template <int NR>
 __global__ void __launch_bounds__(256) mf_forward_nr_kernel(MfView v, MfWork w, const float2 *__restrict__ Fp,
-                                                            float2 *__restrict__ W, const int *sys_done,
+                                                            float2 *__restrict__ W, NrScratch sc, const int *sys_done,
                                                             const int32_t *front_sys)
 {
     extern __shared__ double sm[];
@@ -547,50 +588,51 @@ __global__ void __launch_bounds__(256) mf_forward_nr_kernel(MfView v, MfWork w, 
     const int32_t N = w.front[i];
     if (sys_done && sys_done[front_sys[N]]) return;
     const int s = v.s[N], u = v.u[N], f = s + u;
-    const int cols = nr_cols(s);
-    const int col0 = s + (int)(blockIdx.x - w.prefix[i]) * cols;
-    float2 *xs = reinterpret_cast<float2 *>(sm), *red = xs + (int64_t)s * NR;
+    const int nkc = nr_kchunks(s), local = (int)(blockIdx.x - w.prefix[i]);
+    const int kc = local % nkc, col0 = s + (local / nkc) * NR_COLS, ncol = min(NR_COLS, f - col0);
+    const int q0 = kc * NR_KROWS, nrow = min(NR_KROWS, s - q0);
+    float2 *xs = reinterpret_cast<float2 *>(sm), *red = xs + NR_KROWS * NR, *res = red + 256 * NR;
     float2 *Wn = W + (int64_t)v.woff[N] * NR;
-    for (int e = threadIdx.x; e < s * NR; e += blockDim.x) xs[swz<NR>(e / NR, e % NR)] = Wn[e];
+    for (int e = threadIdx.x; e < nrow * NR; e += blockDim.x) xs[swz<NR>(e / NR, e % NR)] = Wn[(int64_t)q0 * NR + e];
     __syncthreads();
-    auto out = [&](int c, int k, float h, float l) {
-        float2 &o = Wn[(int64_t)(col0 + c) * NR + k];
-        float oh = o.x, ol = o.y;
-        df_add(oh, ol, -h, -l);
-        o = make_float2(oh, ol);
-    };
-    const float2 *Fn = Fp + v.foff[N];
-    if (cols == 32) nr_gemv<NR, 32>(Fn, f, col0, min(32, f - col0), s, xs, red, out);
-    else nr_gemv<NR, 8>(Fn, f, col0, min(8, f - col0), s, xs, red, out);
+    nr_gemv<NR>(Fp + v.foff[N], f, col0, ncol, q0, nrow, xs, red, res);
+    if (!nr_combine<NR>(sc, kc, nkc, res, ncol)) return;
+    for (int o = threadIdx.x; o < ncol * NR; o += blockDim.x) {
+        float2 &t = Wn[(int64_t)col0 * NR + o];
+        float th = t.x, tl = t.y;
+        df_add(th, tl, -res[o].x, -res[o].y);
+        t = make_float2(th, tl);
+    }
 }
 
 template <int NR>
 __global__ void __launch_bounds__(256) mf_backward_nr_kernel(MfView v, MfWork w, const float2 *__restrict__ Fp,
                                                              const float2 *__restrict__ W, float2 *__restrict__ X,
-                                                             const int *sys_done, const int32_t *front_sys)
+                                                             NrScratch sc, const int *sys_done,
+                                                             const int32_t *front_sys)
 {
     extern __shared__ double sm[];
     const int i = find_front(w, blockIdx.x);
     const int32_t N = w.front[i];
     if (sys_done && sys_done[front_sys[N]]) return;
     const int s = v.s[N], u = v.u[N], f = s + u;
-    const int cols = nr_cols(f);
-    const int c0 = (int)(blockIdx.x - w.prefix[i]) * cols;
-    float2 *vec = reinterpret_cast<float2 *>(sm), *red = vec + (int64_t)f * NR;
+    const int nkc = nr_kchunks(f), local = (int)(blockIdx.x - w.prefix[i]);
+    const int kc = local % nkc, c0 = (local / nkc) * NR_COLS, ncol = min(NR_COLS, s - c0);
+    const int q0 = kc * NR_KROWS, nrow = min(NR_KROWS, f - q0);
+    float2 *vec = reinterpret_cast<float2 *>(sm), *red = vec + NR_KROWS * NR, *res = red + 256 * NR;
     const float2 *Wn = W + (int64_t)v.woff[N] * NR;
     const int32_t *bp = v.bnd_pos + v.bnd_off[N];
-#pragma unroll 4
-    for (int e = threadIdx.x; e < f * NR; e += blockDim.x) {
-        const int q = e / NR, k = e % NR;
-        vec[swz<NR>(q, k)] = q < s ? Wn[e] : X[(int64_t)bp[q - s] * NR + k];
+#pragma unroll 8
+    for (int e = threadIdx.x; e < nrow * NR; e += blockDim.x) {
+        const int r = e / NR, k = e % NR, q = q0 + r;
+        vec[swz<NR>(r, k)] = q < s ? Wn[(int64_t)q * NR + k] : X[(int64_t)bp[q - s] * NR + k];
     }
     __syncthreads();
     // x_own = F11^-1 (w_own - F12 x_bnd) = -(column c of the swept front) . vec
-    const int64_t xo = (int64_t)v.p0[N] + c0;
-    auto out = [&](int c, int k, float h, float l) { X[(xo + c) * NR + k] = make_float2(-h, -l); };
-    const float2 *Fn = Fp + v.foff[N];
-    if (cols == 32) nr_gemv<NR, 32>(Fn, f, c0, min(32, s - c0), f, vec, red, out);
-    else nr_gemv<NR, 8>(Fn, f, c0, min(8, s - c0), f, vec, red, out);
+    nr_gemv<NR>(Fp + v.foff[N], f, c0, ncol, q0, nrow, vec, red, res);
+    if (!nr_combine<NR>(sc, kc, nkc, res, ncol)) return;
+    float2 *xo = X + ((int64_t)v.p0[N] + c0) * NR;
+    for (int o = threadIdx.x; o < ncol * NR; o += blockDim.x) xo[o] = make_float2(-res[o].x, -res[o].y);
 }
 
 __global__ void split_pairs_kernel(int64_t n, const double *__restrict__ src, float2 *__restrict__ dst)
@@ -672,22 +714,25 @@ void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
     i64.insert(i64.end(), M.foff.begin(), M.foff.end());
     struct Pending {
         MfWork *w;
-        size_t fat, pat;
+        size_t fat, pat, cat;
     };
     std::vector<Pending> pend;
     levels_.resize(M.levels);
-    auto make = [&](MfWork &w, const std::vector<int32_t> &fronts, auto ctas_of) {
+    auto make = [&](MfWork &w, const std::vector<int32_t> &fronts, auto ctas_of, bool table = false) {
         w.count = (int32_t)fronts.size();
         const size_t fat = put32(fronts);
         const size_t pat = i64.size();
         int64_t acc = 0;
         i64.push_back(0);
-        for (int32_t id : fronts) {
-            acc += ctas_of(id);
+        std::vector<int32_t> item;
+        for (int32_t k = 0; k < (int32_t)fronts.size(); ++k) {
+            const int64_t c = ctas_of(fronts[k]);
+            acc += c;
             i64.push_back(acc);
+            if (table) item.insert(item.end(), (size_t)c, k);
         }
         w.ctas = acc;
-        pend.push_back({&w, fat, pat});
+        pend.push_back({&w, fat, pat, table ? put32(item) : SIZE_MAX});
     };
     auto F_of = [&](int32_t id) { return (int64_t)M.s[id] + M.u[id]; };
     for (int h = 0; h < M.levels; ++h) {
@@ -704,15 +749,13 @@ void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
         make(L.mirror, lv_large[h], [&](int32_t id) { return (F_of(id) * M.s[id] + 255) / 256; });
         make(L.fwd, lv_all[h], [&](int32_t id) { return std::max<int64_t>(1, (M.u[id] + PW - 1) / PW); });
         make(L.bwd, lv_all[h], [&](int32_t id) { return (int64_t)(M.s[id] + PW - 1) / PW; });
-        make(L.fasm_nr, lv_all[h], [&](int32_t id) { return (F_of(id) + 15) / 16; });
+        make(L.fasm_nr, lv_all[h], [&](int32_t id) { return (F_of(id) + 15) / 16; }, true);
         make(L.fwd_nr, lv_all[h], [&](int32_t id) {
-            const int c = nr_cols(M.s[id]);
-            return (int64_t)(M.u[id] + c - 1) / c;
-        });
+            return (int64_t)((M.u[id] + NR_COLS - 1) / NR_COLS) * nr_kchunks(M.s[id]);
+        }, true);
         make(L.bwd_nr, lv_all[h], [&](int32_t id) {
-            const int c = nr_cols(M.s[id] + M.u[id]);
-            return (int64_t)(M.s[id] + c - 1) / c;
-        });
+            return (int64_t)((M.s[id] + NR_COLS - 1) / NR_COLS) * nr_kchunks(M.s[id] + M.u[id]);
+        }, true);
         for (int32_t id : lv_large[h]) L.max_s_large = std::max(L.max_s_large, M.s[id]);
     }
     // extend-add as a gather: per entry of W, the child entries that add into it
@@ -743,6 +786,7 @@ void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
     for (const Pending &q : pend) {
         q.w->front = b32 + q.fat;
         q.w->prefix = b64 + q.pat;
+        q.w->cta_item = q.cat == SIZE_MAX ? nullptr : b32 + q.cat;
     }
     p0_ = b32 + a_p0;
     s_ = b32 + a_s;
@@ -863,28 +907,31 @@ void MfFactor::solve_batch(const StiffDev &S, const double *t, float2 *z, const 
     constexpr int NR = 16;
     const MfView v = make_view(p0_, s_, u_, woff_, bnd_off_, bnd_pos_, child_off_, child_, ea_map_, front_of_pos_,
                                pos2j_, j2pos_, poff_, foff_, sym_.j_base, sym_.npos);
-    const size_t red = (size_t)256 * NR * sizeof(float2);
-    const size_t fsmem = (size_t)sym_.max_s * NR * sizeof(float2) + red;
-    const size_t bsmem = (size_t)sym_.max_f * NR * sizeof(float2) + red;
-    if (fsmem > 227 * 1024 || bsmem > 227 * 1024)
-        fail(LSS_ERR_UNSUPPORTED, "a stiff subdomain front (" + std::to_string(sym_.max_f) +
-                                      " variables) is too large for the batched multifrontal solve");
-    raise_smem_limit((const void *)mf_forward_nr_kernel<NR>, fsmem);
-    raise_smem_limit((const void *)mf_backward_nr_kernel<NR>, bsmem);
+    const size_t smem = NR_SMEM;
+    raise_smem_limit((const void *)mf_forward_nr_kernel<NR>, smem);
+    raise_smem_limit((const void *)mf_backward_nr_kernel<NR>, smem);
     if (d_wb_.size() < (size_t)std::max<int64_t>(sym_.welems, 1) * NR) d_wb_.resize(std::max<int64_t>(sym_.welems, 1) * NR);
     if (d_xb_.size() < (size_t)std::max<int32_t>(sym_.npos, 1) * NR) d_xb_.resize(std::max<int32_t>(sym_.npos, 1) * NR);
+    int64_t maxctas = 1;
+    for (const Level &L : levels_) maxctas = std::max({maxctas, L.fwd_nr.ctas, L.bwd_nr.ctas});
+    if (d_nrpart_.size() < (size_t)maxctas * NR_COLS * NR) {
+        d_nrpart_.resize((size_t)maxctas * NR_COLS * NR);
+        d_nrcnt_.resize((size_t)maxctas);
+        d_nrcnt_.zero(st);
+    }
+    const NrScratch sc{d_nrpart_.data(), d_nrcnt_.data()};
     for (const Level &L : levels_) {
         mf_fassemble_nr_kernel<NR><<<(unsigned)L.fasm_nr.ctas, 256, 0, st>>>(v, L.fasm_nr, gptr_, gsrc_, t,
                                                                            d_wb_.data(), sys_done, front_sys);
         if (L.fwd_nr.ctas > 0)
-            mf_forward_nr_kernel<NR><<<(unsigned)L.fwd_nr.ctas, 256, fsmem, st>>>(v, L.fwd_nr, d_Fp_.data(),
-                                                                                d_wb_.data(), sys_done, front_sys);
+            mf_forward_nr_kernel<NR><<<(unsigned)L.fwd_nr.ctas, 256, smem, st>>>(v, L.fwd_nr, d_Fp_.data(),
+                                                                               d_wb_.data(), sc, sys_done, front_sys);
         LSS_LAUNCH_CHECK();
     }
     for (int h = (int)levels_.size() - 1; h >= 0; --h) {
         const Level &L = levels_[h];
-        mf_backward_nr_kernel<NR><<<(unsigned)L.bwd_nr.ctas, 256, bsmem, st>>>(v, L.bwd_nr, d_Fp_.data(), d_wb_.data(),
-                                                                             d_xb_.data(), sys_done, front_sys);
+        mf_backward_nr_kernel<NR><<<(unsigned)L.bwd_nr.ctas, 256, smem, st>>>(v, L.bwd_nr, d_Fp_.data(), d_wb_.data(),
+                                                                            d_xb_.data(), sc, sys_done, front_sys);
         LSS_LAUNCH_CHECK();
     }
     mf_scatter_nr_kernel<NR><<<(unsigned)(((int64_t)sym_.npos * NR + 255) / 256), 256, 0, st>>>(v, S, d_xb_.data(), z);

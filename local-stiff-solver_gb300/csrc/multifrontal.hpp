@@ -68,6 +68,7 @@ struct MfWork {
     int64_t ctas = 0;
     const int32_t *front = nullptr;
     const int64_t *prefix = nullptr;
+    const int32_t *cta_item = nullptr;  // optional: per CTA its index i (saves the search)
 };
 
 // The device side: symbolic arrays, front storage, solve vectors, and the
@@ -105,6 +106,8 @@ private:
     DBuf<double> d_F_, d_w_, d_x_, d_P_, d_D_;
     DBuf<float2> d_wb_, d_xb_;  // solve vectors of the batched solve (double-float pairs)
     DBuf<float2> d_Fp_;         // fronts as (hi, lo) FP32 pairs, for the batched solve
+    DBuf<float2> d_nrpart_;     // batched solve: per GEMV CTA partial sums of split fronts
+    DBuf<unsigned> d_nrcnt_;    // batched solve: arrival counters of split fronts
     const int32_t *p0_ = nullptr, *s_ = nullptr, *u_ = nullptr, *woff_ = nullptr, *bnd_off_ = nullptr,
                   *bnd_pos_ = nullptr, *child_off_ = nullptr, *child_ = nullptr, *ea_map_ = nullptr,
                   *front_of_pos_ = nullptr, *pos2j_ = nullptr, *j2pos_ = nullptr, *poff_ = nullptr;

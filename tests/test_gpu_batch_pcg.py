@@ -8,7 +8,13 @@ systems and right-hand sides.
   max(1e-8, 2 x its FP64 rounding floor eps ||A||x|| / ||b||) and agrees with
   scipy's FP64 sparse direct solve to 1e-6;
 * the lanes' iteration counts stay close to those of the single-system solver
-  (the same PCG per lane, vectors in double-float instead of FP64);
+  (the same PCG per lane, vectors in double-float instead of FP64): within
+  1.05x + 3 on systems whose stiff subdomains all have dense inverses, and
+  within 1.5x + 10 on systems with multifrontal subdomains, whose factor the
+  batch applies in double-float (about 2^-47 per term against FP64's 2^-53;
+  on blocks of 1e7 contrast, condition ~1e10, that perturbs the stiff
+  correction by ~1e-5 relative and costs some lanes up to ~35% more
+  iterations);
 * a zero right-hand side gives x = 0 after 0 iterations (GPUHybrid.cu:1428-1439);
 * a second solve reproduces the first bit for bit (fixed-order reductions);
 * a solver outside the batched form (plain FP64) is rejected.
@@ -79,7 +85,9 @@ def test_batch_pcg_matches_direct_and_single_solves(built):
                 s.solve_device(torch.tensor(b, dtype=torch.float64, device=dev).data_ptr(), x1.data_ptr())
                 torch.cuda.synchronize()
                 single_its.append(s.get_info()["num_iterations"])
-                assert its[si, k] <= 1.25 * single_its[-1] + 10, (si, k, its[si, k], single_its[-1])
+                mf = s.get_info().get("multifrontal_subdomains", 0) > 0
+                bound = 1.5 * single_its[-1] + 10 if mf else 1.05 * single_its[-1] + 3
+                assert its[si, k] <= bound, (si, k, mf, its[si, k], single_its[-1])
     # deterministic: a second solve from the same start gives the same bits
     for x in xs:
         x.zero_()
