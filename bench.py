@@ -653,7 +653,7 @@ def adjoint_measure(seed, local, steps, warmup, fd_budget_s, max_dirs=20):
         fwd.append(e0.elapsed_time(e2))
     info = sysm.solver.get_info()
     fwd_ms = statistics.mean(fwd)
-    syst = system(1e-10, "fp64", 4000)
+    syst = system(1e-12, "fp64", 8000)
     gt = step(syst).cpu().numpy()
 
     def loss(t):
@@ -683,7 +683,7 @@ def adjoint_measure(seed, local, steps, warmup, fd_budget_s, max_dirs=20):
             "factorize_ms": 1e3 * info.get("time_factorize", 0.0),
             "multifrontal_fronts": info.get("multifrontal_fronts"),
             "fd_check": {"directions": len(errs), "stencil": "5-point, relative step 1e-2",
-                         "solver": "fp64, relative tolerance 1e-10", "budget_s": fd_budget_s,
+                         "solver": "fp64, relative tolerance 1e-12", "budget_s": fd_budget_s,
                          "worst_rel_err": max(errs) if errs else None,
                          "median_rel_err": float(np.median(errs)) if errs else None},
             "mixed_1e-8_gradient_rel_err_vs_tight": float(np.linalg.norm(gm - gt) / np.linalg.norm(gt))}

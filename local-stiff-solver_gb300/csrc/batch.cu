@@ -154,7 +154,12 @@ __global__ void __launch_bounds__(256) spmm_alpha_kernel(BatchDev B, const float
     for (int32_t I = ch.r0 + w; I < ch.r1; I += 8) {
         const int32_t b = B.rows[I], len = B.rows[I + 1] - b;
         const float2 *__restrict__ v = B.vals_df + (int64_t)b * 9;
-        float sh[BD] = {0.f, 0.f, 0.f}, sl[BD] = {0.f, 0.f, 0.f};
+        // one double-float accumulator per (block slot u, row r): 3 U independent chains
+        float uh[U][BD], ul[U][BD];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int r = 0; r < BD; ++r) uh[u][r] = ul[u][r] = 0.f;
         row_blocks<U>(B, b, len, lane, [&](int l, const int32_t (&J)[U], const bool (&ok)[U]) {
             float2 x[U][BD], a[U][BD * BD];
 #pragma unroll
@@ -172,8 +177,16 @@ __global__ void __launch_bounds__(256) spmm_alpha_kernel(BatchDev B, const float
                 for (int r = 0; r < BD; ++r)
 #pragma unroll
                     for (int c = 0; c < BD; ++c)
-                        df_fma(sh[r], sl[r], a[u][r * BD + c].x, a[u][r * BD + c].y, x[u][c].x, x[u][c].y);
+                        df_fma(uh[u][r], ul[u][r], a[u][r * BD + c].x, a[u][r * BD + c].y, x[u][c].x, x[u][c].y);
         });
+        float sh[BD], sl[BD];
+#pragma unroll
+        for (int r = 0; r < BD; ++r) {
+            sh[r] = uh[0][r];
+            sl[r] = ul[0][r];
+#pragma unroll
+            for (int u = 1; u < U; ++u) df_add(sh[r], sl[r], uh[u][r], ul[u][r]);
+        }
 #pragma unroll
         for (int r = 0; r < BD; ++r) {
             const float bh = __shfl_xor_sync(FULL, sh[r], 16), bl = __shfl_xor_sync(FULL, sl[r], 16);
@@ -843,9 +856,9 @@ __global__ void __launch_bounds__(256) stiff_apply_kernel(StiffDev S, const doub
     const int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (j >= S.ndof_dense) return;
     const int32_t s = S.sub_of[j], o = S.off[s], m = S.off[s + 1] - o;
-    const double *row = S.inv + S.inv_off[s] + (int64_t)(j - o) * m;
+    const double *col = S.inv + S.inv_off[s] + (j - o);  // row j of the inverse (stored transposed)
     double acc = 0.0;
-    for (int32_t q = h; q < m; q += 2) acc += row[q] * t[(int64_t)(o + q) * BK + k];
+    for (int32_t q = h; q < m; q += 2) acc += col[(int64_t)q * m] * t[(int64_t)(o + q) * BK + k];
     acc += __shfl_xor_sync(FULL, acc, 16);
     if (h == 0) {
         const int64_t e = (int64_t)S.dofs[j] * BK + k;

@@ -327,81 +327,130 @@ __global__ void __launch_bounds__(256) mf_mirror_kernel(MfView v, MfWork w, doub
 
 // ---- solve
 
-// w_own = t[own] + children's contributions; c = w_bnd - P w_own for 32 outputs
-__global__ void __launch_bounds__(256) mf_forward_kernel(MfView v, MfWork w, const StiffDev S,
-                                                         const double *__restrict__ F, double *__restrict__ W,
-                                                         const int *done)
+constexpr int NR_COLS = 32;    // output columns per GEMV CTA of the solves
+constexpr int NR_KROWS = 256;  // front rows per GEMV CTA of the solves
+
+__host__ __device__ __forceinline__ int nr_kchunks(int rows) { return (rows + NR_KROWS - 1) / NR_KROWS; }
+
+// ---- solve with one right-hand side (FP64).  The same decomposition as the
+// batched solve below: per level, CTAs of 256 entries gather each front's
+// vector (right-hand side + the children's contributions, children in
+// order), then GEMV CTAs of 32 columns x at most 256 front rows (8 warps =
+// 8 row slices, lane = column), fronts with more rows split over several
+// CTAs whose partial sums the last CTA of the group adds in row-chunk order.
+
+constexpr int NR_COLS1 = 32;
+
+struct NrScratch1 {
+    double *part;   // per CTA of a launch: NR_COLS1 partial sums
+    unsigned *cnt;  // per group: arrivals
+};
+
+// res[c] = sum over the CTA's rows of Fn[q][col0 + c] xs[q - q0]; slices in order
+__device__ __forceinline__ void gemv1(const double *__restrict__ Fn, int f, int col0, int ncol, int q0, int nrow,
+                                      const double *__restrict__ xs, double *__restrict__ red,
+                                      double *__restrict__ res)
 {
-    if (done && *done) return;
-    extern __shared__ double sm[];
-    const int i = find_front(w, blockIdx.x);
-    const int32_t N = w.front[i];
-    const int s = v.s[N], u = v.u[N], f = s + u;
-    const int chunk = (int)(blockIdx.x - w.prefix[i]);
-    double *wown = sm, *wb = sm + s, *red = wb + PW;
-    const int r0 = s + chunk * PW;  // first front row of this CTA's outputs
-    for (int k = threadIdx.x; k < s; k += blockDim.x) wown[k] = S.t[v.pos2j[v.p0[N] + k]];
-    if (threadIdx.x < PW) wb[threadIdx.x] = 0.0;
-    __syncthreads();
-    for (int32_t ci = v.child_off[N]; ci < v.child_off[N + 1]; ++ci) {
-        const int32_t c = v.child[ci], uc = v.u[c];
-        const double *cw = W + v.woff[c] + v.s[c];
-        const int32_t *map = v.ea_map + v.bnd_off[c];
-        for (int e = threadIdx.x; e < uc; e += blockDim.x) {
-            const int m = map[e];
-            if (m < s) wown[m] += cw[e];
-            else if (m >= r0 && m < r0 + PW) wb[m - r0] += cw[e];
-        }
-        __syncthreads();
-    }
-    double *Wn = W + v.woff[N];
-    if (chunk == 0)
-        for (int k = threadIdx.x; k < s; k += blockDim.x) Wn[k] = wown[k];
-    if (u == 0) return;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int col = r0 + lane;
-    const double *Fn = F + v.foff[N];
+    const int cl = threadIdx.x & 31, ks = threadIdx.x >> 5;
     double acc = 0.0;
-    if (col < f)
-        for (int k = wid; k < s; k += 8) acc += Fn[(int64_t)k * f + col] * wown[k];
-    red[wid * 32 + lane] = acc;
-    __syncthreads();
-    if (wid == 0 && col < f) {
-        double sum = 0.0;
-        for (int q = 0; q < 8; ++q) sum += red[q * 32 + lane];
-        Wn[col] = wb[lane] - sum;
+    if (cl < ncol) {
+        const double *Fc = Fn + (int64_t)q0 * f + col0 + cl;
+#pragma unroll 8
+        for (int q = ks; q < nrow; q += 8) acc += __ldg(Fc + (int64_t)q * f) * xs[q];
     }
+    red[ks * 32 + cl] = acc;
+    __syncthreads();
+    if (threadIdx.x < ncol) {
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) sum += red[q * 32 + threadIdx.x];
+        res[threadIdx.x] = sum;
+    }
+    __syncthreads();
 }
 
-// x_own = -S[:, own]^T [w_own; x_bnd] for 32 outputs
-__global__ void __launch_bounds__(256) mf_backward_kernel(MfView v, MfWork w, const double *__restrict__ F,
-                                                          const double *__restrict__ W, double *__restrict__ X,
-                                                          const int *done)
+__device__ __forceinline__ bool combine1(NrScratch1 sc, int kc, int nkc, double *__restrict__ res, int ncol)
+{
+    if (nkc == 1) return true;
+    __shared__ bool last;
+    if (threadIdx.x < ncol) sc.part[(int64_t)blockIdx.x * NR_COLS1 + threadIdx.x] = res[threadIdx.x];
+    __threadfence();
+    __syncthreads();
+    const int64_t g = (int64_t)blockIdx.x - kc;
+    if (threadIdx.x == 0) last = atomicAdd(sc.cnt + g, 1u) == (unsigned)(nkc - 1);
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    if (threadIdx.x < ncol) {
+        double sum = 0.0;
+        for (int j = 0; j < nkc; ++j) sum += __ldcg(sc.part + (g + j) * NR_COLS1 + threadIdx.x);
+        res[threadIdx.x] = sum;
+    }
+    if (threadIdx.x == 0) sc.cnt[g] = 0u;
+    __syncthreads();
+    return true;
+}
+
+// forward, step 1: W_N = [t_own ; 0] + the children's contributions (gathered)
+__global__ void __launch_bounds__(256) mf_fassemble1_kernel(MfView v, MfWork w, const int32_t *__restrict__ gptr,
+                                                            const int32_t *__restrict__ gsrc, const StiffDev S,
+                                                            double *__restrict__ W, const int *done)
 {
     if (done && *done) return;
-    extern __shared__ double sm[];
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    const int s = v.s[N], f = s + v.u[N];
+    const int q = (int)(blockIdx.x - w.prefix[i]) * 256 + (int)threadIdx.x;
+    if (q >= f) return;
+    const int64_t e = (int64_t)v.woff[N] + q;
+    double acc = q < s ? S.t[v.pos2j[v.p0[N] + q]] : 0.0;
+    for (int32_t g = gptr[e]; g < gptr[e + 1]; ++g) acc += W[gsrc[g]];
+    W[e] = acc;
+}
+
+// forward, step 2: W_N[bnd] -= P W_N[own] over the CTA's boundary columns
+__global__ void __launch_bounds__(256) mf_forward_kernel(MfView v, MfWork w, const double *__restrict__ F,
+                                                         double *__restrict__ W, NrScratch1 sc, const int *done)
+{
+    if (done && *done) return;
+    __shared__ double xs[NR_KROWS], red[256], res[NR_COLS1];
     const int i = find_front(w, blockIdx.x);
     const int32_t N = w.front[i];
     const int s = v.s[N], u = v.u[N], f = s + u;
-    const int chunk = (int)(blockIdx.x - w.prefix[i]);
-    double *vec = sm, *red = sm + f;
+    const int nkc = nr_kchunks(s), local = (int)(blockIdx.x - w.prefix[i]);
+    const int kc = local % nkc, col0 = s + (local / nkc) * NR_COLS1, ncol = min(NR_COLS1, f - col0);
+    const int q0 = kc * NR_KROWS, nrow = min(NR_KROWS, s - q0);
+    double *Wn = W + v.woff[N];
+    for (int r = threadIdx.x; r < nrow; r += blockDim.x) xs[r] = Wn[q0 + r];
+    __syncthreads();
+    gemv1(F + v.foff[N], f, col0, ncol, q0, nrow, xs, red, res);
+    if (!combine1(sc, kc, nkc, res, ncol)) return;
+    if (threadIdx.x < ncol) Wn[col0 + threadIdx.x] -= res[threadIdx.x];
+}
+
+// backward: x_own = F11^-1 (w_own - F12 x_bnd) = -(columns of the swept front) . [w_own; x_bnd]
+__global__ void __launch_bounds__(256) mf_backward_kernel(MfView v, MfWork w, const double *__restrict__ F,
+                                                          const double *__restrict__ W, double *__restrict__ X,
+                                                          NrScratch1 sc, const int *done)
+{
+    if (done && *done) return;
+    __shared__ double vec[NR_KROWS], red[256], res[NR_COLS1];
+    const int i = find_front(w, blockIdx.x);
+    const int32_t N = w.front[i];
+    const int s = v.s[N], u = v.u[N], f = s + u;
+    const int nkc = nr_kchunks(f), local = (int)(blockIdx.x - w.prefix[i]);
+    const int kc = local % nkc, c0 = (local / nkc) * NR_COLS1, ncol = min(NR_COLS1, s - c0);
+    const int q0 = kc * NR_KROWS, nrow = min(NR_KROWS, f - q0);
     const double *Wn = W + v.woff[N];
     const int32_t *bp = v.bnd_pos + v.bnd_off[N];
-    for (int k = threadIdx.x; k < f; k += blockDim.x) vec[k] = k < s ? Wn[k] : X[bp[k - s]];
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int c = chunk * PW + lane;
-    const double *Fn = F + v.foff[N];
-    double acc = 0.0;
-    if (c < s)
-        for (int k = wid; k < f; k += 8) acc += Fn[(int64_t)k * f + c] * vec[k];
-    red[wid * 32 + lane] = acc;
-    __syncthreads();
-    if (wid == 0 && c < s) {
-        double sum = 0.0;
-        for (int q = 0; q < 8; ++q) sum += red[q * 32 + lane];
-        X[v.p0[N] + c] = -sum;
+    for (int r = threadIdx.x; r < nrow; r += blockDim.x) {
+        const int q = q0 + r;
+        vec[r] = q < s ? Wn[q] : X[bp[q - s]];
     }
+    __syncthreads();
+    gemv1(F + v.foff[N], f, c0, ncol, q0, nrow, vec, red, res);
+    if (!combine1(sc, kc, nkc, res, ncol)) return;
+    if (threadIdx.x < ncol) X[v.p0[N] + c0 + threadIdx.x] = -res[threadIdx.x];
 }
 
 __global__ void mf_scatter_kernel(MfView v, const StiffDev S, const double *__restrict__ X, double *__restrict__ z,
@@ -419,11 +468,6 @@ __global__ void mf_scatter_kernel(MfView v, const StiffDev S, const double *__re
         if (z_lo) z_lo[d] = (float)(nz - (double)h);
     }
 }
-
-constexpr int NR_COLS = 32;    // output columns per GEMV CTA of the batched solve
-constexpr int NR_KROWS = 256;  // front rows per GEMV CTA of the batched solve
-
-__host__ __device__ __forceinline__ int nr_kchunks(int rows) { return (rows + NR_KROWS - 1) / NR_KROWS; }
 
 // ---- solve with NR right-hand sides at once (the batched PCG): t, w and x
 // hold NR values per entry, [entry][NR]; z is a double-float pair vector.
@@ -667,10 +711,6 @@ int64_t MfFactor::bytes() const
 
 void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
 {
-    // one CTA holds a front's solve vector in shared memory (227 KB per CTA)
-    if ((size_t)(sym.max_f + 8 * 32) * sizeof(double) > 227 * 1024)
-        fail(LSS_ERR_UNSUPPORTED, "a stiff subdomain's top separator front (" + std::to_string(sym.max_f) +
-                                      " variables) exceeds the multifrontal solve's shared-memory limit");
     sym_ = sym;
     levels_.clear();
     if (sym_.nfront == 0) {
@@ -750,6 +790,7 @@ void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
         make(L.fwd, lv_all[h], [&](int32_t id) { return std::max<int64_t>(1, (M.u[id] + PW - 1) / PW); });
         make(L.bwd, lv_all[h], [&](int32_t id) { return (int64_t)(M.s[id] + PW - 1) / PW; });
         make(L.fasm_nr, lv_all[h], [&](int32_t id) { return (F_of(id) + 15) / 16; }, true);
+        make(L.fasm1, lv_all[h], [&](int32_t id) { return (F_of(id) + 255) / 256; }, true);
         make(L.fwd_nr, lv_all[h], [&](int32_t id) {
             return (int64_t)((M.u[id] + NR_COLS - 1) / NR_COLS) * nr_kchunks(M.s[id]);
         }, true);
@@ -803,12 +844,14 @@ void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
     poff_ = b32 + a_po;
     foff_ = b64 + a_fo;
     // shared memory of the solve kernels, set here: solve() runs inside graph captures
-    const size_t fsmem = (size_t)(M.max_s + PW + 8 * 32) * sizeof(double);
-    const size_t bsmem = (size_t)(M.max_f + 8 * 32) * sizeof(double);
-    raise_smem_limit((const void *)mf_forward_kernel, fsmem);
-    raise_smem_limit((const void *)mf_backward_kernel, bsmem);
     d_F_.resize(M.elems);
     d_w_.resize(std::max<int64_t>(M.welems, 1));
+    // scratch of the split fronts' partial sums (both solves), zeroed counters
+    int64_t maxctas = 1;
+    for (const Level &L : levels_) maxctas = std::max({maxctas, L.fwd_nr.ctas, L.bwd_nr.ctas});
+    d_part1_.resize((size_t)maxctas * NR_COLS1);
+    d_nrcnt_.resize((size_t)maxctas);
+    d_nrcnt_.zero(st);
     d_x_.resize(std::max<int32_t>(M.npos, 1));
     d_P_.resize(std::max<int64_t>(pmax, 1));
     d_D_.resize(std::max<size_t>(dmax, 1) * PW * PW);
@@ -874,16 +917,18 @@ void MfFactor::solve(const StiffDev &S, double *z, float *z32, float *z_lo, cons
     if (sym_.nfront == 0) return;
     const MfView v = make_view(p0_, s_, u_, woff_, bnd_off_, bnd_pos_, child_off_, child_, ea_map_, front_of_pos_,
                                pos2j_, j2pos_, poff_, foff_, sym_.j_base, sym_.npos);
-    const size_t fsmem = (size_t)(sym_.max_s + PW + 8 * 32) * sizeof(double);
-    const size_t bsmem = (size_t)(sym_.max_f + 8 * 32) * sizeof(double);
+    const NrScratch1 sc{d_part1_.data(), d_nrcnt_.data()};
     for (const Level &L : levels_) {
-        mf_forward_kernel<<<(unsigned)L.fwd.ctas, 256, fsmem, st>>>(v, L.fwd, S, d_F_.data(), d_w_.data(), done);
+        mf_fassemble1_kernel<<<(unsigned)L.fasm1.ctas, 256, 0, st>>>(v, L.fasm1, gptr_, gsrc_, S, d_w_.data(), done);
+        if (L.fwd_nr.ctas > 0)
+            mf_forward_kernel<<<(unsigned)L.fwd_nr.ctas, 256, 0, st>>>(v, L.fwd_nr, d_F_.data(), d_w_.data(), sc,
+                                                                       done);
         LSS_LAUNCH_CHECK();
     }
     for (int h = (int)levels_.size() - 1; h >= 0; --h) {
         const Level &L = levels_[h];
-        mf_backward_kernel<<<(unsigned)L.bwd.ctas, 256, bsmem, st>>>(v, L.bwd, d_F_.data(), d_w_.data(), d_x_.data(),
-                                                                      done);
+        mf_backward_kernel<<<(unsigned)L.bwd_nr.ctas, 256, 0, st>>>(v, L.bwd_nr, d_F_.data(), d_w_.data(),
+                                                                    d_x_.data(), sc, done);
         LSS_LAUNCH_CHECK();
     }
     mf_scatter_kernel<<<(unsigned)((sym_.npos + 255) / 256), 256, 0, st>>>(v, S, d_x_.data(), z, z32, z_lo, done);
@@ -892,6 +937,9 @@ void MfFactor::solve(const StiffDev &S, double *z, float *z32, float *z_lo, cons
 
 void MfFactor::make_pairs(cudaStream_t st)
 {
+    int64_t maxctas = 1;
+    for (const Level &L : levels_) maxctas = std::max({maxctas, L.fwd_nr.ctas, L.bwd_nr.ctas});
+    d_nrpart_.resize((size_t)maxctas * NR_COLS * 16);
     d_Fp_.resize(std::max<int64_t>(sym_.elems, 1));
     if (sym_.elems > 0) {
         split_pairs_kernel<<<(unsigned)((sym_.elems + 255) / 256), 256, 0, st>>>(sym_.elems, d_F_.data(), d_Fp_.data());
@@ -914,11 +962,8 @@ void MfFactor::solve_batch(const StiffDev &S, const double *t, float2 *z, const 
     if (d_xb_.size() < (size_t)std::max<int32_t>(sym_.npos, 1) * NR) d_xb_.resize(std::max<int32_t>(sym_.npos, 1) * NR);
     int64_t maxctas = 1;
     for (const Level &L : levels_) maxctas = std::max({maxctas, L.fwd_nr.ctas, L.bwd_nr.ctas});
-    if (d_nrpart_.size() < (size_t)maxctas * NR_COLS * NR) {
-        d_nrpart_.resize((size_t)maxctas * NR_COLS * NR);
-        d_nrcnt_.resize((size_t)maxctas);
-        d_nrcnt_.zero(st);
-    }
+    if (d_nrpart_.size() < (size_t)maxctas * NR_COLS * NR)
+        fail(LSS_ERR_INTERNAL, "batched multifrontal solve before make_pairs");
     const NrScratch sc{d_nrpart_.data(), d_nrcnt_.data()};
     for (const Level &L : levels_) {
         mf_fassemble_nr_kernel<NR><<<(unsigned)L.fasm_nr.ctas, 256, 0, st>>>(v, L.fasm_nr, gptr_, gsrc_, t,

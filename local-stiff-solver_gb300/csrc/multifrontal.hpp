@@ -96,7 +96,7 @@ public:
 
 private:
     struct Level {
-        MfWork ea, small, diag, panel, update, write, mirror, fwd, bwd, fasm_nr, fwd_nr, bwd_nr;
+        MfWork ea, small, diag, panel, update, write, mirror, fwd, bwd, fasm_nr, fwd_nr, bwd_nr, fasm1;
         int32_t max_s_large = 0;
     };
     MfSymbolic sym_;
@@ -107,7 +107,8 @@ private:
     DBuf<float2> d_wb_, d_xb_;  // solve vectors of the batched solve (double-float pairs)
     DBuf<float2> d_Fp_;         // fronts as (hi, lo) FP32 pairs, for the batched solve
     DBuf<float2> d_nrpart_;     // batched solve: per GEMV CTA partial sums of split fronts
-    DBuf<unsigned> d_nrcnt_;    // batched solve: arrival counters of split fronts
+    DBuf<unsigned> d_nrcnt_;    // arrival counters of split fronts (both solves)
+    DBuf<double> d_part1_;      // single right-hand-side solve: per GEMV CTA partial sums
     const int32_t *p0_ = nullptr, *s_ = nullptr, *u_ = nullptr, *woff_ = nullptr, *bnd_off_ = nullptr,
                   *bnd_pos_ = nullptr, *child_off_ = nullptr, *child_ = nullptr, *ea_map_ = nullptr,
                   *front_of_pos_ = nullptr, *pos2j_ = nullptr, *j2pos_ = nullptr, *poff_ = nullptr;

@@ -95,11 +95,12 @@ __global__ void __launch_bounds__(256) invert_small_kernel(const int32_t *__rest
     }
     __syncthreads();
     sweep_invert_small(S, ld, m, col, scol, bad);
+    // stored transposed (column-major): thread j of the apply reads row j as a column
     for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
         const int r = idx / m, c = idx % m;
         const double val = -S[r * ld + c];
         if (!isfinite(val)) atomicOr(bad, 8);
-        g[(int64_t)r * m + c] = val;
+        g[(int64_t)c * m + r] = val;
     }
 }
 
@@ -130,29 +131,29 @@ __global__ void __launch_bounds__(256) gather_kernel(BsrDev A, StiffDev S, const
     S.t[j] = t;
 }
 
+// z_S += Inv t over the dense subdomains: one thread per stiff DOF row j,
+// the row read as column j of the transposed storage (consecutive threads,
+// consecutive addresses), the sum in column order -- no FP64 shuffles
 template <typename VT>
 __global__ void __launch_bounds__(256) apply_kernel(StiffDev S, const VT *__restrict__ inv, double *__restrict__ z,
                                                     float *__restrict__ z32, float *__restrict__ z_lo, const int *done)
 {
     if (done && *done) return;
-    const int lane = threadIdx.x & 31;
-    const int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= S.ndof_dense) return;
     const int32_t s = S.sub_of[j], o = S.off[s], m = S.off[s + 1] - o;
-    const VT *row = inv + S.inv_off[s] + (int64_t)(j - o) * m;
-    const double *t = S.t + o;
+    const VT *__restrict__ col = inv + S.inv_off[s] + (j - o);
+    const double *__restrict__ t = S.t + o;
     double acc = 0.0;
-    for (int32_t k = lane; k < m; k += 32) acc += (double)row[k] * t[k];
-    acc = warp_sum(acc);
-    if (lane == 0) {
-        const int32_t d = S.dofs[j];
-        const double nz = z[d] + acc;
-        z[d] = nz;
-        if (z32) {
-            const float h = (float)nz;
-            z32[d] = h;
-            if (z_lo) z_lo[d] = (float)(nz - (double)h);
-        }
+#pragma unroll 4
+    for (int32_t q = 0; q < m; ++q) acc += (double)col[(int64_t)q * m] * t[q];
+    const int32_t d = S.dofs[j];
+    const double nz = z[d] + acc;
+    z[d] = nz;
+    if (z32) {
+        const float h = (float)nz;
+        z32[d] = h;
+        if (z_lo) z_lo[d] = (float)(nz - (double)h);
     }
 }
 
@@ -223,7 +224,7 @@ void launch_stiff_apply(const StiffDev &S, bool fp32, double *z, const int *done
                         float *z_lo)
 {
     if (S.ndof_dense == 0) return;
-    const int grid = (int)(((int64_t)S.ndof_dense * 32 + 255) / 256);
+    const int grid = (int)(((int64_t)S.ndof_dense + 255) / 256);
     if (fp32) apply_kernel<float><<<grid, 256, 0, s>>>(S, S.inv32, z, z32, z_lo, done);
     else apply_kernel<double><<<grid, 256, 0, s>>>(S, S.inv, z, z32, z_lo, done);
     LSS_LAUNCH_CHECK();
