@@ -13,6 +13,7 @@
 // level (root first), one scatter; each output is a fixed-order dot product
 // over a column of the front (coalesced across the 32 outputs of a warp).
 #include <algorithm>
+#include <utility>
 
 #include "device_common.cuh"
 #include "multifrontal.hpp"
@@ -327,6 +328,33 @@ __global__ void __launch_bounds__(256) mf_mirror_kernel(MfView v, MfWork w, doub
 
 // ---- solve
 
+// Programmatic dependent launch across the solve's per-level kernels: each
+// lets the next launch be dispatched at once and waits for the previous
+// grid's completion (and memory) before it reads anything -- the launches'
+// latency overlaps the previous level's tail instead of adding to it.
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                Args &&...args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    LSS_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
+
 constexpr int NR_COLS = 32;    // output columns per GEMV CTA of the solves
 constexpr int NR_KROWS = 256;  // front rows per GEMV CTA of the solves
 
@@ -396,6 +424,7 @@ __global__ void __launch_bounds__(256) mf_fassemble1_kernel(MfView v, MfWork w, 
                                                             const int32_t *__restrict__ gsrc, const StiffDev S,
                                                             double *__restrict__ W, const int *done)
 {
+    pdl_enter();
     if (done && *done) return;
     const int i = find_front(w, blockIdx.x);
     const int32_t N = w.front[i];
@@ -412,6 +441,7 @@ __global__ void __launch_bounds__(256) mf_fassemble1_kernel(MfView v, MfWork w, 
 __global__ void __launch_bounds__(256) mf_forward_kernel(MfView v, MfWork w, const double *__restrict__ F,
                                                          double *__restrict__ W, NrScratch1 sc, const int *done)
 {
+    pdl_enter();
     if (done && *done) return;
     __shared__ double xs[NR_KROWS], red[256], res[NR_COLS1];
     const int i = find_front(w, blockIdx.x);
@@ -433,6 +463,7 @@ __global__ void __launch_bounds__(256) mf_backward_kernel(MfView v, MfWork w, co
                                                           const double *__restrict__ W, double *__restrict__ X,
                                                           NrScratch1 sc, const int *done)
 {
+    pdl_enter();
     if (done && *done) return;
     __shared__ double vec[NR_KROWS], red[256], res[NR_COLS1];
     const int i = find_front(w, blockIdx.x);
@@ -456,6 +487,7 @@ __global__ void __launch_bounds__(256) mf_backward_kernel(MfView v, MfWork w, co
 __global__ void mf_scatter_kernel(MfView v, const StiffDev S, const double *__restrict__ X, double *__restrict__ z,
                                   float *__restrict__ z32, float *__restrict__ z_lo, const int *done)
 {
+    pdl_enter();
     if (done && *done) return;
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= v.npos) return;
@@ -605,6 +637,7 @@ __global__ void __launch_bounds__(256) mf_fassemble_nr_kernel(MfView v, MfWork w
                                                               const double *__restrict__ T, float2 *__restrict__ W,
                                                               const int *sys_done, const int32_t *front_sys)
 {
+    pdl_enter();
     static_assert(NR == 16, "16 entries x 16 right-hand sides per CTA");
     const int i = find_front(w, blockIdx.x);
     const int32_t N = w.front[i];
@@ -627,6 +660,7 @@ __global__ void __launch_bounds__(256) mf_forward_nr_kernel(MfView v, MfWork w, 
                                                             float2 *__restrict__ W, NrScratch sc, const int *sys_done,
                                                             const int32_t *front_sys)
 {
+    pdl_enter();
     extern __shared__ double sm[];
     const int i = find_front(w, blockIdx.x);
     const int32_t N = w.front[i];
@@ -655,6 +689,7 @@ __global__ void __launch_bounds__(256) mf_backward_nr_kernel(MfView v, MfWork w,
                                                              NrScratch sc, const int *sys_done,
                                                              const int32_t *front_sys)
 {
+    pdl_enter();
     extern __shared__ double sm[];
     const int i = find_front(w, blockIdx.x);
     const int32_t N = w.front[i];
@@ -689,6 +724,7 @@ template <int NR>
 __global__ void mf_scatter_nr_kernel(MfView v, const StiffDev S, const float2 *__restrict__ X,
                                      float2 *__restrict__ z)
 {
+    pdl_enter();
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)v.npos * NR) return;
     const int64_t p = t / NR;
@@ -919,19 +955,21 @@ void MfFactor::solve(const StiffDev &S, double *z, float *z32, float *z_lo, cons
                                pos2j_, j2pos_, poff_, foff_, sym_.j_base, sym_.npos);
     const NrScratch1 sc{d_part1_.data(), d_nrcnt_.data()};
     for (const Level &L : levels_) {
-        mf_fassemble1_kernel<<<(unsigned)L.fasm1.ctas, 256, 0, st>>>(v, L.fasm1, gptr_, gsrc_, S, d_w_.data(), done);
+        launch_pdl(mf_fassemble1_kernel, (unsigned)L.fasm1.ctas, 256, 0, st, v, L.fasm1, gptr_, gsrc_, S,
+                   d_w_.data(), done);
         if (L.fwd_nr.ctas > 0)
-            mf_forward_kernel<<<(unsigned)L.fwd_nr.ctas, 256, 0, st>>>(v, L.fwd_nr, d_F_.data(), d_w_.data(), sc,
-                                                                       done);
+            launch_pdl(mf_forward_kernel, (unsigned)L.fwd_nr.ctas, 256, 0, st, v, L.fwd_nr,
+                       (const double *)d_F_.data(), d_w_.data(), sc, done);
         LSS_LAUNCH_CHECK();
     }
     for (int h = (int)levels_.size() - 1; h >= 0; --h) {
         const Level &L = levels_[h];
-        mf_backward_kernel<<<(unsigned)L.bwd_nr.ctas, 256, 0, st>>>(v, L.bwd_nr, d_F_.data(), d_w_.data(),
-                                                                    d_x_.data(), sc, done);
+        launch_pdl(mf_backward_kernel, (unsigned)L.bwd_nr.ctas, 256, 0, st, v, L.bwd_nr, (const double *)d_F_.data(),
+                   (const double *)d_w_.data(), d_x_.data(), sc, done);
         LSS_LAUNCH_CHECK();
     }
-    mf_scatter_kernel<<<(unsigned)((sym_.npos + 255) / 256), 256, 0, st>>>(v, S, d_x_.data(), z, z32, z_lo, done);
+    launch_pdl(mf_scatter_kernel, (unsigned)((sym_.npos + 255) / 256), 256, 0, st, v, S, (const double *)d_x_.data(),
+               z, z32, z_lo, done);
     LSS_LAUNCH_CHECK();
 }
 
@@ -966,20 +1004,21 @@ void MfFactor::solve_batch(const StiffDev &S, const double *t, float2 *z, const 
         fail(LSS_ERR_INTERNAL, "batched multifrontal solve before make_pairs");
     const NrScratch sc{d_nrpart_.data(), d_nrcnt_.data()};
     for (const Level &L : levels_) {
-        mf_fassemble_nr_kernel<NR><<<(unsigned)L.fasm_nr.ctas, 256, 0, st>>>(v, L.fasm_nr, gptr_, gsrc_, t,
-                                                                           d_wb_.data(), sys_done, front_sys);
+        launch_pdl(mf_fassemble_nr_kernel<NR>, (unsigned)L.fasm_nr.ctas, 256, 0, st, v, L.fasm_nr, gptr_, gsrc_, t,
+                   d_wb_.data(), sys_done, front_sys);
         if (L.fwd_nr.ctas > 0)
-            mf_forward_nr_kernel<NR><<<(unsigned)L.fwd_nr.ctas, 256, smem, st>>>(v, L.fwd_nr, d_Fp_.data(),
-                                                                               d_wb_.data(), sc, sys_done, front_sys);
+            launch_pdl(mf_forward_nr_kernel<NR>, (unsigned)L.fwd_nr.ctas, 256, smem, st, v, L.fwd_nr,
+                       (const float2 *)d_Fp_.data(), d_wb_.data(), sc, sys_done, front_sys);
         LSS_LAUNCH_CHECK();
     }
     for (int h = (int)levels_.size() - 1; h >= 0; --h) {
         const Level &L = levels_[h];
-        mf_backward_nr_kernel<NR><<<(unsigned)L.bwd_nr.ctas, 256, smem, st>>>(v, L.bwd_nr, d_Fp_.data(), d_wb_.data(),
-                                                                            d_xb_.data(), sc, sys_done, front_sys);
+        launch_pdl(mf_backward_nr_kernel<NR>, (unsigned)L.bwd_nr.ctas, 256, smem, st, v, L.bwd_nr,
+                   (const float2 *)d_Fp_.data(), (const float2 *)d_wb_.data(), d_xb_.data(), sc, sys_done, front_sys);
         LSS_LAUNCH_CHECK();
     }
-    mf_scatter_nr_kernel<NR><<<(unsigned)(((int64_t)sym_.npos * NR + 255) / 256), 256, 0, st>>>(v, S, d_xb_.data(), z);
+    launch_pdl(mf_scatter_nr_kernel<NR>, (unsigned)(((int64_t)sym_.npos * NR + 255) / 256), 256, 0, st, v, S,
+               (const float2 *)d_xb_.data(), z);
     LSS_LAUNCH_CHECK();
 }
 
