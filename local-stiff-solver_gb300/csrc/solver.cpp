@@ -164,6 +164,13 @@ void HybridSolver::analyze(int32_t n, int64_t nnz, const int32_t *outer, const i
     invalidate_graph();
     factorized_ = false;
     have_pattern_ = false;
+    // a new pattern: nothing of the previous pattern's stiff layout is reusable
+    decomp_sel_.clear();
+    decomp_max_ = -1;
+    decomp_subs_.clear();
+    h_sdofs_.clear();
+    h_soff_.assign(1, 0);
+    mf_.reset();
     pat_ = analyze_pattern(n, nnz, outer, inner, p_.block_size, p_.partition_threads);
     h_outer_.assign(outer, outer + n + 1);
     h_inner_.assign(inner, inner + nnz);
@@ -328,7 +335,8 @@ void HybridSolver::factorize_common()
     stats_["time_mas_setup"] = secs(t4);
     setup_precise_rows();
     ensure_vectors();
-    d_csc_.release();
+    // d_csc_ stays allocated: the next factorization of this pattern (Newton
+    // steps) reuses it instead of a cudaMalloc / cudaFree pair of nnz doubles
     factorized_ = true;
     if (!lanes_tuned_) autotune_spmv();
     auto t5 = clk::now();
@@ -355,6 +363,7 @@ void HybridSolver::select_stiff(const CscView &A)
         return;
     }
     std::vector<int32_t> sel;
+    auto tsel0 = clk::now();
     if (p_.select_l1) {
         const int32_t n = A.n;
         DBuf<double> rn(n);
@@ -399,6 +408,8 @@ void HybridSolver::select_stiff(const CscView &A)
             if (v >= 0 && v < A.n) sel.push_back(v);
     }
     gmm_sel_ = sel;
+    stats_["time_selection_gmm"] = secs(tsel0);
+    auto tsel1 = clk::now();
     // GPUHybrid.cu:221-238
     if (p_.decompose) {
         const int32_t m = (int32_t)sel.size();
@@ -420,12 +431,27 @@ void HybridSolver::select_stiff(const CscView &A)
         stats_["filter_too_large"] = fc.too_large;
         stats_["filter_not_poorly_conditioned"] = fc.not_poorly_conditioned;
     }
+    stats_["time_selection_filter"] = secs(tsel1);
+    auto tsel2 = clk::now();
     if (p_.expand && !sel.empty()) sel = expand_subdomains(A, sel);
+    stats_["time_selection_expand"] = secs(tsel2);
     if (sel.empty()) return;
     // Without decompose_subdomains the reference factors one block with every
     // selected DOF; its inverse is block diagonal over the connected components,
     // so factoring the components separately applies the same operator.
-    subs_ = decompose_subdomains(A, sel, p_.decompose ? (int64_t)p_.max_sub : INT64_MAX);
+    auto tsel3 = clk::now();
+    // the components depend only on the pattern and the set: a factorization
+    // that selects the same set as the previous one (same pattern) reuses them
+    const int64_t max_size = p_.decompose ? (int64_t)p_.max_sub : INT64_MAX;
+    if (sel == decomp_sel_ && max_size == decomp_max_) {
+        subs_ = decomp_subs_;
+    } else {
+        subs_ = decompose_subdomains(A, sel, max_size);
+        decomp_sel_ = sel;
+        decomp_max_ = max_size;
+        decomp_subs_ = subs_;
+    }
+    stats_["time_selection_decompose"] = secs(tsel3);
 }
 
 // MASSolver's bad-DOF selections (MASSolver.cu:266-290 with
@@ -488,23 +514,9 @@ void HybridSolver::op_row_scores(double *diag, double *offmax, double *l1)
 
 void HybridSolver::setup_stiff()
 {
-    stiff_ = StiffDev();
-    d_sdofs_.release();
-    d_ssub_.release();
-    d_soff_.release();
-    d_sinvoff_.release();
-    d_sinv_.release();
-    d_sinv32_.release();
-    d_st_.release();
-    mf_ = std::make_unique<MfFactor>();
-    h_sdofs_.clear();
-    h_soff_.assign(1, 0);
-    h_sinvoff_.clear();
-    ndense_ = 0;
-    inv_total_ = 0;
-    if (subs_.empty()) return;
     const int bd = pat_.bd;
-    // subdomains with a dense inverse first, then those of the multifrontal factor
+    // the layout: subdomains with a dense inverse first, then those of the
+    // multifrontal factor; DOFs permuted and ascending within each subdomain
     std::vector<int32_t> order;
     for (int pass = 0; pass < 2; ++pass)
         for (size_t s = 0; s < subs_.size(); ++s)
@@ -531,31 +543,58 @@ void HybridSolver::setup_stiff()
             ++ndense;
         }
     }
-    d_sdofs_.upload(dofs, stream_);
-    d_ssub_.upload(sub_of, stream_);
-    d_soff_.upload(off, stream_);
-    d_sinvoff_.upload(inv_off, stream_);
-    d_sinv_.resize(std::max<int64_t>(inv_total, 1));
+    // the same stiff subdomains as the previous factorization (repeated
+    // factorizations of one pattern, e.g. Newton steps): the device layout,
+    // the multifrontal plan and its storage are kept, only the numbers change
+    const bool same = !subs_.empty() && mf_ && dofs == h_sdofs_ && off == h_soff_ && ndense == ndense_;
+    if (!same) {
+        stiff_ = StiffDev();
+        d_sdofs_.release();
+        d_ssub_.release();
+        d_soff_.release();
+        d_sinvoff_.release();
+        d_sinv_.release();
+        d_sinv32_.release();
+        d_st_.release();
+        mf_ = std::make_unique<MfFactor>();
+        h_sdofs_.clear();
+        h_soff_.assign(1, 0);
+        h_sinvoff_.clear();
+        ndense_ = 0;
+        inv_total_ = 0;
+        if (subs_.empty()) return;
+        d_sdofs_.upload(dofs, stream_);
+        d_ssub_.upload(sub_of, stream_);
+        d_soff_.upload(off, stream_);
+        d_sinvoff_.upload(inv_off, stream_);
+        d_sinv_.resize(std::max<int64_t>(inv_total, 1));
+        d_st_.resize(dofs.size());
+        stiff_.nsub = (int32_t)order.size();
+        stiff_.ndof = (int32_t)dofs.size();
+        stiff_.ndof_dense = off[ndense];
+        stiff_.dofs = d_sdofs_.data();
+        stiff_.sub_of = d_ssub_.data();
+        stiff_.off = d_soff_.data();
+        stiff_.inv_off = d_sinvoff_.data();
+        stiff_.inv = d_sinv_.data();
+        stiff_.t = d_st_.data();
+    }
+    stats_["stiff_layout_reused"] = same ? 1.0 : 0.0;
     d_sinv_.zero(stream_);
-    d_st_.resize(dofs.size());
-    stiff_.nsub = (int32_t)order.size();
-    stiff_.ndof = (int32_t)dofs.size();
-    stiff_.ndof_dense = off[ndense];
-    stiff_.dofs = d_sdofs_.data();
-    stiff_.sub_of = d_ssub_.data();
-    stiff_.off = d_soff_.data();
-    stiff_.inv_off = d_sinvoff_.data();
-    stiff_.inv = d_sinv_.data();
-    stiff_.t = d_st_.data();
     d_bad_.zero(stream_);
     launch_stiff_extract(A_, stiff_, d_sinv_.data(), stream_);
     launch_stiff_invert(stiff_, off.data(), ndense, d_sinv_.data(), d_bad_.data(), stream_);
     if (ndense < stiff_.nsub) {
-        auto t0 = clk::now();
-        const MfSymbolic sym = mf_symbolic(dofs, off, ndense, pat_.rows, pat_.cols, bd);
-        stats_["time_multifrontal_symbolic"] = secs(t0);
-        mf_->setup(sym, stream_);
+        if (!same) {
+            auto t0 = clk::now();
+            const MfSymbolic sym = mf_symbolic(dofs, off, ndense, pat_.rows, pat_.cols, bd);
+            stats_["time_multifrontal_symbolic"] = secs(t0);
+            mf_->setup(sym, stream_);
+        } else {
+            stats_["time_multifrontal_symbolic"] = 0.0;
+        }
         mf_->factorize(A_, stiff_, d_bad_.data(), stream_);
+        const MfSymbolic &sym = mf_->symbolic();
         stats_["multifrontal_fronts"] = sym.nfront;
         stats_["multifrontal_levels"] = sym.levels;
         stats_["multifrontal_max_front"] = sym.max_f;

@@ -103,6 +103,10 @@ private:
     std::vector<int32_t> h_outer_, h_inner_;  // copy of the analysed pattern (adjoint)
     std::vector<int32_t> gmm_sel_;
     std::vector<std::vector<int32_t>> subs_;
+    // the last decomposition (set, size limit, components), reused for the same set
+    std::vector<int32_t> decomp_sel_;
+    int64_t decomp_max_ = -1;
+    std::vector<std::vector<int32_t>> decomp_subs_;
     std::map<std::string, double> stats_;
     std::map<std::string, std::string> sstats_;
 

@@ -79,13 +79,12 @@ __device__ void sweep_invert_small(double *S, int ld, int N, double *col, double
 }
 
 // one CTA per small subdomain (m <= 160), in place in global storage
-__global__ void __launch_bounds__(256) invert_small_kernel(const int32_t *__restrict__ sub_ids,
-                                                           const int32_t *__restrict__ off,
+__global__ void __launch_bounds__(256) invert_small_kernel(const int32_t *__restrict__ off,
                                                            const int64_t *__restrict__ inv_off,
                                                            double *__restrict__ inv, int *bad)
 {
     extern __shared__ double sm[];
-    const int32_t s = sub_ids[blockIdx.x];
+    const int32_t s = blockIdx.x;  // the dense subdomains come first
     const int m = off[s + 1] - off[s], ld = m + 1;
     double *S = sm, *col = sm + m * ld, *scol = col + m;
     double *g = inv + inv_off[s];
@@ -181,10 +180,8 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
                          cudaStream_t s)
 {
     if (nsub == 0) return;
-    std::vector<int32_t> ids(nsub);
     int maxm = 0;
     for (int32_t q = 0; q < nsub; ++q) {
-        ids[q] = q;
         const int m = h_off[q + 1] - h_off[q];
         if (m > STIFF_DENSE_MAX) fail(LSS_ERR_INTERNAL, "a dense stiff block above the shared-memory size");
         maxm = std::max(maxm, m);
@@ -192,11 +189,8 @@ void launch_stiff_invert(const StiffDev &S, const int32_t *h_off, int32_t nsub, 
     // (160 * 161 + 320) doubles = 204 KB of shared memory at most
     const size_t smem = (size_t)(maxm * (maxm + 1) + 2 * maxm) * sizeof(double);
     raise_smem_limit((const void *)invert_small_kernel, smem);
-    DBuf<int32_t> d_ids;
-    d_ids.upload(ids, s);
-    invert_small_kernel<<<(unsigned)nsub, 256, smem, s>>>(d_ids.data(), S.off, S.inv_off, inv, bad);
+    invert_small_kernel<<<(unsigned)nsub, 256, smem, s>>>(S.off, S.inv_off, inv, bad);
     LSS_LAUNCH_CHECK();
-    LSS_CUDA(cudaStreamSynchronize(s));  // d_ids is freed at scope exit
 }
 
 void launch_stiff_to_fp32(int64_t count, const double *src, float *dst, cudaStream_t s)
