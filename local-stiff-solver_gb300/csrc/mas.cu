@@ -338,95 +338,13 @@ __device__ void sweep_invert(double *S, int ld, double *col, double *scol, int *
     }
 }
 
-// The same sweep in double-float on the FP32 pipe, for inverses stored in
-// FP32 (mixed precision): S, col and scol hold (hi, lo) FP32 pairs (8 bytes, as
-// FP64); products are error-free (TwoProd by FMA) plus the cross terms, sums
-// TwoSum-compensated and renormalised, about 2^-47 relative per update --
-// far below the FP32 rounding of the stored result, at a fraction of the FP64
-// pipe's cost (GB300: 2 FP64 FMAs per clock and SM against 128 FP32).  One
-// FP64 division per pivot.
-__device__ __forceinline__ float2 dfp_split(double v)
-{
-    const float h = (float)v;
-    return make_float2(h, (float)(v - (double)h));
-}
-__device__ __forceinline__ float2 dfp_norm(float h, float l)
-{
-    const float s = __fadd_rn(h, l);
-    return make_float2(s, __fsub_rn(l, __fsub_rn(s, h)));
-}
-__device__ __forceinline__ float2 dfp_mul(float2 a, float2 b)
-{
-    const float p = __fmul_rn(a.x, b.x);
-    const float e = __fmaf_rn(a.x, b.x, -p);
-    return dfp_norm(p, __fadd_rn(e, __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x))));
-}
-// a - b
-__device__ __forceinline__ float2 dfp_sub(float2 a, float2 b)
-{
-    const float t = __fsub_rn(a.x, b.x);
-    const float z = __fsub_rn(t, a.x);
-    const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(t, z)), __fsub_rn(-b.x, z));
-    return dfp_norm(t, __fadd_rn(__fsub_rn(a.y, b.y), err));
-}
-
-template <int N>
-__device__ void sweep_invert_df(float2 *S, int ld, float2 *col, float2 *scol, int *bad)
-{
-    constexpr int NE = N * (N + 1) / 2;
-    constexpr int PER = (NE + 255) / 256;
-    const int tid = threadIdx.x;
-    uint32_t tc[PER];
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int e = tid + k * 256;
-        tc[k] = ~0u;
-        if (e < NE) {
-            int t = 0, off = 0;
-            while (off + (N - t) <= e) {
-                off += N - t;
-                ++t;
-            }
-            tc[k] = ((uint32_t)t << 16) | (uint32_t)(t + (e - off));
-        }
-    }
-    for (int p = 0; p < N; ++p) {
-        const float2 pv = S[p * ld + p];
-        const double piv = (double)pv.x + (double)pv.y;
-        const double rpiv = 1.0 / piv;
-        const float2 rp = dfp_split(rpiv);
-        for (int t = tid; t < N; t += 256) {
-            const float2 cv = (t == p) ? make_float2(0.f, 0.f) : (t < p ? S[t * ld + p] : S[p * ld + t]);
-            col[t] = cv;
-            scol[t] = dfp_mul(cv, rp);
-        }
-        if (tid == 0 && (!isfinite(piv) || piv == 0.0)) atomicOr(bad, 1);
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            if (tc[k] == ~0u) continue;
-            const int t = (int)(tc[k] >> 16), c = (int)(tc[k] & 0xffffu);
-            if (t != p && c != p) S[t * ld + c] = dfp_sub(S[t * ld + c], dfp_mul(scol[t], col[c]));
-        }
-        __syncthreads();
-        for (int t = tid; t < N; t += 256) {
-            if (t == p) S[p * ld + p] = dfp_split(-rpiv);
-            else if (t < p) S[t * ld + p] = scol[t];
-            else S[p * ld + t] = scol[t];
-        }
-        __syncthreads();
-    }
-}
-
 template <int BD, typename T, bool BF>
 __global__ void __launch_bounds__(256, 2) mas_invert_kernel(const double *__restrict__ stage, T *__restrict__ out,
                                                          int *bad)
 {
     constexpr int N = 32 * BD, LD = N + 1;
-    constexpr bool DF = std::is_same<T, float>::value;  // FP32 storage: the sweep in double-float
     extern __shared__ double sm[];
     double *S = sm, *col = sm + N * LD, *scol = col + N;
-    float2 *Sp = reinterpret_cast<float2 *>(S);
     const int64_t bank = blockIdx.x;
     const double *src = stage + bank * N * N;
     for (int idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
@@ -434,20 +352,12 @@ __global__ void __launch_bounds__(256, 2) mas_invert_kernel(const double *__rest
         if (r > c) continue;  // the upper triangle is all the sweep uses
         double v = src[(int64_t)r * N + c];
         if (r == c && v == 0.0) v = 1.0;  // padding (MASPreconditioner.cu:779-796)
-        if (DF) Sp[r * LD + c] = dfp_split(v);
-        else S[r * LD + c] = v;
+        S[r * LD + c] = v;
     }
     __syncthreads();
-    if (DF) sweep_invert_df<N>(Sp, LD, reinterpret_cast<float2 *>(col), reinterpret_cast<float2 *>(scol), bad);
-    else sweep_invert<N>(S, LD, col, scol, bad);
-    // the swept entry (i, j), i <= j, as FP64
-    auto entry = [&](int i, int j) -> double {
-        if (DF) {
-            const float2 v = Sp[i * LD + j];
-            return (double)v.x + (double)v.y;
-        }
-        return S[i * LD + j];
-    };
+    sweep_invert<N>(S, LD, col, scol, bad);
+    // the swept entry (i, j), i <= j
+    auto entry = [&](int i, int j) -> double { return S[i * LD + j]; };
     // tiles
     if (BF) {  // FP32 diagonal tiles, BF16 off-diagonal tiles (round to nearest even)
         unsigned char *dst = reinterpret_cast<unsigned char *>(out) + bank * (int64_t)(BD * 17 * 32 * 4 + BD * (BD - 1) / 2 * 2048);

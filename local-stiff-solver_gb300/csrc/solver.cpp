@@ -679,21 +679,21 @@ void HybridSolver::setup_mas()
     d_inv0_.resize(bf ? (size_t)(nparts * mas_.bank_bytes0) : (size_t)(nparts * te * esz));
     d_invc_.resize(std::max<int64_t>(ncoarse, 1) * te * esz);
     d_bad_.zero(stream_);
+    // the dense staging of the Galerkin blocks stays allocated across the
+    // factorizations of a pattern (no cudaMalloc / cudaFree of GBs per step)
     {
         // level 0 (no atomics: every entry comes from its own row)
-        DBuf<double> stage((size_t)nparts * N * N);
-        stage.zero(stream_);
-        launch_mas_assemble0(A_, d_part_of_.data(), d_part_off_.data(), stage.data(), stream_);
-        launch_mas_invert(bd, nparts, stage.data(), d_inv0_.data(), mas_fp32_, d_bad_.data(), stream_, bf);
-        LSS_CUDA(cudaStreamSynchronize(stream_));
+        d_stage0_.resize((size_t)nparts * N * N);
+        d_stage0_.zero(stream_);
+        launch_mas_assemble0(A_, d_part_of_.data(), d_part_off_.data(), d_stage0_.data(), stream_);
+        launch_mas_invert(bd, nparts, d_stage0_.data(), d_inv0_.data(), mas_fp32_, d_bad_.data(), stream_, bf);
     }
     if (ncoarse > 0) {
-        DBuf<double> stage((size_t)ncoarse * N * N);
-        stage.zero(stream_);
-        DBuf<double> partial((size_t)std::max<int64_t>(memb_.nchunk, 1) * bd * bd * 32);
-        launch_mas_assemble_coarse(A_, mas_, d_cmap_.data(), memb_, partial.data(), stage.data(), stream_);
-        launch_mas_invert(bd, ncoarse, stage.data(), d_invc_.data(), mas_fp32_, d_bad_.data(), stream_);
-        LSS_CUDA(cudaStreamSynchronize(stream_));
+        d_stagec_.resize((size_t)ncoarse * N * N);
+        d_stagec_.zero(stream_);
+        d_cpartial_.resize((size_t)std::max<int64_t>(memb_.nchunk, 1) * bd * bd * 32);
+        launch_mas_assemble_coarse(A_, mas_, d_cmap_.data(), memb_, d_cpartial_.data(), d_stagec_.data(), stream_);
+        launch_mas_invert(bd, ncoarse, d_stagec_.data(), d_invc_.data(), mas_fp32_, d_bad_.data(), stream_);
     }
     int bad = 0;
     LSS_CUDA(cudaMemcpyAsync(&bad, d_bad_.data(), sizeof(int), cudaMemcpyDeviceToHost, stream_));

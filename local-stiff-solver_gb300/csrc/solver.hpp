@@ -125,6 +125,7 @@ private:
     std::vector<DBuf<uint8_t>> d_key_, d_ccnt_;
     std::vector<DBuf<int32_t>> d_cbase_;
     DBuf<char> d_inv0_, d_invc_, d_v_, d_u_;
+    DBuf<double> d_stage0_, d_stagec_, d_cpartial_;  // MAS Galerkin staging, kept per pattern
     bool mas_fp32_ = false;
     // stiff blocks
     StiffDev stiff_;
