@@ -662,7 +662,7 @@ def adjoint_measure(seed, local, steps, warmup, fd_budget_s, max_dirs=20):
             return 0.5 * float(((xx - xs) ** 2).sum())
 
     drng = np.random.Generator(np.random.PCG64(7))
-    h = 2.5e-3
+    h = 2e-2
     errs = []
     t_fd = time.perf_counter()
     for _ in range(max_dirs):
@@ -682,7 +682,7 @@ def adjoint_measure(seed, local, steps, warmup, fd_budget_s, max_dirs=20):
             "iterations_forward": info["num_iterations"], "max_subdomain_dofs": info.get("max_subdomain_dofs"),
             "factorize_ms": 1e3 * info.get("time_factorize", 0.0),
             "multifrontal_fronts": info.get("multifrontal_fronts"),
-            "fd_check": {"directions": len(errs), "stencil": "5-point, relative step 2.5e-3",
+            "fd_check": {"directions": len(errs), "stencil": "5-point, relative step 2e-2",
                          "solver": "fp64, relative tolerance 1e-12", "budget_s": fd_budget_s,
                          "worst_rel_err": max(errs) if errs else None,
                          "median_rel_err": float(np.median(errs)) if errs else None},
