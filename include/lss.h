@@ -172,6 +172,16 @@ lss_status lss_partition_pattern(int32_t n, int64_t nnz, const int32_t *outer, c
                                  int32_t block_size, int32_t threads, int32_t *perm, int32_t cap_perm,
                                  int32_t *part_offsets, int32_t cap_offsets, int32_t *nparts);
 
+/* The elimination tree of the multifrontal stiff-block factor for one stiff
+ * subdomain, computed on the host (no device needed): the nested dissection
+ * and front plan the solver builds for a subdomain above the dense size (the
+ * reference's sparse LDL^T via cuDSS, GPUHybrid.cu:1075-1196 / 1248-1249).
+ * dofs: ndofs ascending scalar DOF ids of the pattern (outer index = row).
+ * out[0..3] = fronts, tree levels, largest front (variables), FMAs of the
+ * numeric factorization. */
+lss_status lss_stiff_elimination_tree(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                                      int32_t block_size, const int32_t *dofs, int32_t ndofs, double *out);
+
 /* ---- operator-level entry points (parity tests and benchmarks) ---------- */
 
 /* rn[i] = sum |values| of outer slice i, on the GPU (GPUHybrid.cu:753-765). */

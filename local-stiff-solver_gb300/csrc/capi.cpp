@@ -12,6 +12,7 @@
 
 #include "baddof.hpp"
 #include "batch.hpp"
+#include "multifrontal.hpp"
 #include "noalloc.hpp"
 #include "solver.hpp"
 
@@ -351,6 +352,42 @@ lss_status lss_partition_pattern(int32_t n, int64_t nnz, const int32_t *outer, c
             lss::fail(LSS_ERR_BUFFER_TOO_SMALL, "partition output buffers too small");
         std::memcpy(perm, P.part.perm.data(), P.part.perm.size() * sizeof(int32_t));
         std::memcpy(part_offsets, P.part.part_offsets.data(), P.part.part_offsets.size() * sizeof(int32_t));
+    });
+}
+
+lss_status lss_stiff_elimination_tree(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                                      int32_t block_size, const int32_t *dofs, int32_t ndofs, double *out)
+{
+    if (n <= 0 || nnz < 0 || !outer || !inner || block_size < 1 || n % block_size || !dofs || ndofs <= 0 || !out) {
+        g_create_error = "invalid elimination-tree arguments";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    return guarded(nullptr, [&]() {
+        const int32_t bd = block_size, nb = n / bd;
+        for (int32_t k = 0; k < ndofs; ++k)
+            if (dofs[k] < 0 || dofs[k] >= n || (k > 0 && dofs[k] <= dofs[k - 1]))
+                lss::fail(LSS_ERR_INVALID_ARGUMENT, "dofs must be ascending ids below n");
+        // block pattern (outer index = row, as the solver reads it)
+        std::vector<int32_t> rows{0}, cols, mark(nb, -1);
+        for (int32_t I = 0; I < nb; ++I) {
+            for (int32_t i = I * bd; i < (I + 1) * bd; ++i)
+                for (int64_t e = outer[i]; e < outer[i + 1]; ++e) {
+                    const int32_t J = inner[e] / bd;
+                    if (J < 0 || J >= nb) lss::fail(LSS_ERR_INVALID_ARGUMENT, "inner index out of range");
+                    if (mark[J] != I) {
+                        mark[J] = I;
+                        cols.push_back(J);
+                    }
+                }
+            std::sort(cols.begin() + rows.back(), cols.end());
+            rows.push_back((int32_t)cols.size());
+        }
+        const std::vector<int32_t> d(dofs, dofs + ndofs), off{0, ndofs};
+        const lss::MfSymbolic M = lss::mf_symbolic(d, off, 0, rows, cols, bd);
+        out[0] = M.nfront;
+        out[1] = M.levels;
+        out[2] = M.max_f;
+        out[3] = M.fmas;
     });
 }
 

@@ -823,8 +823,6 @@ void MfFactor::setup(const MfSymbolic &sym, cudaStream_t st)
         });
         make(L.write, lv_large[h], [&](int32_t id) { return (F_of(id) * PW + 255) / 256; });
         make(L.mirror, lv_large[h], [&](int32_t id) { return (F_of(id) * M.s[id] + 255) / 256; });
-        make(L.fwd, lv_all[h], [&](int32_t id) { return std::max<int64_t>(1, (M.u[id] + PW - 1) / PW); });
-        make(L.bwd, lv_all[h], [&](int32_t id) { return (int64_t)(M.s[id] + PW - 1) / PW; });
         make(L.fasm_nr, lv_all[h], [&](int32_t id) { return (F_of(id) + 15) / 16; }, true);
         make(L.fasm1, lv_all[h], [&](int32_t id) { return (F_of(id) + 255) / 256; }, true);
         make(L.fwd_nr, lv_all[h], [&](int32_t id) {

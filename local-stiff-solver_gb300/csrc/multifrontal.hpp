@@ -96,7 +96,7 @@ public:
 
 private:
     struct Level {
-        MfWork ea, small, diag, panel, update, write, mirror, fwd, bwd, fasm_nr, fwd_nr, bwd_nr, fasm1;
+        MfWork ea, small, diag, panel, update, write, mirror, fasm_nr, fwd_nr, bwd_nr, fasm1;
         int32_t max_s_large = 0;
     };
     MfSymbolic sym_;

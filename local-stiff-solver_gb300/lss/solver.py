@@ -40,7 +40,7 @@ EXPORTS = [
     "lss_op_time", "lss_set_memory_cap", "lss_gmm_select_device_noalloc", "lss_solve_batched_device",
     "lss_factorize_batched_device", "lss_op_row_scores", "lss_op_select_bad_dofs", "lss_partition_pattern",
     "lss_batch_create", "lss_batch_destroy", "lss_batch_last_error", "lss_batch_factorize_device",
-    "lss_batch_solve_device", "lss_batch_get_info", "lss_assemble_values_device",
+    "lss_batch_solve_device", "lss_batch_get_info", "lss_assemble_values_device", "lss_stiff_elimination_tree",
 ]
 
 BATCH_RHS = 16
@@ -168,6 +168,20 @@ def partition_pattern(A, block_size: int, threads: int = 0):
     if st != 0:
         raise LssError(st, L.lss_last_error(None).decode())
     return perm[:nb].copy(), offs[:nparts.value + 1].copy()
+
+
+def stiff_elimination_tree(A, block_size: int, dofs) -> dict:
+    """The multifrontal plan for one stiff subdomain (lss_stiff_elimination_tree,
+    host only): fronts, tree levels, largest front, factorization FMAs."""
+    L = load()
+    n, outer, inner, _ = _csc_arrays(A)
+    d = np.ascontiguousarray(np.sort(np.asarray(dofs, np.int32)))
+    out = np.zeros(4, np.float64)
+    st = L.lss_stiff_elimination_tree(n, len(inner), _p(outer, _i32p), _p(inner, _i32p), block_size,
+                                      _p(d, _i32p), len(d), out.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        raise LssError(st, L.lss_last_error(None).decode())
+    return {"fronts": int(out[0]), "levels": int(out[1]), "max_front": int(out[2]), "fmas": float(out[3])}
 
 
 def solve_batched_device(solvers, d_b, d_x, nrhs: int, threads: int = 0) -> np.ndarray:
