@@ -9,9 +9,14 @@
 //                   rank-32 update of the upper-triangle tiles, panel write-back;
 //                   then the swept rows are mirrored into the lower triangle
 // (the original entries are assembled into every front once, before level 0).
-// Solve: one forward launch per level (leaves first), one backward launch per
-// level (root first), one scatter; each output is a fixed-order dot product
-// over a column of the front (coalesced across the 32 outputs of a warp).
+// Solve, per level: a gather extend-add of every front's vector and a forward
+// GEMV launch (leaves first), then one backward GEMV launch per level (root
+// first) and one scatter.  GEMV CTAs take 32 output columns and at most 256
+// of a front's rows; larger fronts split their rows over several CTAs whose
+// partial sums the last CTA of the group adds in a fixed order.  The
+// per-level launches use programmatic dependent launch.  The solve with one
+// right-hand side is FP64; the batched solve with 16 reads the fronts as
+// double-float pairs (below).
 #include <algorithm>
 #include <utility>
 

@@ -14,8 +14,9 @@
 //     [ -F11^-1        F11^-1 F12 ]
 //     [ F21 F11^-1     F22 - F21 F11^-1 F12 ]
 // in place: the pivot block's inverse, the coupling P = F21 F11^-1 and the
-// Schur complement U that the parent sums in.  Everything is FP64.  The solve
-// is one GEMV per front and direction:
+// Schur complement U that the parent sums in.  The factor is FP64 (the
+// batched 16-right-hand-side solve applies it as double-float pairs).  The
+// solve is one GEMV per front and direction:
 //     forward (leaves first):  c = w_bnd - P w_own      (passed to the parent)
 //     backward (root first):   x_own = F11^-1 (w_own - F12 x_bnd)
 // where w_own holds the right-hand side plus the children's contributions.
