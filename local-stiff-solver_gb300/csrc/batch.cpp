@@ -49,6 +49,7 @@ struct BatchSolver::Impl {
     std::vector<DBuf<uint8_t>> key, ccnt;
     std::vector<DBuf<int32_t>> cbase;
     DBuf<float> inv0, invc, v, u;
+    DBuf<float> inv0x;  // level-0 banks as full 96 x 96 matrices (the level-0 apply reads these)
     // stiff
     DBuf<int32_t> sdofs, ssub, soff, front_sys;
     DBuf<int64_t> sinvoff;
@@ -324,7 +325,14 @@ void BatchSolver::merge()
     D.u.resize((size_t)std::max<int64_t>(voff, 1) * BK);
     D.v.zero(st);
     D.u.zero(st);
-    D.M.inv0 = D.inv0.data();
+    // level-0 banks expanded once into full matrices: the apply then copies
+    // them into shared memory as they are, instead of expanding the stored
+    // diagonals on every apply
+    D.inv0x.resize((size_t)np * (32 * BDIM) * (32 * BDIM));
+    bk::launch_expand_banks(D.inv0.data(), D.inv0x.data(), np, st);
+    LSS_CUDA(cudaStreamSynchronize(st));
+    D.inv0.release();
+    D.M.inv0 = D.inv0x.data();
     D.M.invc = D.invc.data();
     D.M.v = D.v.data();
     D.M.u = D.u.data();

@@ -442,21 +442,27 @@ constexpr int XBUF_BYTES = 32 * BD * BK * 8;            // 32 nodes of pairs: 12
 constexpr int STAGE_BYTES = TILE_BYTES + XBUF_BYTES + 512;  // + pad: the partial sums need 25,600
 constexpr int RSTRIDE = NB * BK + 64;                   // partial sums of one column quarter (+ skew)
 constexpr int BANK_SMEM = NB * NB * 4 + 2 * STAGE_BYTES + 16;
+// pre-expanded banks (level 0): a stage holds the full 96 x 96 matrix, then X
+constexpr int FULL_BYTES = NB * NB * 4;                  // 36,864
+constexpr int STAGE_FULL_BYTES = FULL_BYTES + XBUF_BYTES;  // 49,152
+constexpr int BANK_SMEM_FULL = 2 * STAGE_FULL_BYTES + 16;
+static_assert(4 * RSTRIDE * 4 <= STAGE_FULL_BYTES && STAGE_FULL_BYTES % 16 == 0, "full-bank stages");
 static_assert(4 * RSTRIDE * 4 <= STAGE_BYTES, "the partial sums fit in a stage");
 static_assert(STAGE_BYTES % 16 == 0 && TILE_BYTES % 16 == 0, "bulk copies need 16-byte alignment");
 
 struct BankSmem {
-    float *S;            // 96 x 96
-    unsigned char *st;   // 2 stages: tile (TILE_BYTES), then X (XBUF_BYTES)
+    float *S;            // 96 x 96 (stored diagonals expanded here; unused with pre-expanded banks)
+    unsigned char *st;   // 2 stages: the bank's inverse (tiles or the full matrix), then X
     uint64_t *bar;
 };
 
+template <bool FULL>
 __device__ __forceinline__ BankSmem bank_smem(unsigned char *raw)
 {
     BankSmem b;
     b.S = reinterpret_cast<float *>(raw);
-    b.st = raw + NB * NB * 4;
-    b.bar = reinterpret_cast<uint64_t *>(b.st + 2 * STAGE_BYTES);
+    b.st = FULL ? raw : raw + NB * NB * 4;
+    b.bar = reinterpret_cast<uint64_t *>(b.st + 2 * (FULL ? STAGE_FULL_BYTES : STAGE_BYTES));
     return b;
 }
 
@@ -489,6 +495,15 @@ __device__ __forceinline__ void expand_tile(const float *__restrict__ T, float *
         S[qj * NB + qi] = a;
         if (c != c2 || (d != 0 && d != 16)) S[qi * NB + qj] = a;
     }
+}
+
+// stored diagonals -> full column-major matrices, once per factorization
+// (one CTA per bank)
+__global__ void __launch_bounds__(BANK_THREADS) expand_banks_kernel(const float *__restrict__ tiles,
+                                                                    float *__restrict__ full)
+{
+    const int64_t b = blockIdx.x;
+    expand_tile(tiles + b * TILE_FLOATS, full + b * NB * NB, threadIdx.x >> 5, threadIdx.x & 31);
 }
 
 template <typename XT>
@@ -547,10 +562,15 @@ __device__ __forceinline__ float bank_result(const float *__restrict__ R, int ro
 // reads it; thread t takes rows t / 16 + 16 j, right-hand side t % 16).
 // Returns false, with *err set, when a copy did not arrive within the poll
 // limit.
-template <typename XT, typename Job, typename Epi>
+// FULL: the banks were expanded once into full column-major matrices (the
+// layout expand_tile writes), which the copy engine brings instead of the
+// stored diagonals -- twice the bytes, no expansion per apply.
+template <typename XT, bool FULL, typename Job, typename Epi>
 __device__ bool bank_pipeline(unsigned char *raw, int nj, Job job, Epi epi, int *err)
 {
-    const BankSmem sm = bank_smem(raw);
+    constexpr int STG = FULL ? STAGE_FULL_BYTES : STAGE_BYTES;
+    constexpr int MATB = FULL ? FULL_BYTES : TILE_BYTES;
+    const BankSmem sm = bank_smem<FULL>(raw);
     __shared__ int s_fail;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     auto issue = [&](int i, int b) {
@@ -559,10 +579,10 @@ __device__ bool bank_pipeline(unsigned char *raw, int nj, Job job, Epi epi, int 
         int cnt;
         job(i, tile, x, cnt);
         const uint32_t xbytes = (uint32_t)cnt * BD * BK * sizeof(XT);
-        unsigned char *stage = sm.st + b * STAGE_BYTES;
-        mbar_arrive_expect_tx(sm.bar + b, TILE_BYTES + xbytes);
-        bulk_load(stage, tile, TILE_BYTES, sm.bar + b);
-        bulk_load(stage + TILE_BYTES, x, xbytes, sm.bar + b);
+        unsigned char *stage = sm.st + b * STG;
+        mbar_arrive_expect_tx(sm.bar + b, MATB + xbytes);
+        bulk_load(stage, tile, MATB, sm.bar + b);
+        bulk_load(stage + MATB, x, xbytes, sm.bar + b);
     };
     if (t == 0) {
         mbar_init(sm.bar, 1);
@@ -593,11 +613,15 @@ __device__ bool bank_pipeline(unsigned char *raw, int nj, Job job, Epi epi, int 
         const XT *xsrc;
         int cnt;
         job(i, tile, xsrc, cnt);
-        unsigned char *stage = sm.st + b * STAGE_BYTES;
-        expand_tile(reinterpret_cast<const float *>(stage), sm.S, w, lane);
-        __syncthreads();
+        unsigned char *stage = sm.st + b * STG;
+        const float *S = reinterpret_cast<const float *>(stage);
+        if (!FULL) {
+            expand_tile(reinterpret_cast<const float *>(stage), sm.S, w, lane);
+            __syncthreads();
+            S = sm.S;
+        }
         float acc[12][2];
-        bank_mma<XT>(sm.S, reinterpret_cast<const float *>(stage + TILE_BYTES), 3 * cnt, w, lane, acc);
+        bank_mma<XT>(S, reinterpret_cast<const float *>(stage + MATB), 3 * cnt, w, lane, acc);
         __syncthreads();
         float *R = reinterpret_cast<float *>(stage);  // the stage is consumed: partial sums
         bank_store_partials(R, w, lane, acc);
@@ -663,7 +687,7 @@ __global__ void __launch_bounds__(BANK_THREADS) symv_coarse_kernel(MasDev m, con
 #pragma unroll 4
         for (int row = threadIdx.x >> 4; row < NB; row += BANK_THREADS / BK) u[at + row * BK + k] = bank_result(R, row, k);
     };
-    bank_pipeline<float>(smem_raw, nj, job, epi, err);
+    bank_pipeline<float, false>(smem_raw, nj, job, epi, err);
 }
 
 // level 0: z = omega (Inv_0 x + u_1) (+ z with acc), as pairs; optional
@@ -684,7 +708,7 @@ __global__ void __launch_bounds__(BANK_THREADS) symv0_kernel(BatchDev B, MasDev 
     float dh = 0.f, dl = 0.f;
     auto job = [&](int i, const float *&tile, const XT *&x, int &cnt) {
         const int32_t p = ch.p0 + i, lo = m.part_off[p];
-        tile = inv0 + (int64_t)p * TILE_FLOATS;
+        tile = inv0 + (int64_t)p * NB * NB;  // pre-expanded
         x = xin + (int64_t)lo * BD * BK;
         cnt = m.part_off[p + 1] - lo;
     };
@@ -720,7 +744,7 @@ __global__ void __launch_bounds__(BANK_THREADS) symv0_kernel(BatchDev B, MasDev 
             if (DOT) df_fma(dh, dl, rv[j].x, rv[j].y, val.x, val.y);
         }
     };
-    if (!bank_pipeline<XT>(smem_raw, ch.p1 - ch.p0, job, epi, B.err)) return;
+    if (!bank_pipeline<XT, true>(smem_raw, ch.p1 - ch.p0, job, epi, B.err)) return;
     if (DOT) {
         __shared__ double red[BANK_THREADS / BK][BK];
         red[threadIdx.x >> 4][k] = (double)dh + (double)dl;
@@ -1009,10 +1033,11 @@ void launch_mas(const BatchDev &B, const BatchMas &M, const float2 *xin_pair, co
         if (m.L > 2 && m.nitems[1] > 0)
             prolong_kernel<<<(unsigned)(((int64_t)m.nitems[1] * BD * BK + 255) / 256), 256, 0, s>>>(m, M.u);
     }
-#define LSS_B0(XT_, X_, A_, D_)                                                                          \
-    do {                                                                                                 \
-        raise_smem_limit((const void *)symv0_kernel<XT_, A_, D_>, smem);                                 \
-        symv0_kernel<XT_, A_, D_><<<B.nchunk, BANK_THREADS, smem, s>>>(B, m, M.inv0, M.u, X_, z, rdot);  \
+    const size_t smem0 = (size_t)BANK_SMEM_FULL;
+#define LSS_B0(XT_, X_, A_, D_)                                                                           \
+    do {                                                                                                  \
+        raise_smem_limit((const void *)symv0_kernel<XT_, A_, D_>, smem0);                                 \
+        symv0_kernel<XT_, A_, D_><<<B.nchunk, BANK_THREADS, smem0, s>>>(B, m, M.inv0, M.u, X_, z, rdot);  \
     } while (0)
     if (xin_pair) {
         if (acc) {
@@ -1036,6 +1061,13 @@ void launch_mas(const BatchDev &B, const BatchMas &M, const float2 *xin_pair, co
         }
     }
 #undef LSS_B0
+    LSS_LAUNCH_CHECK();
+}
+
+void launch_expand_banks(const float *tiles, float *full, int64_t nbank, cudaStream_t s)
+{
+    if (nbank == 0) return;
+    expand_banks_kernel<<<(unsigned)nbank, BANK_THREADS, 0, s>>>(tiles, full);
     LSS_LAUNCH_CHECK();
 }
 

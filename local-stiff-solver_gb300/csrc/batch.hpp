@@ -70,7 +70,7 @@ struct BatchDev {
 // ccnt = 0.
 struct BatchMas {
     MasDev m;                              // merged level sizes, maps and offsets (pointers into own buffers)
-    const float *inv0 = nullptr, *invc = nullptr;
+    const float *inv0 = nullptr, *invc = nullptr;  // inv0: full 96 x 96 matrices; invc: stored diagonals
     float *v = nullptr, *u = nullptr;      // level vectors, [item * BD + c][BK]
 };
 
@@ -101,6 +101,8 @@ void launch_lane_norms(const BatchDev &B, const double *b, double *bb, cudaStrea
 void launch_mas(const BatchDev &B, const BatchMas &M, const float2 *xin_pair, const float *xin32, float2 *z, bool acc,
                 int dot, const float2 *rdot, cudaStream_t s);
 void launch_residual32(const BatchDev &B, const float2 *r, const float2 *z, float *w, cudaStream_t s);
+// the level-0 banks' stored diagonals expanded into full 96 x 96 column-major matrices
+void launch_expand_banks(const float *tiles, float *full, int64_t nbank, cudaStream_t s);
 // t = r_S - (A z)_S over every stiff DOF; z_S += Inv t over the dense subdomains
 void launch_stiff(const BatchDev &B, const StiffDev &S, const float2 *r, const float2 *z_in, double *t, float2 *z,
                   cudaStream_t s);
