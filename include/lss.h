@@ -182,6 +182,19 @@ lss_status lss_partition_pattern(int32_t n, int64_t nnz, const int32_t *outer, c
 lss_status lss_stiff_elimination_tree(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
                                       int32_t block_size, const int32_t *dofs, int32_t ndofs, double *out);
 
+/* The post-processing of a stiff-DOF selection as the solver runs it, on the
+ * host (no device needed): filter_subdomains (GPUHybrid.cu:885-970; the
+ * Gershgorin sums over the selected submatrix come from `values` here, the
+ * solver forms them on the device), one-ring expansion (:972-991) and the
+ * decomposition into connected components (:691-735), switched and sized by
+ * the "GPUHybrid" parameters of params_json.  sel: nsel ascending scalar
+ * ids (the GMM selection).  Output: the subdomains, each ascending, ordered by
+ * their first DOF: sub_off[nsub + 1] into sub_dofs. */
+lss_status lss_postprocess_selection(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                                     const double *values, const char *params_json, const int32_t *sel,
+                                     int32_t nsel, int32_t *sub_off, int32_t cap_off, int32_t *sub_dofs,
+                                     int32_t cap_dofs, int32_t *nsub);
+
 /* ---- operator-level entry points (parity tests and benchmarks) ---------- */
 
 /* rn[i] = sum |values| of outer slice i, on the GPU (GPUHybrid.cu:753-765). */

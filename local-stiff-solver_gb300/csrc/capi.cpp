@@ -2,6 +2,8 @@
 // into status codes and records the message; nothing here exits the process.
 #include <algorithm>
 #include <atomic>
+#include <climits>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -14,6 +16,7 @@
 #include "batch.hpp"
 #include "multifrontal.hpp"
 #include "noalloc.hpp"
+#include "postproc.hpp"
 #include "solver.hpp"
 
 namespace lss {
@@ -388,6 +391,60 @@ lss_status lss_stiff_elimination_tree(int32_t n, int64_t nnz, const int32_t *out
         out[1] = M.levels;
         out[2] = M.max_f;
         out[3] = M.fmas;
+    });
+}
+
+lss_status lss_postprocess_selection(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                                     const double *values, const char *params_json, const int32_t *sel,
+                                     int32_t nsel, int32_t *sub_off, int32_t cap_off, int32_t *sub_dofs,
+                                     int32_t cap_dofs, int32_t *nsub)
+{
+    if (n <= 0 || nnz < 0 || !outer || !inner || !values || nsel < 0 || (nsel > 0 && !sel) || !nsub) {
+        g_create_error = "invalid post-processing arguments";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    return guarded(nullptr, [&]() {
+        const lss::Params p = lss::parse_params(params_json, lss::Params());
+        std::vector<int32_t> s(sel, sel + nsel);
+        for (int32_t k = 0; k < nsel; ++k)
+            if (s[k] < 0 || s[k] >= n || (k > 0 && s[k] <= s[k - 1]))
+                lss::fail(LSS_ERR_INVALID_ARGUMENT, "sel must be ascending ids below n");
+        const lss::CscView A{n, nnz, outer, inner, nullptr};
+        // the solver's steps after the GMM selection (HybridSolver::select_stiff)
+        if (p.decompose) {
+            // Gershgorin data of the selected submatrix: diagonal entry and the
+            // sum of |a| over the other selected columns of the row
+            std::vector<uint8_t> mask((size_t)n, 0);
+            for (int32_t k : s) mask[k] = 1;
+            std::vector<double> diag(s.size(), 0.0), off(s.size(), 0.0);
+            for (size_t a = 0; a < s.size(); ++a) {
+                const int32_t k = s[a];
+                for (int64_t e = outer[k]; e < outer[k + 1]; ++e) {
+                    const int32_t j = inner[e];
+                    if (j < 0 || j >= n) lss::fail(LSS_ERR_INVALID_ARGUMENT, "inner index out of range");
+                    if (!mask[j]) continue;
+                    if (j == k) diag[a] = values[e];
+                    else off[a] += std::fabs(values[e]);
+                }
+            }
+            s = lss::filter_subdomains(A, s, diag, off, p.min_sub, p.max_sub, p.cond_threshold, nullptr);
+        }
+        if (p.expand && !s.empty()) s = lss::expand_subdomains(A, s);
+        std::vector<std::vector<int32_t>> subs;
+        if (!s.empty()) subs = lss::decompose_subdomains(A, s, p.decompose ? (int64_t)p.max_sub : INT64_MAX);
+        *nsub = (int32_t)subs.size();
+        if (!sub_off || !sub_dofs) return;
+        int64_t total = 0;
+        for (const auto &c : subs) total += (int64_t)c.size();
+        if (cap_off < *nsub + 1 || cap_dofs < total)
+            lss::fail(LSS_ERR_BUFFER_TOO_SMALL, "post-processing output buffers too small");
+        int32_t at = 0;
+        sub_off[0] = 0;
+        for (int32_t q = 0; q < *nsub; ++q) {
+            std::copy(subs[q].begin(), subs[q].end(), sub_dofs + at);
+            at += (int32_t)subs[q].size();
+            sub_off[q + 1] = at;
+        }
     });
 }
 

@@ -41,6 +41,7 @@ EXPORTS = [
     "lss_factorize_batched_device", "lss_op_row_scores", "lss_op_select_bad_dofs", "lss_partition_pattern",
     "lss_batch_create", "lss_batch_destroy", "lss_batch_last_error", "lss_batch_factorize_device",
     "lss_batch_solve_device", "lss_batch_get_info", "lss_assemble_values_device", "lss_stiff_elimination_tree",
+    "lss_postprocess_selection",
 ]
 
 BATCH_RHS = 16
@@ -168,6 +169,28 @@ def partition_pattern(A, block_size: int, threads: int = 0):
     if st != 0:
         raise LssError(st, L.lss_last_error(None).decode())
     return perm[:nb].copy(), offs[:nparts.value + 1].copy()
+
+
+def postprocess_selection(A, params: dict, sel):
+    """The solver's post-processing of a stiff-DOF selection, on the host
+    (lss_postprocess_selection): filter, one-ring expansion, decomposition.
+    params: the "GPUHybrid" parameters.  Returns the subdomains (ascending
+    arrays, ordered by first DOF)."""
+    import json as _json
+    L = load()
+    n, outer, inner, vals = _csc_arrays(A)
+    s = np.ascontiguousarray(np.asarray(sel, np.int32))
+    cfg = _json.dumps({"solver": "GPUHybrid", "GPUHybrid": dict(params)}).encode()
+    nsub = C.c_int32(0)
+    off = np.zeros(n + 1, np.int32)
+    dofs = np.zeros(max(n, 1), np.int32)
+    st = L.lss_postprocess_selection(n, len(inner), _p(outer, _i32p), _p(inner, _i32p),
+                                     vals.ctypes.data_as(C.POINTER(C.c_double)), cfg, _p(s, _i32p), len(s),
+                                     _p(off, _i32p), len(off), _p(dofs, _i32p), len(dofs), C.byref(nsub))
+    if st != 0:
+        raise LssError(st, L.lss_last_error(None).decode())
+    k = nsub.value
+    return [dofs[off[q]:off[q + 1]].copy() for q in range(k)]
 
 
 def stiff_elimination_tree(A, block_size: int, dofs) -> dict:

@@ -148,3 +148,36 @@ def test_reference_build_edge_cases():
     raw, subs, _ = O.ref_select_pipeline(one, {})
     allc, _, _ = O.c_select_pipeline(one, {})
     assert len(raw) == 0 or np.array_equal(np.sort(raw), allc)
+
+
+@pytest.mark.parametrize("key,src,params", _cases())
+def test_product_postprocessing_reproduces_reference_build(key, src, params, built):
+    """The library's own host post-processing (lss_postprocess_selection: the
+    filter with the selected submatrix's Gershgorin sums, the one-ring
+    expansion and the decomposition, as HybridSolver::select_stiff runs them)
+    fed with the reference build's GMM selection gives the reference build's
+    final stiff set and subdomains exactly."""
+    import lss
+    A = _matrix(src)
+    subs = _canonical(lss.postprocess_selection(A, params, REF[key + "/gmm_selection"]))
+    allsel = np.sort(np.concatenate(subs)) if subs else np.zeros(0, np.int32)
+    np.testing.assert_array_equal(allsel, REF[key + "/selected"])
+    if not params.get("decompose_subdomains", True):
+        # The reference factors one block holding every selected DOF; the
+        # library factors its connected components (the same operator, the
+        # inverse being block diagonal over them): the components partition the
+        # reference's block and no entry of A couples two of them.
+        assert len(REF[key + "/sub_offsets"]) == 2
+        comp = np.full(A.shape[0], -1)
+        for q, c in enumerate(subs):
+            comp[c] = q
+        Ac = A.tocsc()
+        for q, c in enumerate(subs):
+            for k in c:
+                rows = Ac.indices[Ac.indptr[k]:Ac.indptr[k + 1]]
+                other = comp[rows]
+                assert np.all((other == -1) | (other == q)), (key, k)
+        return
+    np.testing.assert_array_equal(np.cumsum([0] + [len(s) for s in subs]), REF[key + "/sub_offsets"])
+    got = np.concatenate(subs) if subs else np.zeros(0, np.int32)
+    np.testing.assert_array_equal(got, REF[key + "/sub_dofs"])
