@@ -195,6 +195,17 @@ lss_status lss_postprocess_selection(int32_t n, int64_t nnz, const int32_t *oute
                                      int32_t nsel, int32_t *sub_off, int32_t cap_off, int32_t *sub_dofs,
                                      int32_t cap_dofs, int32_t *nsub);
 
+/* The MAS coarse space the solver builds for a pattern, on the host (no
+ * device needed): MASPreconditioner.cu:376-481 semantics on the partition
+ * of lss_partition_pattern.  *levels = matrix levels including level 0;
+ * items[l] (cap_items >= *levels) = nodes (l = 0) or coarse items of level l;
+ * cmap[(l - 1) * nb + i] (cap_cmap >= (*levels - 1) * nb) = the level-l item
+ * of permuted block row i.  With items == NULL or cmap == NULL only *levels
+ * is written. */
+lss_status lss_coarse_space(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner, int32_t block_size,
+                            int32_t max_coarse_levels, int32_t *levels, int32_t *items, int32_t cap_items,
+                            int32_t *cmap, int64_t cap_cmap);
+
 /* ---- operator-level entry points (parity tests and benchmarks) ---------- */
 
 /* rn[i] = sum |values| of outer slice i, on the GPU (GPUHybrid.cu:753-765). */

@@ -448,6 +448,26 @@ lss_status lss_postprocess_selection(int32_t n, int64_t nnz, const int32_t *oute
     });
 }
 
+lss_status lss_coarse_space(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner, int32_t block_size,
+                            int32_t max_coarse_levels, int32_t *levels, int32_t *items, int32_t cap_items,
+                            int32_t *cmap, int64_t cap_cmap)
+{
+    if (n <= 0 || nnz < 0 || !outer || !inner || block_size < 1 || !levels || max_coarse_levels < 0) {
+        g_create_error = "invalid coarse-space arguments";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    return guarded(nullptr, [&]() {
+        const lss::Pattern P = lss::analyze_pattern(n, nnz, outer, inner, block_size, 0);
+        const lss::CoarseSpace cs = lss::build_coarse_space(P, max_coarse_levels);
+        *levels = cs.L;
+        if (!items || !cmap) return;
+        if (cap_items < cs.L || cap_cmap < (int64_t)cs.cmap.size())
+            lss::fail(LSS_ERR_BUFFER_TOO_SMALL, "coarse-space output buffers too small");
+        for (int l = 0; l < cs.L; ++l) items[l] = l == 0 ? P.nb : cs.nitems[l];
+        std::copy(cs.cmap.begin(), cs.cmap.end(), cmap);
+    });
+}
+
 lss_status lss_op_row_l1_norms(int32_t n, int64_t nnz, const int32_t *outer, const double *values, double *rn)
 {
     if (n <= 0 || nnz < 0 || !outer || !values || !rn) return LSS_ERR_INVALID_ARGUMENT;

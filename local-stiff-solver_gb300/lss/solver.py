@@ -41,7 +41,7 @@ EXPORTS = [
     "lss_factorize_batched_device", "lss_op_row_scores", "lss_op_select_bad_dofs", "lss_partition_pattern",
     "lss_batch_create", "lss_batch_destroy", "lss_batch_last_error", "lss_batch_factorize_device",
     "lss_batch_solve_device", "lss_batch_get_info", "lss_assemble_values_device", "lss_stiff_elimination_tree",
-    "lss_postprocess_selection",
+    "lss_postprocess_selection", "lss_coarse_space",
 ]
 
 BATCH_RHS = 16
@@ -191,6 +191,24 @@ def postprocess_selection(A, params: dict, sel):
         raise LssError(st, L.lss_last_error(None).decode())
     k = nsub.value
     return [dofs[off[q]:off[q + 1]].copy() for q in range(k)]
+
+
+def coarse_space(A, block_size: int, max_coarse_levels: int = 4):
+    """The MAS coarse space of A's pattern (lss_coarse_space, host only):
+    (items per level, [cmap of level l for l = 1 .. L-1] over the permuted
+    block rows)."""
+    L = load()
+    n, outer, inner, _ = _csc_arrays(A)
+    nb = n // block_size
+    lev = C.c_int32(0)
+    items = np.zeros(16, np.int32)
+    cmap = np.zeros(max(16 * nb, 1), np.int32)
+    st = L.lss_coarse_space(n, len(inner), _p(outer, _i32p), _p(inner, _i32p), block_size, max_coarse_levels,
+                            C.byref(lev), _p(items, _i32p), len(items), _p(cmap, _i32p), C.c_int64(len(cmap)))
+    if st != 0:
+        raise LssError(st, L.lss_last_error(None).decode())
+    k = lev.value
+    return items[:k].copy(), [cmap[(l - 1) * nb:l * nb].copy() for l in range(1, k)]
 
 
 def stiff_elimination_tree(A, block_size: int, dofs) -> dict:
