@@ -206,6 +206,19 @@ lss_status lss_coarse_space(int32_t n, int64_t nnz, const int32_t *outer, const 
                             int32_t max_coarse_levels, int32_t *levels, int32_t *items, int32_t cap_items,
                             int32_t *cmap, int64_t cap_cmap);
 
+/* The full plan behind lss_stiff_elimination_tree, for checking it: call
+ * with the arrays NULL to get counts[0..3] = fronts, positions, boundary
+ * entries, child entries; then with arrays of those sizes.  Fronts in
+ * postorder (children first): front f owns positions front_p0[f] ..
+ * + front_s[f] - 1 and couples to the later positions bnd_pos[bnd_off[f] ..
+ * bnd_off[f+1]) (ascending, front_u[f] of them); its children are
+ * child[child_off[f] .. child_off[f+1]); pos2j[p] = the index into dofs of
+ * position p. */
+lss_status lss_stiff_elimination_plan(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                                      int32_t block_size, const int32_t *dofs, int32_t ndofs, int64_t *counts,
+                                      int32_t *front_p0, int32_t *front_s, int32_t *front_u, int32_t *bnd_off,
+                                      int32_t *bnd_pos, int32_t *child_off, int32_t *child, int32_t *pos2j);
+
 /* ---- operator-level entry points (parity tests and benchmarks) ---------- */
 
 /* rn[i] = sum |values| of outer slice i, on the GPU (GPUHybrid.cu:753-765). */

@@ -358,6 +358,63 @@ lss_status lss_partition_pattern(int32_t n, int64_t nnz, const int32_t *outer, c
     });
 }
 
+namespace {
+// the multifrontal plan of one stiff subdomain (dofs ascending) of a pattern
+lss::MfSymbolic elimination_plan(int32_t n, const int32_t *outer, const int32_t *inner, int32_t block_size,
+                                 const int32_t *dofs, int32_t ndofs)
+{
+    const int32_t bd = block_size, nb = n / bd;
+    for (int32_t k = 0; k < ndofs; ++k)
+        if (dofs[k] < 0 || dofs[k] >= n || (k > 0 && dofs[k] <= dofs[k - 1]))
+            lss::fail(LSS_ERR_INVALID_ARGUMENT, "dofs must be ascending ids below n");
+    // block pattern (outer index = row, as the solver reads it)
+    std::vector<int32_t> rows{0}, cols, mark(nb, -1);
+    for (int32_t I = 0; I < nb; ++I) {
+        for (int32_t i = I * bd; i < (I + 1) * bd; ++i)
+            for (int64_t e = outer[i]; e < outer[i + 1]; ++e) {
+                const int32_t J = inner[e] / bd;
+                if (J < 0 || J >= nb) lss::fail(LSS_ERR_INVALID_ARGUMENT, "inner index out of range");
+                if (mark[J] != I) {
+                    mark[J] = I;
+                    cols.push_back(J);
+                }
+            }
+        std::sort(cols.begin() + rows.back(), cols.end());
+        rows.push_back((int32_t)cols.size());
+    }
+    const std::vector<int32_t> d(dofs, dofs + ndofs), off{0, ndofs};
+    return lss::mf_symbolic(d, off, 0, rows, cols, bd);
+}
+}  // namespace
+
+lss_status lss_stiff_elimination_plan(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
+                                      int32_t block_size, const int32_t *dofs, int32_t ndofs, int64_t *counts,
+                                      int32_t *front_p0, int32_t *front_s, int32_t *front_u, int32_t *bnd_off,
+                                      int32_t *bnd_pos, int32_t *child_off, int32_t *child, int32_t *pos2j)
+{
+    if (n <= 0 || nnz < 0 || !outer || !inner || block_size < 1 || n % block_size || !dofs || ndofs <= 0 ||
+        !counts) {
+        g_create_error = "invalid elimination-plan arguments";
+        return LSS_ERR_INVALID_ARGUMENT;
+    }
+    return guarded(nullptr, [&]() {
+        const lss::MfSymbolic M = elimination_plan(n, outer, inner, block_size, dofs, ndofs);
+        counts[0] = M.nfront;
+        counts[1] = M.npos;
+        counts[2] = (int64_t)M.bnd_pos.size();
+        counts[3] = (int64_t)M.child.size();
+        if (!front_p0 || !front_s || !front_u || !bnd_off || !bnd_pos || !child_off || !child || !pos2j) return;
+        std::copy(M.p0.begin(), M.p0.end(), front_p0);
+        std::copy(M.s.begin(), M.s.end(), front_s);
+        std::copy(M.u.begin(), M.u.end(), front_u);
+        std::copy(M.bnd_off.begin(), M.bnd_off.end(), bnd_off);
+        std::copy(M.bnd_pos.begin(), M.bnd_pos.end(), bnd_pos);
+        std::copy(M.child_off.begin(), M.child_off.end(), child_off);
+        std::copy(M.child.begin(), M.child.end(), child);
+        std::copy(M.pos2j.begin(), M.pos2j.end(), pos2j);
+    });
+}
+
 lss_status lss_stiff_elimination_tree(int32_t n, int64_t nnz, const int32_t *outer, const int32_t *inner,
                                       int32_t block_size, const int32_t *dofs, int32_t ndofs, double *out)
 {
@@ -366,27 +423,7 @@ lss_status lss_stiff_elimination_tree(int32_t n, int64_t nnz, const int32_t *out
         return LSS_ERR_INVALID_ARGUMENT;
     }
     return guarded(nullptr, [&]() {
-        const int32_t bd = block_size, nb = n / bd;
-        for (int32_t k = 0; k < ndofs; ++k)
-            if (dofs[k] < 0 || dofs[k] >= n || (k > 0 && dofs[k] <= dofs[k - 1]))
-                lss::fail(LSS_ERR_INVALID_ARGUMENT, "dofs must be ascending ids below n");
-        // block pattern (outer index = row, as the solver reads it)
-        std::vector<int32_t> rows{0}, cols, mark(nb, -1);
-        for (int32_t I = 0; I < nb; ++I) {
-            for (int32_t i = I * bd; i < (I + 1) * bd; ++i)
-                for (int64_t e = outer[i]; e < outer[i + 1]; ++e) {
-                    const int32_t J = inner[e] / bd;
-                    if (J < 0 || J >= nb) lss::fail(LSS_ERR_INVALID_ARGUMENT, "inner index out of range");
-                    if (mark[J] != I) {
-                        mark[J] = I;
-                        cols.push_back(J);
-                    }
-                }
-            std::sort(cols.begin() + rows.back(), cols.end());
-            rows.push_back((int32_t)cols.size());
-        }
-        const std::vector<int32_t> d(dofs, dofs + ndofs), off{0, ndofs};
-        const lss::MfSymbolic M = lss::mf_symbolic(d, off, 0, rows, cols, bd);
+        const lss::MfSymbolic M = elimination_plan(n, outer, inner, block_size, dofs, ndofs);
         out[0] = M.nfront;
         out[1] = M.levels;
         out[2] = M.max_f;

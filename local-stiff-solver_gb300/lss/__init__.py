@@ -7,8 +7,9 @@ reference's linear-solver interface (``lss.Solver``), builds it in-tree
 """
 from .solver import (BATCH_RHS, Batch, LssError, Solver, factorize_batched_device, load,  # noqa: F401
                      partition_pattern, row_l1_norms, select_bad_dofs, solve_batched_device,
-                     stiff_elimination_tree, postprocess_selection, coarse_space)
+                     stiff_elimination_tree, postprocess_selection, coarse_space,
+                     stiff_elimination_plan)
 
 __all__ = ["Solver", "LssError", "load", "row_l1_norms", "solve_batched_device", "factorize_batched_device",
-           "select_bad_dofs", "partition_pattern", "stiff_elimination_tree", "postprocess_selection", "coarse_space", "Batch",
+           "select_bad_dofs", "partition_pattern", "stiff_elimination_tree", "postprocess_selection", "coarse_space", "stiff_elimination_plan", "Batch",
            "BATCH_RHS"]

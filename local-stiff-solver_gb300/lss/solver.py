@@ -41,7 +41,7 @@ EXPORTS = [
     "lss_factorize_batched_device", "lss_op_row_scores", "lss_op_select_bad_dofs", "lss_partition_pattern",
     "lss_batch_create", "lss_batch_destroy", "lss_batch_last_error", "lss_batch_factorize_device",
     "lss_batch_solve_device", "lss_batch_get_info", "lss_assemble_values_device", "lss_stiff_elimination_tree",
-    "lss_postprocess_selection", "lss_coarse_space",
+    "lss_postprocess_selection", "lss_coarse_space", "lss_stiff_elimination_plan",
 ]
 
 BATCH_RHS = 16
@@ -209,6 +209,34 @@ def coarse_space(A, block_size: int, max_coarse_levels: int = 4):
         raise LssError(st, L.lss_last_error(None).decode())
     k = lev.value
     return items[:k].copy(), [cmap[(l - 1) * nb:l * nb].copy() for l in range(1, k)]
+
+
+def stiff_elimination_plan(A, block_size: int, dofs) -> dict:
+    """The full multifrontal plan for one stiff subdomain
+    (lss_stiff_elimination_plan, host only): per front (postorder) its first
+    position, own and boundary counts, boundary positions and children, and
+    pos2j (position -> index into dofs)."""
+    L = load()
+    n, outer, inner, _ = _csc_arrays(A)
+    d = np.ascontiguousarray(np.sort(np.asarray(dofs, np.int32)))
+    counts = np.zeros(4, np.int64)
+    args = [n, len(inner), _p(outer, _i32p), _p(inner, _i32p), block_size, _p(d, _i32p), len(d),
+            counts.ctypes.data_as(C.POINTER(C.c_int64))]
+    st = L.lss_stiff_elimination_plan(*args, *([None] * 8))
+    if st != 0:
+        raise LssError(st, L.lss_last_error(None).decode())
+    nf, npos, nb_, nc = (int(v) for v in counts)
+    arr = {"p0": np.zeros(nf, np.int32), "s": np.zeros(nf, np.int32), "u": np.zeros(nf, np.int32),
+           "bnd_off": np.zeros(nf + 1, np.int32), "bnd_pos": np.zeros(max(nb_, 1), np.int32),
+           "child_off": np.zeros(nf + 1, np.int32), "child": np.zeros(max(nc, 1), np.int32),
+           "pos2j": np.zeros(npos, np.int32)}
+    st = L.lss_stiff_elimination_plan(*args, *[_p(arr[k], _i32p) for k in
+                                               ("p0", "s", "u", "bnd_off", "bnd_pos", "child_off", "child", "pos2j")])
+    if st != 0:
+        raise LssError(st, L.lss_last_error(None).decode())
+    arr["bnd_pos"] = arr["bnd_pos"][:nb_]
+    arr["child"] = arr["child"][:nc]
+    return arr
 
 
 def stiff_elimination_tree(A, block_size: int, dofs) -> dict:
